@@ -1,0 +1,311 @@
+"""Oracle for Pylians' density-field and clustering path: MA, Pk, XPk, Bk on the CPU.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline / reference legs of ``bench.py`` use this module, as the checker
+and as the timed CPU baseline.  The product (``pylians_gb300``) never imports it.
+
+The hot loops are the plain-C restatement in ``pyl_oracle.c`` (mass assignment,
+P(k) mode loop); this file restates the rest in numpy, each part citing the
+reference lines it follows:
+
+  MA()                MAS_library.pyx:57-112 (dispatch, 2D renormalisation)
+  frequencies()       Pk_library.pyx:59-64
+  MAS_function()      Pk_library.pyx:75-81
+  check_number_modes  Pk_library.pyx:90-102
+  FFT3Dr_f/IFFT3Dr_f  Pk_library.pyx:120-133,152-165 (unnormalised, float32)
+  Pk                  Pk_library.pyx:266-425
+  XPk                 Pk_library.pyx:534-798
+  Bk                  bispectrum_library.pyx:32-196
+
+The FFT is ``scipy.fft`` in float32.  The reference's FFT is pyFFTW/FFTW3,
+which is not vendored and is pinned to no version; FFT parity is therefore
+pinned only against scipy.fft (float32) and numpy's float64 FFT, within the
+tolerance each test states.
+
+Interlacing has no counterpart in the reference.  Its oracle is this file's
+``interlace_combine``: the reference mass assignment run on positions shifted
+by half a cell, combined in Fourier space as
+    delta(k) = 1/2 [delta_1(k) + delta_2(k) exp(i pi (kx+ky+kz)/N)]
+(Sefusatti, Crocce, Scoccimarro & Couchman 2016, MNRAS 460, 3624).
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, 'liboracle_pyl.so')
+_lib = None
+
+MAS_INDEX = {'NGP': 1, 'CIC': 2, 'TSC': 3, 'PCS': 4}
+
+
+def build(force=False):
+    """Compile pyl_oracle.c into oracle/liboracle_pyl.so (gcc, OpenMP, no FMA contraction)."""
+    src = os.path.join(HERE, 'pyl_oracle.c')
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+        return _LIB_PATH
+    cmd = ['gcc', '-O2', '-fopenmp', '-ffp-contract=off', '-fPIC', '-shared',
+           src, '-o', _LIB_PATH + '.tmp', '-lm']
+    subprocess.check_call(cmd)
+    os.replace(_LIB_PATH + '.tmp', _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        L.oracle_ma.argtypes = [P, ctypes.c_int64, ctypes.c_int, P, ctypes.c_int, ctypes.c_float,
+                                ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
+        L.oracle_ma.restype = ctypes.c_int
+        L.oracle_pk_modes.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int] + [P] * 12
+        L.oracle_pk_modes.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+# --------------------------------------------------------------------------- MA
+def ma_kernel(pos, number, BoxSize, MAS, W=None, threads=1, flavor=0):
+    """One deposit pass (no 2D renormalisation).  flavor 0: MAS_library.pyx kernels;
+    flavor 1: MAS_c.c kernels (threads>1 uses OpenMP atomics as MAS_c.c does)."""
+    assert pos.dtype == np.float32 and pos.flags.c_contiguous
+    assert number.dtype == np.float32 and number.flags.c_contiguous
+    ndim = pos.shape[1]
+    assert number.ndim == ndim
+    w = None
+    if W is not None:
+        w = np.ascontiguousarray(W, dtype=np.float32)
+        assert w.shape[0] == pos.shape[0]
+    rc = lib().oracle_ma(_ptr(pos), pos.shape[0], ndim, _ptr(number), number.shape[0],
+                         float(BoxSize), MAS_INDEX[MAS], _ptr(w), int(threads), int(flavor))
+    if rc:
+        raise ValueError('oracle_ma failed (%d)' % rc)
+
+
+def MA(pos, number, BoxSize, MAS='CIC', W=None, renormalize_2D=True, threads=1):
+    """MAS_library.MA (MAS_library.pyx:57-112): accumulate into ``number`` in place."""
+    if pos.shape[1] != number.ndim:
+        raise ValueError('pos have %d dimensions and the density %d' % (pos.shape[1], number.ndim))
+    if MAS not in MAS_INDEX:
+        raise ValueError('option not valid: MAS=%r' % (MAS,))
+    ma_kernel(pos, number, BoxSize, MAS, W, threads=threads, flavor=0)
+    if number.ndim == 2 and renormalize_2D and MAS != 'NGP':
+        number /= {'CIC': 2.0, 'TSC': 3.0, 'PCS': 4.0}[MAS]
+
+
+# ------------------------------------------------------------------ P(k) pieces
+def frequencies(BoxSize, dims):
+    kF = 2.0 * np.pi / BoxSize
+    middle = dims // 2
+    kN = middle * kF
+    kmax_par = middle
+    kmax_per = int(np.sqrt(middle ** 2 + middle ** 2))
+    kmax = int(np.sqrt(middle ** 2 + middle ** 2 + middle ** 2))
+    return kF, kN, kmax_par, kmax_per, kmax
+
+
+def MAS_function(MAS):
+    return MAS_INDEX.get(MAS, 0)
+
+
+def check_number_modes(Nmodes, dims):
+    own = 1 if dims % 2 == 1 else 8
+    indep = (dims ** 3 - own) // 2 + own
+    if int(np.sum(Nmodes)) != indep:
+        raise RuntimeError('Not all modes counted: %d vs %d' % (int(np.sum(Nmodes)), indep))
+
+
+def fft_r2c(delta, threads=1):
+    import scipy.fft
+    return scipy.fft.rfftn(np.asarray(delta, dtype=np.float32), workers=max(1, threads))
+
+
+def fft_c2r(dk, dims, threads=1):
+    import scipy.fft
+    return scipy.fft.irfftn(np.asarray(dk, dtype=np.complex64), s=(dims,) * 3, norm='forward',
+                            workers=max(1, threads))
+
+
+def interlace_combine(dk1, dk2):
+    """1/2 [dk1 + dk2 exp(i pi (kx+ky+kz)/N)] on the half-complex grid, phase in float64."""
+    dims = dk1.shape[0]
+    k = np.fft.fftfreq(dims, 1.0 / dims)
+    kz = np.arange(dims // 2 + 1)
+    ph = np.pi / dims * (k[:, None, None] + k[None, :, None] + kz[None, None, :])
+    out = 0.5 * (dk1.astype(np.complex128) + dk2.astype(np.complex128) * np.exp(1j * ph))
+    return out.astype(np.complex64)
+
+
+def pk_mode_sums(dk_fields, axis, mas_p, threads=1):
+    """Raw per-bin sums of the Pk/XPk mode loop.  ``dk_fields`` is modified (MAS-corrected)."""
+    F = len(dk_fields)
+    dims = dk_fields[0].shape[0]
+    kF, kN, kmax_par, kmax_per, kmax = frequencies(1.0, dims)
+    nb1, nb2, nb3 = kmax_par + 1, (kmax_par + 1) * (kmax_per + 1), kmax + 1
+    X = F * (F - 1) // 2
+    dk = np.ascontiguousarray(np.stack(dk_fields).astype(np.complex64))
+    z = lambda *s: np.zeros(s, np.float64)
+    out = dict(k1D=z(nb1), Nmodes1D=z(nb1), Pk1D=z(nb1, F), PkX1D=z(nb1, max(X, 1)),
+               Nmodes2D=z(nb2), Pk2D=z(nb2, F), PkX2D=z(nb2, max(X, 1)),
+               k3D=z(nb3), Nmodes3D=z(nb3), Pk3D=z(nb3, 3, F), PkX3D=z(nb3, 3, max(X, 1)),
+               Pkphase=z(nb3, F))
+    mp = np.asarray(mas_p, dtype=np.int32)
+    names = ['k1D', 'Nmodes1D', 'Pk1D', 'PkX1D', 'Nmodes2D', 'Pk2D', 'PkX2D',
+             'k3D', 'Nmodes3D', 'Pk3D', 'PkX3D', 'Pkphase']
+    rc = lib().oracle_pk_modes(_ptr(dk), F, dims, int(axis), _ptr(mp), int(threads),
+                               *[_ptr(out[n]) for n in names])
+    if rc:
+        raise RuntimeError('oracle_pk_modes failed (%d)' % rc)
+    out['delta_k'] = dk
+    return out
+
+
+class _Result(object):
+    pass
+
+
+def finalize_pk(s, BoxSize, dims, F, cross=False):
+    """Finalisation of Pk (Pk_library.pyx:384-421) and XPk (:740-796) in float64."""
+    kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+    fact = (BoxSize / dims ** 2) ** 3
+    X = F * (F - 1) // 2
+    r = _Result()
+    with np.errstate(divide='ignore', invalid='ignore'):
+        k1D = s['k1D'][1:].copy(); N1 = s['Nmodes1D'][1:].copy()
+        k1D = (k1D / N1) * kF
+        kmaxper = np.sqrt(kN ** 2 - k1D ** 2)
+        area = (np.pi * kmaxper ** 2 / N1) / (2.0 * np.pi) ** 2
+        Pk1D = s['Pk1D'][1:] * fact * area[:, None]
+        PkX1D = s['PkX1D'][1:, :X] * fact * area[:, None]
+        ip = np.arange(kmax_par + 1); iq = np.arange(kmax_per + 1)
+        kpar = np.zeros((kmax_par + 1) * (kmax_per + 1)); kper = np.zeros_like(kpar)
+        idx = (kmax_par + 1) * iq[None, :] + ip[:, None]
+        kpar[idx] = (0.5 * (ip + ip + 1) * kF)[:, None]
+        kper[idx] = (0.5 * (iq + iq + 1) * kF)[None, :]
+        N2 = s['Nmodes2D']
+        Pk2D = s['Pk2D'] * fact / N2[:, None]
+        PkX2D = s['PkX2D'][:, :X] * fact / N2[:, None]
+        check_number_modes(s['Nmodes3D'], dims)
+        N3 = s['Nmodes3D'][1:].copy()
+        k3D = (s['k3D'][1:] / N3) * kF
+        P3 = s['Pk3D'][1:].copy()
+        P3[:, 0] = (P3[:, 0] / N3[:, None]) * fact
+        P3[:, 1] = (P3[:, 1] * 5.0 / N3[:, None]) * fact
+        P3[:, 2] = (P3[:, 2] * 9.0 / N3[:, None]) * fact
+        X3 = s['PkX3D'][1:, :, :X].copy()
+        X3[:, 0] = (X3[:, 0] / N3[:, None]) * fact
+        X3[:, 1] = (X3[:, 1] * 5.0 / N3[:, None]) * fact
+        X3[:, 2] = (X3[:, 2] * 9.0 / N3[:, None]) * fact
+        ph = (s['Pkphase'][1:] / N3[:, None]) * fact
+    r.k1D, r.Nmodes1D = k1D, N1
+    r.kpar, r.kper, r.Nmodes2D = kpar, kper, N2.copy()
+    r.k3D, r.Nmodes3D = k3D, N3
+    if cross:
+        r.Pk1D, r.PkX1D, r.Pk2D, r.PkX2D = Pk1D, PkX1D, Pk2D, PkX2D
+        r.Pk, r.XPk = P3, X3
+    else:
+        r.Pk1D, r.Pk2D, r.Pk, r.Pkphase = Pk1D[:, 0], Pk2D[:, 0], P3[:, :, 0], ph[:, 0]
+    return r
+
+
+def Pk(delta, BoxSize, axis=2, MAS='CIC', threads=1, keep_deltak=False, interlaced=None):
+    """Pk_library.Pk (Pk_library.pyx:266-425); ``interlaced`` is the half-cell-shifted grid."""
+    dims = delta.shape[0]
+    dk = fft_r2c(delta, threads)
+    if interlaced is not None:
+        dk = interlace_combine(dk, fft_r2c(interlaced, threads))
+    s = pk_mode_sums([dk], axis, [MAS_function(MAS)], threads)
+    r = finalize_pk(s, BoxSize, dims, 1)
+    if keep_deltak:
+        r.delta_k = s['delta_k'][0]
+    return r
+
+
+def XPk(delta, BoxSize, axis=2, MAS=None, threads=1, interlaced=None):
+    """Pk_library.XPk (Pk_library.pyx:534-798)."""
+    F = len(delta)
+    dims = delta[0].shape[0]
+    for d in delta[1:]:
+        if d.shape[0] != dims:
+            raise ValueError('Fields have different grid sizes')
+    dks = [fft_r2c(d, threads) for d in delta]
+    if interlaced is not None:
+        dks = [interlace_combine(a, fft_r2c(b, threads)) for a, b in zip(dks, interlaced)]
+    s = pk_mode_sums(dks, axis, [MAS_function(m) for m in MAS], threads)
+    return finalize_pk(s, BoxSize, dims, F, cross=True)
+
+
+# -------------------------------------------------------------------- bispectrum
+def mas_factor_grid(dims, MAS):
+    """float32 MAS factor on the half-complex grid: (float)(C(kx) C(ky) C(kz)), C in float64."""
+    p = MAS_function(MAS)
+    middle = dims // 2
+    k = np.arange(dims); k = np.where(k > middle, k - dims, k)
+    x = (np.pi / dims) * k
+    with np.errstate(divide='ignore', invalid='ignore'):
+        c = np.where(x == 0.0, 1.0, (x / np.sin(x)) ** p)
+    cz = c[:middle + 1]
+    return ((c[:, None, None] * c[None, :, None]) * cz[None, None, :]).astype(np.float32)
+
+
+def mode_k2(dims):
+    middle = dims // 2
+    k = np.arange(dims); k = np.where(k > middle, k - dims, k).astype(np.int64)
+    kz = np.arange(middle + 1, dtype=np.int64)
+    return k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+
+
+def Bk(delta, BoxSize, k1, k2, theta, MAS='CIC', threads=1):
+    """Pk_library.Bk (bispectrum_library.pyx:32-196)."""
+    dims = delta.shape[0]
+    kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+    theta = np.asarray(theta, dtype=np.float64)
+    bins = theta.shape[0]
+    k3 = np.sqrt((k2 * np.sin(theta)) ** 2 + (k2 * np.cos(theta) + k1) ** 2)
+    k_all = np.zeros(bins + 2); k_all[0] = k1; k_all[1] = k2; k_all[2:] = k3
+    k_min = (k_all - kF) / kF
+    k_max = (k_all + kF) / kF
+    dk = fft_r2c(delta, threads)
+    mf = mas_factor_grid(dims, MAS)
+    dk = (dk.real * mf + 1j * (dk.imag * mf)).astype(np.complex64)
+    kk = np.sqrt(mode_k2(dims).astype(np.float64))
+
+    def shell(i):
+        m = (kk >= k_min[i]) & (kk < k_max[i])
+        d = np.where(m, dk, 0).astype(np.complex64)
+        I = m.astype(np.complex64)
+        return fft_c2r(d, dims, threads), fft_c2r(I, dims, threads)
+
+    fact_p = (BoxSize / dims ** 2) ** 3
+    fact_b = (BoxSize ** 2 / dims ** 3) ** 3
+    Pk = np.zeros(bins + 2)
+    B = np.zeros(bins); Q = np.zeros(bins)
+    d1, I1 = shell(0)
+    Pk[0] = np.sum((d1 * d1).astype(np.float64)) / np.sum((I1 * I1).astype(np.float64)) * fact_p
+    d2, I2 = shell(1)
+    Pk[1] = np.sum((d2 * d2).astype(np.float64)) / np.sum((I2 * I2).astype(np.float64)) * fact_p
+    d12 = d1 * d2
+    I12 = I1 * I2
+    for j in range(bins):
+        d3, I3 = shell(j + 2)
+        Pk[j + 2] = (np.sum((d3 * d3).astype(np.float64)) /
+                     np.sum((I3 * I3).astype(np.float64))) * fact_p
+        B[j] = (np.sum((d12 * d3).astype(np.float64)) / np.sum((I12 * I3).astype(np.float64))) * fact_b
+        Q[j] = B[j] / (Pk[0] * Pk[1] + Pk[0] * Pk[j + 2] + Pk[1] * Pk[j + 2])
+    r = _Result()
+    r.B, r.Q, r.k, r.Pk = B, Q, k_all, Pk
+    return r
+
+
+if __name__ == '__main__':
+    print(build(force='--force' in sys.argv))

@@ -1,0 +1,163 @@
+"""Pins the oracle (oracle/pyl_oracle.c + oracle/oracle.py) to the reference's own outputs.
+
+The fixtures in tests/golden were produced by the compiled reference
+(tests/golden/make_golden.py).  Tolerances:
+  * NGP / NGPW grids, Nmodes*, kpar/kper: bit-exact;
+  * CIC/TSC/PCS grids: |diff| <= 2e-6 * max|grid| (the reference is built with
+    -ffast-math -march=native, so its compiler may fuse a multiply into the grid
+    update; the oracle never does);
+  * P(k)/XPk/B(k) from the same float32 input: relative 1e-9 (only the FFT
+    library differs: scipy.fft float32 here, FFTW float32 in the reference).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import oracle as O
+
+MAS_LIST = ['NGP', 'CIC', 'TSC', 'PCS']
+
+
+@pytest.fixture(scope='module')
+def ma():
+    return np.load(os.path.join(GOLDEN, 'ma_golden.npz'))
+
+
+@pytest.fixture(scope='module')
+def pk():
+    return np.load(os.path.join(GOLDEN, 'pk_golden.npz'))
+
+
+@pytest.fixture(scope='module')
+def bk():
+    return np.load(os.path.join(GOLDEN, 'bk_golden.npz'))
+
+
+def _grid_close(a, b, mas):
+    if mas == 'NGP':
+        np.testing.assert_array_equal(a, b)
+    else:
+        assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('weighted', [False, True])
+def test_ma_conservation(ma, mas, weighted):
+    """Test/test_MAS.py:10-84: sum(grid)/N == 1 (NGP to 20 places, others to 8)."""
+    pos = ma['conservation_pos']
+    W = np.full(pos.shape[0], 3.0, np.float32) if weighted else None
+    d = np.zeros((64, 64, 64), np.float32)
+    O.MA(pos, d, 1.0, mas, W=W)
+    s = np.sum(d, dtype=np.float64)
+    ref = float(ma['conservation_sum_%s%s' % (mas, 'W' if weighted else '')])
+    norm = 3.0 * pos.shape[0] if weighted else pos.shape[0]
+    assert round(s / norm - 1.0, 20 if mas == 'NGP' else 8) == 0
+    if mas == 'NGP':
+        assert s == ref
+    else:
+        assert abs(s - ref) <= 1e-8 * norm
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('tag', ['', 'W'])
+def test_ma_grids(ma, mas, tag):
+    pos, W = ma['grid_pos'], ma['grid_W']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    w = W if tag else None
+    d = np.zeros((N, N, N), np.float32)
+    O.MA(pos, d, L, mas, W=w)
+    _grid_close(d, ma['MA3D_%s%s' % (mas, tag)], mas)
+    d2 = np.zeros((N, N), np.float32)
+    O.MA(np.ascontiguousarray(pos[:, :2]), d2, L, mas, W=w)
+    _grid_close(d2, ma['MA2D_%s%s' % (mas, tag)], mas)
+    c = np.zeros((N, N, N), np.float32)
+    O.ma_kernel(pos, c, L, mas, w, threads=1, flavor=1)
+    _grid_close(c, ma['MASc3D_%s%s' % (mas, tag)], mas)
+
+
+def test_ma_accumulates(ma):
+    pos = ma['grid_pos']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    d = ma['accum_base'].copy()
+    O.MA(pos, d, L, 'NGP')
+    np.testing.assert_array_equal(d, ma['accum_NGP'])
+
+
+def test_ma_openmp_matches_serial(ma):
+    pos = ma['grid_pos']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    a = np.zeros((N, N, N), np.float32)
+    b = np.zeros((N, N, N), np.float32)
+    O.ma_kernel(pos, a, L, 'NGP', None, threads=1, flavor=1)
+    O.ma_kernel(pos, b, L, 'NGP', None, threads=4, flavor=1)
+    np.testing.assert_array_equal(a, b)
+
+
+def _cmp_attr(x, y, name):
+    x = np.asarray(x); y = np.asarray(y)
+    assert x.shape == y.shape, name
+    if name.startswith('Nmodes') or name in ('kpar', 'kper'):
+        np.testing.assert_array_equal(x, y, err_msg=name)
+    else:
+        scale = np.abs(y).max() if y.size else 1.0
+        np.testing.assert_allclose(x, y, rtol=1e-9, atol=1e-9 * scale, err_msg=name)
+
+
+@pytest.mark.parametrize('N', [32, 15])
+@pytest.mark.parametrize('axis', [0, 1, 2])
+def test_pk(pk, N, axis):
+    r = O.Pk(pk['delta_%d' % N], 1000.0, axis, 'CIC', 1)
+    for name in ['k1D', 'Pk1D', 'Nmodes1D', 'kpar', 'kper', 'Pk2D', 'Nmodes2D',
+                 'k3D', 'Pk', 'Nmodes3D', 'Pkphase']:
+        _cmp_attr(getattr(r, name), pk['Pk_%d_axis%d_%s' % (N, axis, name)], name)
+
+
+@pytest.mark.parametrize('N', [32, 15])
+def test_xpk(pk, N):
+    fields = [pk['delta_%d' % N], pk['delta2_%d' % N], pk['delta3_%d' % N]]
+    r = O.XPk(fields, 1000.0, 1, ['CIC', 'PCS', 'NGP'], 1)
+    for name in ['k1D', 'Pk1D', 'PkX1D', 'Nmodes1D', 'kpar', 'kper', 'Pk2D', 'PkX2D',
+                 'Nmodes2D', 'k3D', 'Pk', 'XPk', 'Nmodes3D']:
+        _cmp_attr(getattr(r, name), pk['XPk_%d_%s' % (N, name)], name)
+
+
+def test_pk_threads_match(pk):
+    d = pk['delta_32']
+    a = O.Pk(d, 1000.0, 2, 'CIC', 1)
+    b = O.Pk(d, 1000.0, 2, 'CIC', 4)
+    np.testing.assert_array_equal(a.Nmodes3D, b.Nmodes3D)
+    np.testing.assert_allclose(a.Pk, b.Pk, rtol=1e-12)
+
+
+def test_bk(bk):
+    N, L, k1, k2 = bk['meta']
+    r = O.Bk(bk['delta'], L, k1, k2, bk['theta'], 'CIC', 1)
+    for n in ('B', 'Q', 'k', 'Pk'):
+        np.testing.assert_allclose(getattr(r, n), bk['Bk_' + n], rtol=1e-9, err_msg=n)
+    e = O.Bk(bk['delta'], L, 0.1, 0.1, np.array([2 * np.pi / 3]), 'CIC', 1)
+    for n in ('B', 'Q', 'k', 'Pk'):
+        np.testing.assert_allclose(getattr(e, n), bk['Bkeq_' + n], rtol=1e-9, err_msg=n)
+
+
+def test_interlace_phase_reduces_aliasing():
+    """Interlacing (no reference counterpart): the combined field's NGP/CIC P(k) of a
+    uniform random catalogue approaches the shot noise 1/nbar near the Nyquist frequency,
+    while the non-interlaced one overshoots it (aliasing of the shot noise)."""
+    rng = np.random.default_rng(3)
+    N, L = 32, 1000.0
+    pos = (rng.random((N ** 3, 3)) * L).astype(np.float32)
+    h = L / N
+    pos2 = np.mod(pos + np.float32(0.5 * h), np.float32(L)).astype(np.float32)
+    a = np.zeros((N, N, N), np.float32); O.MA(pos, a, L, 'CIC')
+    b = np.zeros((N, N, N), np.float32); O.MA(pos2, b, L, 'CIC')
+    m = np.mean(a, dtype=np.float64)
+    a = (a / m - 1).astype(np.float32); b = (b / m - 1).astype(np.float32)
+    plain = O.Pk(a, L, 0, 'CIC', 1)
+    inter = O.Pk(a, L, 0, 'CIC', 1, interlaced=b)
+    shot = L ** 3 / pos.shape[0]
+    sel = (plain.k3D > 0.6 * np.pi / h) & (plain.k3D < 0.9 * np.pi / h)
+    err_plain = np.abs(np.mean(plain.Pk[sel, 0]) / shot - 1)
+    err_inter = np.abs(np.mean(inter.Pk[sel, 0]) / shot - 1)
+    assert err_inter < err_plain
