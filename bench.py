@@ -1,0 +1,329 @@
+"""Benchmark: CIC + interlaced P(k) of 1024^3 particles on a 1024^3 grid, one GB300.
+
+One step = the whole particle -> P(k) chain on one batch of synthetic particles
+already resident in HBM: zero both grids, CIC deposit into the grid and its
+half-cell-shifted twin, overdensity (mean = N/dims^3), batched R2C of both
+grids, fused interlace + deconvolve + |k|/mu binning + l=0,2,4 sums.
+  value  particles/s over K device-timed steps (CUDA events, max over ranks)
+  e2e    the same chain through ParticlePk with the positions copied from pinned
+         host memory every step and the float64 bin sums read back every step
+  roofline   the dominant stage's algorithmic bytes / its CUDA-event duration
+  cpu_baseline   the oracle (C restatement of the reference's MAS_c.c scatter and
+         Pk mode loop, scipy float32 FFT) on all host cores, on a 256^3 sample
+--impl reference: the same CPU port timed as the reference arm.
+
+Inputs (12.9 GB of positions) are larger than L2 (129 MB), so no flush is needed
+between steps.  Synthetic data: uniform positions in a 1000 Mpc/h box, seed 1.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'CIC+interlaced P(k) particles/s'
+UNIT = 'particles/s'
+BOX = 1000.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--grid', type=int, default=1024)
+    ap.add_argument('--particles-side', type=int, default=1024)
+    ap.add_argument('--cpu-side', type=int, default=256, help='side of the CPU baseline sample')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_chain(pos, dims, threads):
+    """The reference's CPU path on `pos`: MAS_c.c-style OpenMP CIC into two grids,
+    overdensity, float32 FFTs, the Pk mode loop (oracle restatement)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    n = pos.shape[0]
+    a = np.zeros((dims,) * 3, np.float32)
+    b = np.zeros((dims,) * 3, np.float32)
+    O.ma_kernel(pos, a, BOX, 'CIC', None, threads=threads, flavor=1)
+    pos2 = (pos + np.float32(0.5 * BOX / dims)).astype(np.float32)
+    O.ma_kernel(pos2, b, BOX, 'CIC', None, threads=threads, flavor=1)
+    m = np.float32(n / dims ** 3)
+    a /= m; a -= np.float32(1)
+    b /= m; b -= np.float32(1)
+    return O.Pk(a, BOX, 0, 'CIC', threads, interlaced=b)
+
+
+def cpu_sample(side, seed=1):
+    rng = np.random.default_rng(seed)
+    return (rng.random((side ** 3, 3), dtype=np.float32) * np.float32(BOX)).astype(np.float32)
+
+
+def run_cpu_baseline(side):
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    pos = cpu_sample(side)
+    cpu_chain(pos[: min(len(pos), 4096)], 16, threads)   # warm the library
+    t0 = time.perf_counter()
+    cpu_chain(pos, side, threads)
+    dt = time.perf_counter() - t0
+    return dict(value=pos.shape[0] / dt, unit=UNIT, cores=threads, kind='port',
+                sample='%d^3 particles CIC+interlaced onto %d^3 grids + P(k) axis 0 (%.2f s)'
+                % (side, side, dt))
+
+
+def reference_arm(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    side = a.cpu_side
+    pos = cpu_sample(side)
+    for _ in range(a.warmup):
+        cpu_chain(pos, side, threads)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        cpu_chain(pos, side, threads)
+    dt = time.perf_counter() - t0
+    v = pos.shape[0] * a.steps / dt
+    line = dict(metric=METRIC, value=v, unit=UNIT, n_gpus=world, steps=a.steps, warmup=a.warmup,
+                ms_per_step=dt / a.steps * 1e3, higher_is_better=True, scaling='weak',
+                vs_baseline=None, dtype='f32', data='synthetic',
+                config=dict(workload='cic_interlaced_pk_cpu_sample_%d^3_particles_%d^3_grid' % (side, side),
+                            box_mpc_h=BOX, axis=0, MAS='CIC', interlaced=True),
+                impl='reference',
+                cpu_baseline=dict(value=v, unit=UNIT, cores=threads, kind='port',
+                                  sample='%d^3 particles onto %d^3 grids per step' % (side, side)),
+                e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------- clocks
+class ClockSampler(object):
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, 'gpurun_out', 'clocks_bench.csv')
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.QUERY,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in open(self.path):
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return dict(sm_mhz=float(np.median(sm)), sm_max_mhz=mx, reasons=sorted(reasons),
+                    samples=len(sm))
+
+
+# -------------------------------------------------------------------- GPU arm
+def main():
+    a = parse()
+    if a.impl == 'reference':
+        return reference_arm(a)
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    import pylians_gb300.build as pb
+    pb.build()
+    from pylians_gb300.pipeline import ParticlePk
+    from pylians_gb300 import _lib
+
+    dims, side = a.grid, a.particles_side
+    n = side ** 3
+    dev = torch.device('cuda', local)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1 + rank)
+    pos = torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float32) * BOX
+    pp = ParticlePk(dims, BOX, 'CIC', axis=0, interlaced=True, strategy='auto', max_particles=n)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(a.warmup):
+        pp.step(pos)
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(); torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.steps):
+        pp.step(pos)
+    e1.record()
+    torch.cuda.synchronize(); barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    value = n * a.steps * world / (ms / 1e3)
+    res = pp.result()
+    assert int(res.Nmodes3D.sum()) + 1 == (dims ** 3 - 8) // 2 + 8
+
+    # ---- per-stage durations (events between C-ABI calls on the launching stream)
+    stages = stage_times(pp, pos, reps=max(2, min(a.steps, 5)))
+
+    # ---- end to end: pinned host positions -> device -> chain -> sums to host
+    e2e = None
+    if not a.no_e2e:
+        host = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        host.copy_(pos)
+        sums_host = torch.empty(pp.sums.shape, dtype=torch.float64, pin_memory=True)
+        dpos = torch.empty_like(pos)
+        for _ in range(1):
+            dpos.copy_(host, non_blocking=True); pp.step(dpos); sums_host.copy_(pp.sums, non_blocking=True)
+        torch.cuda.synchronize(); barrier()
+        k2 = a.steps
+        e0.record()
+        for _ in range(k2):
+            dpos.copy_(host, non_blocking=True)
+            pp.step(dpos)
+            sums_host.copy_(pp.sums, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize(); barrier()
+        ms2 = e0.elapsed_time(e1)
+        e2e = dict(value=n * k2 * world / (ms2 / 1e3), unit=UNIT,
+                   h2d_bytes_per_step=int(host.numel() * 4),
+                   d2h_bytes_per_step=int(sums_host.numel() * 8), ms_per_step=ms2 / k2)
+        del host, dpos
+
+    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
+        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    roof = roofline(stages, n, dims, hbm, 'measured' if 'hbm_gbs' in peaks else 'fallback')
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cpu = run_cpu_baseline(a.cpu_side)
+
+    if rank == 0:
+        line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=a.steps,
+                    warmup=a.warmup, ms_per_step=ms / a.steps, higher_is_better=True,
+                    scaling='weak', vs_baseline=None, dtype='f32', data='synthetic',
+                    config=dict(workload='cic_interlaced_pk_np%d^3_grid%d^3' % (side, dims),
+                                particles=n, grid=dims, box_mpc_h=BOX, axis=0, MAS='CIC',
+                                interlaced=True, strategy='auto', parallelism='replicas',
+                                l2_flush='inputs larger than L2 (12.9 GB positions)'),
+                    e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
+                    gpu_launches=KERNELS_PER_STEP * a.steps, stages_ms=stages)
+        print(json.dumps(line))
+
+
+# our kernels per step: tile count, scan, scatter, deposit, 2 overdensity, bin
+KERNELS_PER_STEP = 7
+
+
+def stage_times(pp, pos, reps):
+    import torch
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr, stream_ptr
+    d = pp.dims
+    n = pos.shape[0]
+    cells = d ** 3
+    st = stream_ptr()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    acc = np.zeros(5)
+    for _ in range(reps):
+        ev[0].record()
+        pp.grids.zero_()
+        ev[1].record()
+        _lib.call('pyl_ma', ptr(pos), None, n, 3, ptr(pp.grids[0]), ptr(pp.grids[1]), d, pp.BoxSize,
+                  _lib.MAS_INDEX[pp.MAS], _lib.STRATEGY[pp.strategy], 0, ptr(pp.ws), pp.ws_bytes, st)
+        ev[2].record()
+        for i in range(2):
+            _lib.call('pyl_overdensity', ptr(pp.grids[i]), cells, None, float(n) / cells, st)
+        ev[3].record()
+        _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, 2, st)
+        ev[4].record()
+        _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]), 1, pp.dk[0].numel(), d, pp.axis,
+                  pp.mas_p, ptr(pp.sums), None, 0, st)
+        ev[5].record()
+        torch.cuda.synchronize()
+        acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]
+    acc /= reps
+    return dict(zero=acc[0], scatter=acc[1], overdensity=acc[2], fft_r2c=acc[3], pk_bin=acc[4])
+
+
+def roofline(stages, n, dims, hbm, src):
+    """Algorithmic HBM bytes per launch of each stage:
+    scatter: 12 B/particle read + 2 grids x 4 B/cell written;
+    overdensity: 2 grids x 8 B/cell; fft_r2c: 2 x (4 B/cell + 8 B/mode);
+    pk_bin: 2 fields x 8 B/mode."""
+    cells = dims ** 3
+    modes = dims * dims * (dims // 2 + 1)
+    alg = dict(scatter=12.0 * n + 2 * 4.0 * cells, overdensity=2 * 8.0 * cells,
+               fft_r2c=2 * (4.0 * cells + 8.0 * modes), pk_bin=2 * 8.0 * modes,
+               zero=2 * 4.0 * cells)
+    top = max((k for k in alg if k != 'zero'), key=lambda k: stages[k])
+    achieved = alg[top] / (stages[top] / 1e3) / 1e9
+    return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
+                frac=achieved / hbm, traffic=None, peak_source=src,
+                alg_bytes=alg[top], ms=stages[top],
+                all_stages={k: dict(ms=stages[k], gbs=alg[k] / (stages[k] / 1e3) / 1e9)
+                            for k in alg})
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,160 @@
+/*
+ * pylians_gb300 — C-ABI of the GB300 (sm_103a) density-field and clustering path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns a
+ * status code (0 = success) and never exits the process or traps the GPU.  All
+ * buffers are owned by the caller and live on the device unless the parameter
+ * name says `host_`.  `stream` is a cudaStream_t (NULL = legacy default stream);
+ * every call is stream-ordered and asynchronous unless documented otherwise.
+ * The library itself owns only its cached cuFFT plans (and their workspaces),
+ * released by pyl_fft_cache_clear().
+ *
+ * Each entry point names the reference interface it replaces
+ * (franciscovillaescusa/Pylians, path:line).
+ */
+#ifndef PYLIANS_GB300_H
+#define PYLIANS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define PYL_OK 0
+#define PYL_ERR_INVALID 1     /* bad argument (shape, size, enum, null pointer) */
+#define PYL_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define PYL_ERR_CUFFT 3       /* a cuFFT call failed */
+#define PYL_ERR_WORKSPACE 4   /* workspace smaller than *_workspace_size() */
+#define PYL_ERR_UNSUPPORTED 5 /* valid request this build does not implement */
+
+/* mass-assignment schemes: the reference's MAS_function indices (Pk_library.pyx:75-81) */
+#define PYL_MAS_NONE 0
+#define PYL_MAS_NGP 1
+#define PYL_MAS_CIC 2
+#define PYL_MAS_TSC 3
+#define PYL_MAS_PCS 4
+
+/* scatter strategies for pyl_ma */
+#define PYL_STRATEGY_AUTO 0   /* library picks by grid size and particle count */
+#define PYL_STRATEGY_ATOMIC 1 /* one thread per particle, atomics into the grid */
+#define PYL_STRATEGY_TILED 2  /* bin particles by tile, deposit tiles in shared memory */
+#define PYL_STRATEGY_SORTED 3 /* stable sort by tile + fixed-order deposit: bit-reproducible */
+
+const char *pyl_strerror(int status);
+/* Detail of the last failure on the calling host thread ("" if none). */
+const char *pyl_last_error(void);
+int pyl_version(void);
+
+/* ---- mass assignment --------------------------------------------------------
+ * Replaces MAS_library.MA (library/MAS_library/MAS_library.pyx:57-112) and the
+ * kernels it dispatches to: NGP/NGPW (:273-325), CIC/CICW (:123-216),
+ * TSC/TSCW (:369-452), PCS/PCSW (:463-545); also MAS_c.c NGP/CIC/TSC/PCS
+ * (library/MAS_library/MAS_c.c:8-266) behind NGPc3D..PCSWc2D (:1136-1221).
+ *
+ * pos      float32 [n_particles][ndim], C-contiguous, ndim = 2 or 3
+ * weights  float32 [n_particles] or NULL (W=None)
+ * grid     float32 [dims]^ndim, row-major; ACCUMULATED into (+=), as MA does
+ * grid_interlaced  NULL, or a second grid that receives the same particles
+ *          shifted by +half a cell on every axis (float32 x + 0.5*BoxSize/dims);
+ *          no counterpart in the reference (interlacing).
+ * renormalize_2d   for ndim == 2: divide the whole grid by 2/3/4 after a
+ *          CIC/TSC/PCS deposit, as MA's renormalize_2D=True does (:84-110).
+ * Cell indices wrap periodically; positions outside [0, BoxSize) are wrapped,
+ * never written out of bounds.  NGP counts (W=NULL) are bit-exact.
+ */
+size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims, int mas, int strategy,
+                             int interlaced);
+int pyl_ma(const float *pos, const float *weights, int64_t n_particles, int ndim,
+           float *grid, float *grid_interlaced, int dims, float box_size, int mas,
+           int strategy, int renormalize_2d, void *workspace, size_t workspace_bytes,
+           void *stream);
+
+/* ---- overdensity --------------------------------------------------------------
+ * Replaces the callers' normalisation `delta /= mean; delta -= 1.0`
+ * (library/Pk_library/Pk_snapshot.py:80-88, documentation/Documentation.md:93).
+ * pyl_grid_sum writes the float64 sum of n float32 values into *d_sum (device).
+ * pyl_overdensity applies delta = x / mean - 1 in float32, with mean = *d_sum / n
+ * (d_sum != NULL) or mean = host_mean (d_sum == NULL).
+ */
+int pyl_grid_sum(const float *grid, int64_t n, double *d_sum, void *stream);
+int pyl_overdensity(float *grid, int64_t n, const double *d_sum, double host_mean,
+                    void *stream);
+
+/* ---- FFT ---------------------------------------------------------------------
+ * Replaces FFT3Dr_f / IFFT3Dr_f (library/Pk_library/Pk_library.pyx:120-133,152-165):
+ * unnormalised single-precision R2C (forward) and C2R (backward) of `batch`
+ * contiguous dims^3 grids.  Complex layout: complex64 [dims][dims][dims/2+1].
+ * pyl_fft_c2r overwrites its input (cuFFT multi-dimensional C2R does).
+ */
+int pyl_fft_r2c(const float *in, void *out_c64, int dims, int batch, void *stream);
+int pyl_fft_c2r(void *in_c64, float *out, int dims, int batch, void *stream);
+int pyl_fft_cache_clear(void);
+
+/* ---- power spectrum -----------------------------------------------------------
+ * Replaces the mode loops of Pk (library/Pk_library/Pk_library.pyx:311-381) and
+ * XPk (:625-737).  One read of F half-complex fields; MAS deconvolution
+ * (x/sin x)^p per axis, optional interlacing combine, |k| / k_par / k_per
+ * binning and Legendre l=0,2,4 sums, all without writing a k-grid.
+ *
+ * Channels: C = F + F(F-1)/2 — the F autos, then the cross pairs (i<j) in the
+ * reference's order.  Bin counts: nb1 = dims/2+1, nb2 = (dims/2+1)*(kmax_per+1),
+ * nb3 = kmax+1 (frequencies(), :59-64).  `sums` (device, float64, zeroed by
+ * the call) receives, in order:
+ *   P3   [nb3][3][C]   sum |d|^2 * L_l(mu), l = 0,2,4
+ *   PH   [nb3][F]      sum phase^2, phase = atan2(Re d, |d|)
+ *   P1   [nb1][C]      sum |d|^2 over |k| <= dims/2, by |k_par|
+ *   P2   [nb2][C]      sum |d|^2 by (kmax_par+1)*k_per + |k_par|
+ * pyl_pk_sums_len() returns that length.  `dk_interlaced` is NULL or the
+ * half-cell-shifted partners of the F fields; then each field is
+ * 1/2 [d1 + d2 exp(i pi (kx+ky+kz)/dims)] before deconvolution.
+ * `field_stride` is the distance between consecutive fields in complex elements.
+ *
+ * pyl_pk_geometry fills the data-independent part (device, float64, zeroed):
+ *   K1 [nb1] sum |k_par|, N1 [nb1], N2 [nb2], K3 [nb3] sum |k|, N3 [nb3]
+ * (mode counts are exact integers stored as float64).
+ */
+int64_t pyl_pk_sums_len(int dims, int n_fields);
+int64_t pyl_pk_geometry_len(int dims);
+size_t pyl_pk_workspace_size(int dims, int n_fields, int axis);
+int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_fields, int64_t field_stride,
+               int dims, int axis, const int *host_mas_p, double *sums, void *workspace,
+               size_t workspace_bytes, void *stream);
+int pyl_pk_geometry(int dims, int axis, double *geom, void *stream);
+
+/* In place: d <- (interlace-combined d) * W(k)^-1 as float32, on every stored
+ * mode (Pk_library.pyx:353-355; bispectrum_library.pyx:107-109).  This is the
+ * delta_k the reference keeps with keep_deltak=True. */
+int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p, void *stream);
+
+/* ---- bispectrum ---------------------------------------------------------------
+ * Replaces Bk (library/Pk_library/bispectrum_library.pyx:32-196).
+ * Shell s holds the modes with host_k2_lo[s] <= kx^2+ky^2+kz^2 < host_k2_hi[s]
+ * (the integer form of  k_min <= |k| < k_max  in units of kF, :73-77,116-118).
+ * pyl_bk_shell_fill reads the deconvolved half-complex field once and writes,
+ * for each shell, delta_s (complex64) and the indicator I_s (1+0i) half grids at
+ * out_delta + s*half, out_ind + s*half (half = dims*dims*(dims/2+1)), and
+ * power[2*s] = sum_x delta_s(x)^2 / dims^3, power[2*s+1] = sum_x I_s(x)^2 / dims^3
+ * (float64, via Parseval on the Hermitian half grid; zeroed by the call).
+ * At most PYL_BK_MAX_SHELLS shells per call.
+ *
+ * pyl_bk_triangles reduces the C2R'd real fields: for triangle t with shells
+ * (a,b,c) = host_tri[3t..3t+2], num[t] = sum_x d_a d_b d_c and
+ * den[t] = sum_x I_a I_b I_c (float64, zeroed by the call) over dims^3 cells;
+ * d_fields / i_fields are float32, shell s at offset s*field_stride elements
+ * (field_stride >= dims^3, a multiple of 4; buffers 16-byte aligned).
+ */
+#define PYL_BK_MAX_SHELLS 96
+int pyl_bk_shell_fill(const void *dk, int dims, const int64_t *host_k2_lo,
+                      const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
+                      double *power, void *stream);
+int pyl_bk_triangles(const float *d_fields, const float *i_fields, int dims, int64_t field_stride,
+                     int n_shells, const int *host_tri, int n_tri, double *num, double *den,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYLIANS_GB300_H */

@@ -1,0 +1,388 @@
+"""Drop-in for Pylians' Pk_library (power spectra and bispectrum) on the GPU.
+
+Mirrors library/Pk_library/Pk_library.pyx and bispectrum_library.pyx:
+  frequencies(BoxSize, dims)                          Pk_library.pyx:59-64
+  MAS_function(MAS)                                   :75-81
+  check_number_modes(Nmodes, dims)                    :90-102
+  FFT3Dr_f(a, threads) / IFFT3Dr_f(a, threads)        :120-133, :152-165
+  Pk(delta, BoxSize, axis=2, MAS='CIC', threads=1, keep_deltak=False)   :266-425
+      -> k1D, Pk1D, Nmodes1D, kpar, kper, Pk2D, Nmodes2D, k3D, Pk, Pkphase, Nmodes3D
+  XPk(delta, BoxSize, axis=2, MAS=None, threads=1)    :534-798
+      -> k1D, Pk1D, PkX1D, Nmodes1D, kpar, kper, Pk2D, PkX2D, Nmodes2D, k3D, Pk, XPk, Nmodes3D
+  Bk(delta, BoxSize, k1, k2, theta, MAS='CIC', threads=1)   bispectrum_library.pyx:32-196
+      -> B, Q, k, Pk
+
+The mode loops run in libpylgpu.so (one read of each half-complex field, no
+k-grid materialised); only the O(bins) finalisation below runs on the host,
+in float64, with the reference's formulas.  `threads` is accepted and ignored.
+Differences: check_number_modes raises RuntimeError instead of sys.exit();
+keyword-only `interlaced=` takes the half-cell-shifted grid(s) produced by
+MAS_library.MA(..., interlaced=...).  Inputs may be numpy arrays or CUDA tensors.
+"""
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._device import as_device_c64, as_device_f32, is_torch, ptr, require_cuda, stream_ptr
+
+__all__ = ['frequencies', 'MAS_function', 'check_number_modes', 'FFT3Dr_f', 'IFFT3Dr_f',
+           'Pk', 'XPk', 'Bk', 'Bk_triangles', 'pk_sums_device', 'finalize_pk', 'geometry']
+
+
+def frequencies(BoxSize, dims):
+    kF = 2.0 * np.pi / BoxSize
+    middle = dims // 2
+    kN = middle * kF
+    kmax_par = middle
+    kmax_per = int(np.sqrt(middle ** 2 + middle ** 2))
+    kmax = int(np.sqrt(middle ** 2 + middle ** 2 + middle ** 2))
+    return kF, kN, kmax_par, kmax_per, kmax
+
+
+def MAS_function(MAS):
+    return _lib.MAS_INDEX.get(MAS, 0)
+
+
+def check_number_modes(Nmodes, dims):
+    own = 1 if dims % 2 == 1 else 8
+    indep = (dims ** 3 - own) // 2 + own
+    counted = int(np.sum(Nmodes))
+    if counted != indep:
+        raise RuntimeError('Not all modes counted: counted %d independent modes, expected %d'
+                           % (counted, indep))
+
+
+def _half_shape(dims):
+    return (dims, dims, dims // 2 + 1)
+
+
+def FFT3Dr_f(a, threads=1):
+    """Unnormalised float32 R2C of a dims^3 grid -> complex64 (dims, dims, dims//2+1)."""
+    require_cuda()
+    x = as_device_f32(a, 'a')
+    dims = x.shape[0]
+    out = torch.empty(_half_shape(dims), dtype=torch.complex64, device=x.device)
+    _lib.call('pyl_fft_r2c', ptr(x), ptr(out), dims, 1, stream_ptr())
+    return out if is_torch(a) else out.cpu().numpy()
+
+
+def IFFT3Dr_f(a, threads=1):
+    """Unnormalised float32 C2R of a (dims, dims, dims//2+1) complex64 grid."""
+    require_cuda()
+    x = as_device_c64(a, 'a').clone()     # cuFFT C2R overwrites its input
+    dims = x.shape[0]
+    out = torch.empty((dims,) * 3, dtype=torch.float32, device=x.device)
+    _lib.call('pyl_fft_c2r', ptr(x), ptr(out), dims, 1, stream_ptr())
+    return out if is_torch(a) else out.cpu().numpy()
+
+
+# --------------------------------------------------------------- geometry cache
+_GEOM = {}
+
+
+def geometry(dims, axis, device=None):
+    """Data-independent per-bin sums (mode counts, sum |k|, sum |k_par|) for a grid and
+    line of sight, computed once on the device and cached like an FFT plan."""
+    dev = device if device is not None else torch.cuda.current_device()
+    key = (str(dev), dims, axis)
+    g = _GEOM.get(key)
+    if g is None:
+        L = _lib.load()
+        n = L.pyl_pk_geometry_len(dims)
+        t = torch.empty(n, dtype=torch.float64, device=dev)
+        _lib.call('pyl_pk_geometry', dims, axis, ptr(t), stream_ptr())
+        g = t.cpu().numpy()
+        _GEOM[key] = g
+    return g
+
+
+def _split_geometry(g, dims):
+    _, _, kmax_par, kmax_per, kmax = frequencies(1.0, dims)
+    nb1, nb2, nb3 = kmax_par + 1, (kmax_par + 1) * (kmax_per + 1), kmax + 1
+    o = np.cumsum([0, nb1, nb1, nb2, nb3, nb3])
+    return dict(K1=g[o[0]:o[1]], N1=g[o[1]:o[2]], N2=g[o[2]:o[3]], K3=g[o[3]:o[4]], N3=g[o[4]:o[5]])
+
+
+def _split_sums(s, dims, F):
+    _, _, kmax_par, kmax_per, kmax = frequencies(1.0, dims)
+    nb1, nb2, nb3 = kmax_par + 1, (kmax_par + 1) * (kmax_per + 1), kmax + 1
+    C = F + F * (F - 1) // 2
+    o = np.cumsum([0, nb3 * 3 * C, nb3 * F, nb1 * C, nb2 * C])
+    return dict(P3=s[o[0]:o[1]].reshape(nb3, 3, C), PH=s[o[1]:o[2]].reshape(nb3, F),
+                P1=s[o[2]:o[3]].reshape(nb1, C), P2=s[o[3]:o[4]].reshape(nb2, C))
+
+
+def pk_sums_device(dk, dims, axis, mas_list, dk_interlaced=None, out=None, stream=None):
+    """Launch the fused deconvolve+bin kernel on F stacked half-complex fields
+    (complex64 tensor [F, dims, dims, dims//2+1]); returns the float64 sums tensor."""
+    F = dk.shape[0]
+    L = _lib.load()
+    n = L.pyl_pk_sums_len(dims, F)
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=dk.device)
+    mp, keep = ctypes_int_array(mas_list)
+    fstride = dims * dims * (dims // 2 + 1)
+    _lib.call('pyl_pk_bin', ptr(dk), ptr(dk_interlaced), F, fstride, dims, axis, mp, ptr(out),
+              None, 0, stream_ptr(stream))
+    del keep
+    return out
+
+
+def ctypes_int_array(vals):
+    import ctypes
+    arr = (ctypes.c_int * len(vals))(*[int(v) for v in vals])
+    return ctypes.cast(arr, ctypes.c_void_p), arr
+
+
+class _Result(object):
+    pass
+
+
+def finalize_pk(sums, geom, BoxSize, dims, F, cross):
+    """Host float64 finalisation: Pk_library.pyx:384-421 (Pk) and :740-796 (XPk)."""
+    kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+    fact = (BoxSize / dims ** 2) ** 3
+    X = F * (F - 1) // 2
+    s = _split_sums(sums, dims, F)
+    g = _split_geometry(geom, dims)
+    r = _Result()
+    with np.errstate(divide='ignore', invalid='ignore'):
+        N1 = g['N1'][1:].copy()
+        k1D = (g['K1'][1:] / N1) * kF
+        kmaxper = np.sqrt(kN ** 2 - k1D ** 2)
+        area = (np.pi * kmaxper ** 2 / N1) / (2.0 * np.pi) ** 2
+        P1 = s['P1'][1:] * fact * area[:, None]
+        ip = np.arange(kmax_par + 1)
+        iq = np.arange(kmax_per + 1)
+        kpar = np.zeros((kmax_par + 1) * (kmax_per + 1))
+        kper = np.zeros_like(kpar)
+        idx = (kmax_par + 1) * iq[None, :] + ip[:, None]
+        kpar[idx] = (0.5 * (ip + ip + 1) * kF)[:, None]
+        kper[idx] = (0.5 * (iq + iq + 1) * kF)[None, :]
+        N2 = g['N2'].copy()
+        P2 = s['P2'] * fact / N2[:, None]
+        check_number_modes(g['N3'], dims)
+        N3 = g['N3'][1:].copy()
+        k3D = (g['K3'][1:] / N3) * kF
+        P3 = s['P3'][1:].copy()
+        P3[:, 0] = (P3[:, 0] / N3[:, None]) * fact
+        P3[:, 1] = (P3[:, 1] * 5.0 / N3[:, None]) * fact
+        P3[:, 2] = (P3[:, 2] * 9.0 / N3[:, None]) * fact
+        PH = (s['PH'][1:] / N3[:, None]) * fact
+    r.k1D, r.Nmodes1D = k1D, N1
+    r.kpar, r.kper, r.Nmodes2D = kpar, kper, N2
+    r.k3D, r.Nmodes3D = k3D, N3
+    if cross:
+        r.Pk1D, r.PkX1D = np.ascontiguousarray(P1[:, :F]), np.ascontiguousarray(P1[:, F:F + X])
+        r.Pk2D, r.PkX2D = np.ascontiguousarray(P2[:, :F]), np.ascontiguousarray(P2[:, F:F + X])
+        r.Pk, r.XPk = np.ascontiguousarray(P3[:, :, :F]), np.ascontiguousarray(P3[:, :, F:F + X])
+    else:
+        r.Pk1D, r.Pk2D = P1[:, 0].copy(), P2[:, 0].copy()
+        r.Pk, r.Pkphase = np.ascontiguousarray(P3[:, :, 0]), PH[:, 0].copy()
+    return r
+
+
+def _fields_to_dk(deltas, device):
+    dims = deltas[0].shape[0]
+    F = len(deltas)
+    dk = torch.empty((F,) + _half_shape(dims), dtype=torch.complex64, device=device)
+    for i, d in enumerate(deltas):
+        x = as_device_f32(d, 'delta')
+        if tuple(x.shape) != (dims,) * 3:
+            raise ValueError('Fields have different grid sizes!!!')
+        _lib.call('pyl_fft_r2c', ptr(x), ptr(dk[i]), dims, 1, stream_ptr())
+    return dk
+
+
+class Pk(object):
+    def __init__(self, delta, BoxSize, axis=2, MAS='CIC', threads=1, keep_deltak=False, *,
+                 interlaced=None, verbose=False):
+        require_cuda()
+        start = time.time()
+        if axis not in (0, 1, 2):
+            raise ValueError('axis must be 0, 1 or 2')
+        dims = delta.shape[0]
+        dev = torch.device('cuda', torch.cuda.current_device())
+        dk = _fields_to_dk([delta], dev)
+        dk2 = _fields_to_dk([interlaced], dev) if interlaced is not None else None
+        p = MAS_function(MAS)
+        mp = ctypes_int_array([p])
+        s = torch.empty(_lib.load().pyl_pk_sums_len(dims, 1), dtype=torch.float64, device=dev)
+        _lib.call('pyl_pk_bin', ptr(dk), ptr(dk2), 1, dk[0].numel(), dims, axis, mp[0], ptr(s),
+                  None, 0, stream_ptr())
+        geom = geometry(dims, axis)
+        r = finalize_pk(s.cpu().numpy(), geom, BoxSize, dims, 1, cross=False)
+        self.__dict__.update(r.__dict__)
+        if keep_deltak:
+            _lib.call('pyl_mas_deconvolve', ptr(dk[0]), ptr(dk2), dims, p, stream_ptr())
+            self.delta_k = dk[0] if is_torch(delta) else dk[0].cpu().numpy()
+        if verbose:
+            print('Time taken = %.2f seconds' % (time.time() - start))
+
+
+class XPk(object):
+    def __init__(self, delta, BoxSize, axis=2, MAS=None, threads=1, *, interlaced=None,
+                 verbose=False):
+        require_cuda()
+        start = time.time()
+        if axis not in (0, 1, 2):
+            raise ValueError('axis must be 0, 1 or 2')
+        F = len(delta)
+        if MAS is None or len(MAS) != F:
+            raise ValueError('XPk needs one MAS per field')
+        dims = delta[0].shape[0]
+        dev = torch.device('cuda', torch.cuda.current_device())
+        dk = _fields_to_dk(list(delta), dev)
+        dk2 = _fields_to_dk(list(interlaced), dev) if interlaced is not None else None
+        mas_p = [MAS_function(m) for m in MAS]
+        geom = geometry(dims, axis)
+        if F <= 4:
+            s = pk_sums_device(dk, dims, axis, mas_p, dk2)
+            r = finalize_pk(s.cpu().numpy(), geom, BoxSize, dims, F, cross=True)
+        else:
+            r = self._pairwise(dk, dk2, dims, axis, mas_p, geom, BoxSize)
+        self.__dict__.update(r.__dict__)
+        if verbose:
+            print('Time taken = %.2f seconds' % (time.time() - start))
+
+    @staticmethod
+    def _pairwise(dk, dk2, dims, axis, mas_p, geom, BoxSize):
+        """More than 4 fields: one 2-field launch per pair (i<j); field i's auto spectra
+        come from its first pair."""
+        F = dk.shape[0]
+        X = F * (F - 1) // 2
+        out, x = None, 0
+        for i in range(F):
+            for j in range(i + 1, F):
+                pair = torch.stack([dk[i], dk[j]])
+                pair2 = torch.stack([dk2[i], dk2[j]]) if dk2 is not None else None
+                s = pk_sums_device(pair, dims, axis, [mas_p[i], mas_p[j]], pair2)
+                r = finalize_pk(s.cpu().numpy(), geom, BoxSize, dims, 2, cross=True)
+                if out is None:
+                    out = _Result()
+                    for k in ('k1D', 'Nmodes1D', 'kpar', 'kper', 'Nmodes2D', 'k3D', 'Nmodes3D'):
+                        setattr(out, k, getattr(r, k))
+                    nb3, nb1, nb2 = r.Pk.shape[0], r.Pk1D.shape[0], r.Pk2D.shape[0]
+                    out.Pk, out.XPk = np.zeros((nb3, 3, F)), np.zeros((nb3, 3, X))
+                    out.Pk1D, out.PkX1D = np.zeros((nb1, F)), np.zeros((nb1, X))
+                    out.Pk2D, out.PkX2D = np.zeros((nb2, F)), np.zeros((nb2, X))
+                for f, c in ((i, 0), (j, 1)):
+                    if (f == i and j == i + 1) or (f == j and i == 0):
+                        out.Pk[:, :, f] = r.Pk[:, :, c]
+                        out.Pk1D[:, f] = r.Pk1D[:, c]
+                        out.Pk2D[:, f] = r.Pk2D[:, c]
+                out.XPk[:, :, x] = r.XPk[:, :, 0]
+                out.PkX1D[:, x] = r.PkX1D[:, 0]
+                out.PkX2D[:, x] = r.PkX2D[:, 0]
+                x += 1
+        return out
+
+
+# ------------------------------------------------------------------ bispectrum
+def shell_k2_bounds(k_min, k_max):
+    """Exact integer bounds [lo, hi) on kx^2+ky^2+kz^2 for k_min <= sqrt(k2) < k_max, with
+    sqrt the correctly rounded float64 square root the reference compares (:115-117)."""
+    def first_at_least(x):
+        if x <= 0.0:
+            return 0
+        c = max(0, int(math.floor(x * x)) - 2)
+        while np.sqrt(np.float64(c)) < x:
+            c += 1
+        while c > 0 and np.sqrt(np.float64(c - 1)) >= x:
+            c -= 1
+        return c
+    return first_at_least(k_min), first_at_least(k_max)
+
+
+def _bk_fields(dk, dims, bounds):
+    """Shell fill + C2R for a list of shells; returns real delta_s, I_s fields and
+    the Parseval sums (sum_x delta_s^2 / N^3, sum_x I_s^2 / N^3)."""
+    S = len(bounds)
+    dev = dk.device
+    half = dims * dims * (dims // 2 + 1)
+    cells = dims ** 3
+    stride = (cells + 3) // 4 * 4
+    d_real = torch.empty(S * stride, dtype=torch.float32, device=dev)
+    i_real = torch.empty(S * stride, dtype=torch.float32, device=dev)
+    power = torch.empty(2 * S, dtype=torch.float64, device=dev)
+    import ctypes
+    maxs = 96
+    for s0 in range(0, S, maxs):
+        ns = min(maxs, S - s0)
+        lo = (ctypes.c_int64 * ns)(*[b[0] for b in bounds[s0:s0 + ns]])
+        hi = (ctypes.c_int64 * ns)(*[b[1] for b in bounds[s0:s0 + ns]])
+        cd = torch.empty((ns, half), dtype=torch.complex64, device=dev)
+        ci = torch.empty((ns, half), dtype=torch.complex64, device=dev)
+        pw = torch.empty(2 * ns, dtype=torch.float64, device=dev)
+        _lib.call('pyl_bk_shell_fill', ptr(dk), dims, ctypes.cast(lo, ctypes.c_void_p),
+                  ctypes.cast(hi, ctypes.c_void_p), ns, ptr(cd), ptr(ci), ptr(pw), stream_ptr())
+        power[2 * s0:2 * (s0 + ns)] = pw
+        if stride == cells:
+            _lib.call('pyl_fft_c2r', ptr(cd), ptr(d_real[s0 * stride:]), dims, ns, stream_ptr())
+            _lib.call('pyl_fft_c2r', ptr(ci), ptr(i_real[s0 * stride:]), dims, ns, stream_ptr())
+        else:
+            for j in range(ns):
+                o = (s0 + j) * stride
+                _lib.call('pyl_fft_c2r', ptr(cd[j]), ptr(d_real[o:]), dims, 1, stream_ptr())
+                _lib.call('pyl_fft_c2r', ptr(ci[j]), ptr(i_real[o:]), dims, 1, stream_ptr())
+        del cd, ci
+    return d_real, i_real, power, stride
+
+
+def Bk_triangles(delta, BoxSize, triangles, MAS='CIC', threads=1):
+    """Bispectra of many triangles (k1, k2, k3) in h/Mpc sharing one FFT, one shell
+    fill, one batched C2R and one reduction launch.  Returns (B, Q, Pk1, Pk2, Pk3)."""
+    require_cuda()
+    import ctypes
+    dims = delta.shape[0]
+    kF = frequencies(BoxSize, dims)[0]
+    dev = torch.device('cuda', torch.cuda.current_device())
+    x = as_device_f32(delta, 'delta')
+    dk = torch.empty(_half_shape(dims), dtype=torch.complex64, device=dev)
+    _lib.call('pyl_fft_r2c', ptr(x), ptr(dk), dims, 1, stream_ptr())
+    _lib.call('pyl_mas_deconvolve', ptr(dk), None, dims, MAS_function(MAS), stream_ptr())
+    keys, index = [], {}
+    tri_idx = []
+    for (a, b, c) in triangles:
+        ids = []
+        for k in (a, b, c):
+            kmin, kmax = (k - kF) / kF, (k + kF) / kF       # bispectrum_library.pyx:73-77
+            if (kmin, kmax) not in index:
+                index[(kmin, kmax)] = len(keys)
+                keys.append((kmin, kmax))
+            ids.append(index[(kmin, kmax)])
+        tri_idx.append(ids)
+    bounds = [shell_k2_bounds(lo, hi) for lo, hi in keys]
+    d_real, i_real, power, stride = _bk_fields(dk, dims, bounds)
+    T = len(tri_idx)
+    flat = (ctypes.c_int * (3 * T))(*[i for t in tri_idx for i in t])
+    num = torch.empty(T, dtype=torch.float64, device=dev)
+    den = torch.empty(T, dtype=torch.float64, device=dev)
+    _lib.call('pyl_bk_triangles', ptr(d_real), ptr(i_real), dims, stride, len(keys),
+              ctypes.cast(flat, ctypes.c_void_p), T, ptr(num), ptr(den), stream_ptr())
+    pw = power.cpu().numpy()
+    P = (pw[0::2] / pw[1::2]) * (BoxSize / dims ** 2) ** 3
+    B = (num.cpu().numpy() / den.cpu().numpy()) * (BoxSize ** 2 / dims ** 3) ** 3
+    t = np.asarray(tri_idx)
+    P1, P2, P3 = P[t[:, 0]], P[t[:, 1]], P[t[:, 2]]
+    Q = B / (P1 * P2 + P1 * P3 + P2 * P3)
+    return B, Q, P1, P2, P3
+
+
+class Bk(object):
+    def __init__(self, delta, BoxSize, k1, k2, theta, MAS='CIC', threads=1, *, verbose=False):
+        start = time.time()
+        theta = np.asarray(theta, dtype=np.float64)
+        bins = theta.shape[0]
+        k3 = np.sqrt((k2 * np.sin(theta)) ** 2 + (k2 * np.cos(theta) + k1) ** 2)   # :66
+        tris = [(k1, k2, float(k3[j])) for j in range(bins)]
+        B, Q, P1, P2, P3 = Bk_triangles(delta, BoxSize, tris, MAS, threads)
+        self.B = B
+        self.Q = Q
+        self.k = np.concatenate([[k1, k2], k3]).astype(np.float64)
+        self.Pk = np.concatenate([[P1[0], P2[0]], P3]).astype(np.float64)
+        if verbose:
+            print('Time to compute bispectrum = %.2f' % (time.time() - start))

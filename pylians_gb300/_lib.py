@@ -1,0 +1,84 @@
+"""ctypes binding of libpylgpu.so (declared in include/pylians_gb300.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every compute entry point raises.
+"""
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libpylgpu.so')
+
+PYL_OK, PYL_ERR_INVALID, PYL_ERR_CUDA, PYL_ERR_CUFFT, PYL_ERR_WORKSPACE, PYL_ERR_UNSUPPORTED = range(6)
+MAS_INDEX = {'NGP': 1, 'CIC': 2, 'TSC': 3, 'PCS': 4}
+STRATEGY = {'auto': 0, 'atomic': 1, 'tiled': 2, 'sorted': 3}
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_F = ctypes.c_float
+_D = ctypes.c_double
+_SZ = ctypes.c_size_t
+
+# name -> (restype, argtypes); the exact list of exported C-ABI symbols
+SIGNATURES = {
+    'pyl_strerror': (ctypes.c_char_p, [_I]),
+    'pyl_last_error': (ctypes.c_char_p, []),
+    'pyl_version': (_I, []),
+    'pyl_ma_workspace_size': (_SZ, [_I64, _I, _I, _I, _I, _I]),
+    'pyl_ma': (_I, [_P, _P, _I64, _I, _P, _P, _I, _F, _I, _I, _I, _P, _SZ, _P]),
+    'pyl_grid_sum': (_I, [_P, _I64, _P, _P]),
+    'pyl_overdensity': (_I, [_P, _I64, _P, _D, _P]),
+    'pyl_fft_r2c': (_I, [_P, _P, _I, _I, _P]),
+    'pyl_fft_c2r': (_I, [_P, _P, _I, _I, _P]),
+    'pyl_fft_cache_clear': (_I, []),
+    'pyl_pk_sums_len': (_I64, [_I, _I]),
+    'pyl_pk_geometry_len': (_I64, [_I]),
+    'pyl_pk_workspace_size': (_SZ, [_I, _I, _I]),
+    'pyl_pk_bin': (_I, [_P, _P, _I, _I64, _I, _I, _P, _P, _P, _SZ, _P]),
+    'pyl_pk_geometry': (_I, [_I, _I, _P, _P]),
+    'pyl_mas_deconvolve': (_I, [_P, _P, _I, _I, _P]),
+    'pyl_bk_shell_fill': (_I, [_P, _I, _P, _P, _I, _P, _P, _P, _P]),
+    'pyl_bk_triangles': (_I, [_P, _P, _I, _I64, _I, _P, _I, _P, _P, _P]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class PylError(RuntimeError):
+    pass
+
+
+def load():
+    """Load (never build) libpylgpu.so and declare every signature."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise PylError('libpylgpu.so is not built (%s); run pylians_gb300.build.build() '
+                               'or __graft_entry__.build()' % LIB_PATH)
+            lib = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def check(rc, what=''):
+    if rc == PYL_OK:
+        return
+    lib = load()
+    msg = '%s: %s (%s)' % (what, lib.pyl_strerror(rc).decode(), lib.pyl_last_error().decode())
+    if rc == PYL_ERR_INVALID:
+        raise ValueError(msg)
+    raise PylError(msg)
+
+
+def call(name, *args):
+    rc = getattr(load(), name)(*args)
+    check(rc, name)
+    return rc

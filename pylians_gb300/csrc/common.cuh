@@ -1,0 +1,81 @@
+// Shared helpers for the sm_103a kernels of the density-field / clustering path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/pylians_gb300.h"
+
+namespace pyl {
+
+// Thread-local detail message behind the status codes returned by the C-ABI.
+void set_error(const std::string &msg);
+
+#define PYL_CHECK_ARG(cond, msg)                                 \
+    do {                                                         \
+        if (!(cond)) {                                           \
+            ::pyl::set_error(std::string(__func__) + ": " + msg); \
+            return PYL_ERR_INVALID;                              \
+        }                                                        \
+    } while (0)
+
+#define PYL_CUDA(call)                                                               \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            ::pyl::set_error(std::string(__func__) + ": " + cudaGetErrorString(e_)); \
+            return PYL_ERR_CUDA;                                                     \
+        }                                                                            \
+    } while (0)
+
+#define PYL_LAUNCH_CHECK() PYL_CUDA(cudaGetLastError())
+
+static inline int num_sms()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 152;
+    }
+    return n;
+}
+
+// Non-negative modulo: the cell index of any integer on a periodic axis.
+__device__ __forceinline__ int wrap_index(long long i, int n)
+{
+    long long r = i % n;
+    return (int)(r < 0 ? r + n : r);
+}
+
+// Signed frequency of FFT index i on an axis of n points (Pk_library.pyx:315).
+__device__ __host__ __forceinline__ int freq_of(int i, int n)
+{
+    return i > n / 2 ? i - n : i;
+}
+
+// Exact floor(sqrt(v)) for 0 <= v < 2^31.
+__device__ __forceinline__ int isqrt_exact(int v)
+{
+    int r = (int)sqrtf((float)v);
+    while (r * r > v) --r;
+    while ((r + 1) * (r + 1) <= v) ++r;
+    return r;
+}
+
+// Raise a kernel's dynamic shared-memory limit once per size (kept out of the
+// steady state so that launches can be captured in a CUDA graph).
+template <typename K>
+static inline cudaError_t ensure_smem(K kernel, size_t bytes, size_t *done)
+{
+    if (bytes <= *done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) *done = bytes;
+    return e;
+}
+
+__device__ __forceinline__ void red_add(float *p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void red_add(double *p, double v) { atomicAdd(p, v); }
+
+}  // namespace pyl

@@ -1,0 +1,100 @@
+"""Particles -> overdensity -> R2C -> fused deconvolve/bin on one stream, buffers kept resident.
+
+This is the caller-side chain the reference's drivers run around MA and Pk
+(library/Pk_library/Pk_snapshot.py:66-89, documentation/Documentation.md:88-118):
+
+    delta = zeros; MA(pos, delta, BoxSize, MAS[, W]); delta /= mean; delta -= 1
+    Pk(delta, BoxSize, axis, MAS)
+
+with mean = N_particles / dims^3 (or sum(W) / dims^3 with weights), plus the
+interlaced second grid when `interlaced=True`.  Every launch goes to one CUDA
+stream, so a whole step can be captured in a CUDA graph (`capture()`), and the
+grids, FFT outputs and sums stay allocated across steps.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from . import Pk_library as PKL
+from ._device import ptr, require_cuda, stream_ptr
+
+
+class ParticlePk(object):
+    def __init__(self, dims, BoxSize, MAS='CIC', axis=2, interlaced=False, strategy='auto',
+                 max_particles=0, weighted=False, device=None):
+        require_cuda()
+        if MAS not in _lib.MAS_INDEX:
+            raise ValueError('MAS must be NGP, CIC, TSC or PCS')
+        self.dims, self.BoxSize, self.MAS, self.axis = int(dims), float(BoxSize), MAS, int(axis)
+        self.interlaced = bool(interlaced)
+        self.strategy = strategy
+        self.device = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
+        ng = 2 if self.interlaced else 1
+        d = self.dims
+        self.grids = torch.empty((ng, d, d, d), dtype=torch.float32, device=self.device)
+        self.dk = torch.empty((ng, d, d, d // 2 + 1), dtype=torch.complex64, device=self.device)
+        L = _lib.load()
+        self.sums = torch.empty(L.pyl_pk_sums_len(d, 1), dtype=torch.float64, device=self.device)
+        self.wsum = torch.empty(1, dtype=torch.float64, device=self.device)
+        self.mas_p, self._keep = PKL.ctypes_int_array([_lib.MAS_INDEX[MAS]])
+        self.ws_bytes = 0
+        self.ws = None
+        self.reserve(max_particles, weighted)
+        self.geom = PKL.geometry(d, self.axis, self.device)
+        self.graph = None
+
+    def reserve(self, n, weighted=False):
+        L = _lib.load()
+        need = L.pyl_ma_workspace_size(int(n), 3, self.dims, _lib.MAS_INDEX[self.MAS],
+                                       _lib.STRATEGY[self.strategy], int(self.interlaced))
+        if weighted:
+            need += 4 * int(n) + 256
+        if need > self.ws_bytes:
+            self.ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+            self.ws_bytes = need
+
+    def step(self, pos, W=None, stream=None):
+        """Enqueue one pass: zero grids, deposit, normalise, FFT, bin -> self.sums."""
+        n = pos.shape[0]
+        d = self.dims
+        cells = d ** 3
+        st = stream_ptr(stream)
+        self.reserve(n, W is not None)
+        self.grids.zero_()
+        g2 = self.grids[1] if self.interlaced else None
+        _lib.call('pyl_ma', ptr(pos), ptr(W), n, 3, ptr(self.grids[0]), ptr(g2), d,
+                  self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy], 0,
+                  ptr(self.ws), self.ws_bytes, st)
+        ng = self.grids.shape[0]
+        if W is None:
+            mean = float(n) / cells
+            for i in range(ng):
+                _lib.call('pyl_overdensity', ptr(self.grids[i]), cells, None, mean, st)
+        else:
+            # mean = sum(W) / dims^3 in float64 (Pk_snapshot.py:80)
+            _lib.call('pyl_grid_sum', ptr(W), n, ptr(self.wsum), st)
+            for i in range(ng):
+                _lib.call('pyl_overdensity', ptr(self.grids[i]), cells, ptr(self.wsum), 0.0, st)
+        _lib.call('pyl_fft_r2c', ptr(self.grids), ptr(self.dk), d, ng, st)
+        dk2 = self.dk[1] if self.interlaced else None
+        _lib.call('pyl_pk_bin', ptr(self.dk[0]), ptr(dk2), 1, self.dk[0].numel(), d, self.axis,
+                  self.mas_p, ptr(self.sums), None, 0, st)
+        return self.sums
+
+    def capture(self, pos, W=None):
+        """Capture one step on `pos` (fixed size and address) into a CUDA graph."""
+        self.step(pos, W)           # warm-up: plans, workspace, function attributes
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step(pos, W)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+        return self.sums
+
+    def result(self, sums=None):
+        s = (sums if sums is not None else self.sums).cpu().numpy()
+        return PKL.finalize_pk(s, self.geom, self.BoxSize, self.dims, 1, cross=False)

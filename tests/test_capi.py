@@ -1,0 +1,95 @@
+"""C-ABI checks that need no GPU: the library loads, exports exactly what
+include/pylians_gb300.h declares, and rejects bad arguments on the host."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, 'include', 'pylians_gb300.h')
+
+
+@pytest.fixture(scope='module')
+def lib():
+    import pylians_gb300.build as b
+    b.build()
+    from pylians_gb300 import _lib
+    return _lib.load()
+
+
+def declared():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(pyl_\w+)\s*\(', text)))
+
+
+def test_header_matches_bindings():
+    from pylians_gb300 import _lib
+    assert declared() == sorted(_lib.SIGNATURES)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared():
+        assert hasattr(lib, name), name
+
+
+def test_strerror_and_version(lib):
+    assert lib.pyl_strerror(0) == b'success'
+    assert lib.pyl_strerror(1) == b'invalid argument'
+    assert lib.pyl_strerror(99) == b'unknown status'
+    assert lib.pyl_version() >= 100
+
+
+def test_sizes_are_host_side(lib):
+    # 128^3: nb3 = 111, nb1 = 65, nb2 = 65*91
+    assert lib.pyl_pk_sums_len(128, 1) == 111 * 4 + 65 + 65 * 91
+    assert lib.pyl_pk_sums_len(128, 2) == 111 * (3 * 3 + 2) + 65 * 3 + 65 * 91 * 3
+    assert lib.pyl_pk_geometry_len(128) == 2 * 65 + 65 * 91 + 2 * 111
+    assert lib.pyl_ma_workspace_size(1000, 3, 64, 2, 1, 0) == 0          # atomic: no workspace
+    assert lib.pyl_ma_workspace_size(10 ** 6, 3, 512, 2, 2, 1) >= 12 * 10 ** 6
+
+
+@pytest.mark.parametrize('kw,msg', [
+    (dict(ndim=4), 'ndim'), (dict(mas=7), 'MAS'), (dict(dims=0), 'dims'),
+    (dict(box=-1.0), 'BoxSize'), (dict(strategy=9), 'strategy'), (dict(n=-5), 'negative'),
+])
+def test_ma_rejects_bad_arguments(lib, kw, msg):
+    a = dict(ndim=3, mas=2, dims=16, box=1.0, strategy=0, n=10)
+    a.update(kw)
+    buf = ctypes.c_void_p(16)   # never dereferenced: validation fails first
+    rc = lib.pyl_ma(buf, None, a['n'], a['ndim'], buf, None, a['dims'], a['box'], a['mas'],
+                    a['strategy'], 1, None, 0, None)
+    assert rc == 1
+    assert msg in lib.pyl_last_error().decode()
+
+
+def test_pk_rejects_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)
+    mp = (ctypes.c_int * 1)(2)
+    assert lib.pyl_pk_bin(buf, None, 1, 0, 32, 3, mp, buf, None, 0, None) == 1
+    assert 'axis' in lib.pyl_last_error().decode()
+    mp5 = (ctypes.c_int * 5)(2, 2, 2, 2, 2)
+    assert lib.pyl_pk_bin(buf, None, 5, 10 ** 6, 32, 0, mp5, buf, None, 0, None) == 5
+    bad = (ctypes.c_int * 1)(7)
+    assert lib.pyl_pk_bin(buf, None, 1, 0, 32, 0, bad, buf, None, 0, None) == 1
+
+
+def test_bk_rejects_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)
+    lo = (ctypes.c_int64 * 1)(1)
+    assert lib.pyl_bk_shell_fill(buf, 32, lo, lo, 0, buf, buf, buf, None) == 1
+    tri = (ctypes.c_int * 3)(0, 0, 5)
+    assert lib.pyl_bk_triangles(buf, buf, 16, 4096, 2, tri, 1, buf, buf, None) == 1
+
+
+def test_python_facade_errors_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('GPU present')
+    import numpy as np
+    import pylians_gb300.MAS_library as MASL
+    from pylians_gb300._lib import PylError
+    with pytest.raises(PylError):
+        MASL.MA(np.zeros((4, 3), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'CIC')

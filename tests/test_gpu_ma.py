@@ -1,0 +1,171 @@
+"""GPU parity of mass assignment (pyl_ma through the C-ABI) against the reference's
+golden grids and the oracle.
+
+Tolerances: NGP without weights bit-exact (integer counts, any order);
+NGP with weights and CIC/TSC/PCS: |gpu - ref| <= 2e-6 * max|ref| per cell (the
+reference and the GPU add the same float32 terms in different orders).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+MAS_LIST = ['NGP', 'CIC', 'TSC', 'PCS']
+STRATS = ['atomic', 'tiled']
+
+
+@pytest.fixture(scope='module')
+def MASL():
+    import pylians_gb300.build as b
+    b.build()
+    import pylians_gb300.MAS_library as M
+    return M
+
+
+@pytest.fixture(scope='module')
+def ma():
+    return np.load(os.path.join(GOLDEN, 'ma_golden.npz'))
+
+
+def close(a, b, exact, tol=2e-6):
+    if exact:
+        np.testing.assert_array_equal(a, b)
+    else:
+        assert np.abs(a - b).max() <= tol * max(np.abs(b).max(), 1e-30), np.abs(a - b).max()
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('tag', ['', 'W'])
+@pytest.mark.parametrize('strategy', STRATS)
+def test_ma_golden_3d(MASL, ma, mas, tag, strategy):
+    pos, W = ma['grid_pos'], ma['grid_W']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    d = np.zeros((N, N, N), np.float32)
+    MASL.MA(pos, d, L, mas, W if tag else None, strategy=strategy)
+    close(d, ma['MA3D_%s%s' % (mas, tag)], exact=(mas == 'NGP' and not tag))
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('tag', ['', 'W'])
+def test_ma_golden_2d(MASL, ma, mas, tag):
+    pos, W = ma['grid_pos'], ma['grid_W']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    d2 = np.zeros((N, N), np.float32)
+    MASL.MA(np.ascontiguousarray(pos[:, :2]), d2, L, mas, W if tag else None)
+    close(d2, ma['MA2D_%s%s' % (mas, tag)], exact=(mas == 'NGP' and not tag))
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+def test_ma_c_path_golden(MASL, ma, mas):
+    pos = ma['grid_pos']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    c = np.zeros((N, N, N), np.float32)
+    getattr(MASL, mas + 'c3D')(pos, c, L, 4)
+    close(c, ma['MASc3D_%s' % mas], exact=(mas == 'NGP'))
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+def test_ma_conservation(MASL, ma, mas):
+    """Test/test_MAS.py:10-84 on the GPU: sum(grid)/N == 1."""
+    pos = ma['conservation_pos']
+    for W in (None, np.full(pos.shape[0], 3.0, np.float32)):
+        d = np.zeros((64, 64, 64), np.float32)
+        MASL.MA(pos, d, 1.0, mas, W=W)
+        norm = pos.shape[0] * (3.0 if W is not None else 1.0)
+        s = np.sum(d, dtype=np.float64) / norm
+        assert round(s - 1.0, 20 if mas == 'NGP' else 8) == 0
+
+
+def test_ma_accumulates(MASL, ma):
+    pos = ma['grid_pos']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    d = ma['accum_base'].copy()
+    MASL.MA(pos, d, L, 'NGP')
+    np.testing.assert_array_equal(d, ma['accum_NGP'])
+    t = torch.from_numpy(ma['accum_base'].copy()).cuda()
+    MASL.MA(torch.from_numpy(pos).cuda(), t, L, 'NGP', strategy='tiled')
+    np.testing.assert_array_equal(t.cpu().numpy(), ma['accum_NGP'])
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('strategy', STRATS)
+def test_ma_interlaced_vs_oracle(MASL, mas, strategy):
+    rng = np.random.default_rng(42)
+    N, L, n = 48, 500.0, 300000
+    pos = (rng.random((n, 3)) * L).astype(np.float32)
+    W = (rng.random(n) * 2).astype(np.float32)
+    g1 = torch.zeros((N, N, N), device='cuda')
+    g2 = torch.zeros((N, N, N), device='cuda')
+    MASL.MA(torch.from_numpy(pos).cuda(), g1, L, mas, torch.from_numpy(W).cuda(),
+            interlaced=g2, strategy=strategy)
+    o1 = np.zeros((N, N, N), np.float32)
+    o2 = np.zeros((N, N, N), np.float32)
+    O.MA(pos, o1, L, mas, W)
+    O.MA((pos + np.float32(0.5 * L / N)).astype(np.float32), o2, L, mas, W)
+    close(g1.cpu().numpy(), o1, False, 5e-6)
+    close(g2.cpu().numpy(), o2, False, 5e-6)
+
+
+@pytest.mark.parametrize('mas', MAS_LIST)
+def test_tiled_matches_atomic_large(MASL, mas):
+    """A grid larger than the tile with ragged tiles (dims not a multiple of 16/32)."""
+    rng = np.random.default_rng(7)
+    N, L, n = 200, 1000.0, 2_000_000
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    a = torch.zeros((N, N, N), device='cuda')
+    b = torch.zeros((N, N, N), device='cuda')
+    MASL.MA(pos, a, L, mas, strategy='atomic')
+    MASL.MA(pos, b, L, mas, strategy='tiled')
+    if mas == 'NGP':
+        assert torch.equal(a, b)
+    else:
+        assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
+    assert abs(b.double().sum().item() - n) <= 1e-6 * n
+
+
+def test_ngp_bit_exact_config1(MASL):
+    """128^3 particles on a 128^3 grid (the small CPU-runnable configuration): NGP
+    counts equal the oracle's bit for bit."""
+    rng = np.random.default_rng(1)
+    N, L = 128, 1000.0
+    pos = (rng.random((N ** 3, 3)) * L).astype(np.float32)
+    o = np.zeros((N, N, N), np.float32)
+    O.MA(pos, o, L, 'NGP', threads=os.cpu_count() or 1)
+    for strategy in STRATS:
+        g = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(torch.from_numpy(pos).cuda(), g, L, 'NGP', strategy=strategy)
+        np.testing.assert_array_equal(g.cpu().numpy(), o)
+
+
+def test_edge_positions(MASL):
+    """Empty input, positions on cell edges, at 0, at L, slightly negative and beyond L:
+    every index wraps periodically, like the oracle (the reference writes out of bounds
+    for the negative ones)."""
+    N, L = 16, 1.0
+    h = np.float32(L / N)
+    pts = np.array([[0, 0, 0], [h, 2 * h, 3 * h], [0.5 * h, 1.5 * h, 2.5 * h], [L, L, L],
+                    [np.nextafter(np.float32(L), np.float32(0))] * 3, [-1e-3, -0.2 * h, -0.7 * h],
+                    [L + 0.3 * h, 2 * L, 3.3 * L]], np.float32)
+    for mas in MAS_LIST:
+        for strategy in STRATS:
+            g = np.zeros((N, N, N), np.float32)
+            MASL.MA(np.zeros((0, 3), np.float32), g, L, mas, strategy=strategy)
+            assert not g.any()
+            MASL.MA(pts, g, L, mas, strategy=strategy)
+            o = np.zeros((N, N, N), np.float32)
+            O.MA(pts, o, L, mas)
+            close(g, o, mas == 'NGP', 1e-6)
+
+
+def test_bad_input_raises(MASL):
+    with pytest.raises(ValueError):
+        MASL.MA(np.zeros((4, 3), np.float64), np.zeros((8, 8, 8), np.float32), 1.0, 'CIC')
+    with pytest.raises(ValueError):
+        MASL.MA(np.zeros((4, 2), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'CIC')
+    with pytest.raises(ValueError):
+        MASL.MA(np.zeros((4, 3), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'XYZ')
