@@ -43,6 +43,7 @@ def parse():
     ap.add_argument('--cpu-side', type=int, default=256, help='side of the CPU baseline sample')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--strategy', default='auto', choices=['auto', 'atomic', 'tiled', 'sorted'])
     return ap.parse_args()
 
 
@@ -192,7 +193,7 @@ def main():
     gen = torch.Generator(device=dev)
     gen.manual_seed(1 + rank)
     pos = torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float32) * BOX
-    pp = ParticlePk(dims, BOX, 'CIC', axis=0, interlaced=True, strategy='auto', max_particles=n)
+    pp = ParticlePk(dims, BOX, 'CIC', axis=0, interlaced=True, strategy=a.strategy, max_particles=n)
 
     def barrier():
         if world > 1:
@@ -264,7 +265,7 @@ def main():
                     scaling='weak', vs_baseline=None, dtype='f32', data='synthetic',
                     config=dict(workload='cic_interlaced_pk_np%d^3_grid%d^3' % (side, dims),
                                 particles=n, grid=dims, box_mpc_h=BOX, axis=0, MAS='CIC',
-                                interlaced=True, strategy='auto', parallelism='replicas',
+                                interlaced=True, strategy=a.strategy, parallelism='replicas',
                                 l2_flush='inputs larger than L2 (12.9 GB positions)'),
                     e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
                     gpu_launches=KERNELS_PER_STEP * a.steps, stages_ms=stages)

@@ -137,9 +137,13 @@ def fft_c2r(dk, dims, threads=1):
 
 
 def interlace_combine(dk1, dk2):
-    """1/2 [dk1 + dk2 exp(i pi (kx+ky+kz)/N)] on the half-complex grid, phase in float64."""
+    """1/2 [dk1 + dk2 exp(i pi (kx+ky+kz)/N)] on the half-complex grid, phase in float64.
+    The frequencies are the reference's: index i > N/2 means i - N, so the Nyquist
+    index N/2 of an even grid is +N/2."""
     dims = dk1.shape[0]
-    k = np.fft.fftfreq(dims, 1.0 / dims)
+    middle = dims // 2
+    k = np.arange(dims)
+    k = np.where(k > middle, k - dims, k)      # the reference's signed frequency (Pk_library.pyx:315)
     kz = np.arange(dims // 2 + 1)
     ph = np.pi / dims * (k[:, None, None] + k[None, :, None] + kz[None, None, :])
     out = 0.5 * (dk1.astype(np.complex128) + dk2.astype(np.complex128) * np.exp(1j * ph))

@@ -62,7 +62,9 @@ def test_bk_vs_oracle(PKL, N, mas):
 def test_bk_triangles_batch_equals_single_calls(PKL, bk):
     N, L, k1, k2 = bk['meta']
     d = bk['delta']
-    ks = np.linspace(0.03, 0.3, 5)
+    # shells inside the grid's sphere |k| < kN (k/kF < 16): beyond it almost no
+    # triangle closes and B = num/den is round-off in any implementation
+    ks = np.linspace(0.03, 0.09, 5)
     tri = [(k, k, k) for k in ks]
     B, Q, P1, P2, P3 = PKL.Bk_triangles(d, L, tri, 'CIC')
     for j, k in enumerate(ks):
