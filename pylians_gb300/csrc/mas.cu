@@ -33,8 +33,25 @@ namespace {
 template <int MAS>
 struct Support { static constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS; };
 
+// First cell (unwrapped) of the support of one particle coordinate.
+template <int MAS>
+__device__ __forceinline__ long long axis_first(float p, float inv)
+{
+    const float dist = __fmul_rn(p, inv);
+    if (MAS == PYL_MAS_CIC) return (long long)truncf(dist);
+    const float fl = floorf(dist);
+    const float frac = __fsub_rn(dist, fl);
+    if (MAS == PYL_MAS_NGP) {
+        long long k = (long long)fl + (frac >= 0.5f ? 1 : 0);
+        if (dist < -0.5f && frac != 0.5f) k += 1;
+        return k;
+    }
+    if (MAS == PYL_MAS_TSC) return (long long)fl - 1 + (frac >= 0.5f ? 1 : 0);
+    return (long long)fl - 1;   // PCS
+}
+
 // Per-axis support of one particle coordinate: first cell f (unwrapped) and the
-// S weights of cells f, f+1, ..., f+S-1.
+// S weights of cells f, f+1, ..., f+S-1.  f equals axis_first<MAS>(p, inv).
 template <int MAS>
 __device__ __forceinline__ long long axis_weights(float p, float inv, float *C)
 {
@@ -153,10 +170,24 @@ __global__ void __launch_bounds__(256) ma_atomic_kernel(
 }
 
 // ------------------------------------------------------------------- TILED path
-constexpr int TX = 16, TY = 32, TZ = 32;   // tile extent in cells (x slowest)
+// Tiles are TB^3 cells.  Binning (per-CTA shared-memory histograms, no
+// per-particle global atomics):
+//   1. chunk_hist:  CTA c counts its contiguous chunk of particles per tile in
+//                   shared memory and writes the row hist[c][*];
+//   2. colscan:     hist[c][t] <- sum_{c'<c} hist[c'][t], total[t] = column sum;
+//   3. tile_scan:   offsets[t] = exclusive scan of total;
+//   4. chunk_scatter: CTA c starts shared-memory cursors at offsets[t] + hist[c][t]
+//                   and writes each particle to its tile's range.
+// Grids with more than HIST_MAX_TILES tiles count and place particles with
+// global atomics instead (the same tile layout).  Then one CTA per tile deposits
+// into a (TB+H)^3 shared-memory block (H = kernel support - 1, +1 for the
+// interlaced shift) and adds it to the grid with coalesced red.global.add.
+constexpr int TB = 32;
+constexpr int HIST_MAX_TILES = 49152;
+constexpr int MAX_CHUNKS = 256;
 
 struct TileGeom {
-    int dims, ntx, nty, ntz;               // grid side, tiles per axis
+    int dims, nt;          // grid side, tiles per axis
     long long ntiles;
 };
 
@@ -164,23 +195,85 @@ __host__ __device__ inline TileGeom tile_geom(int dims)
 {
     TileGeom g;
     g.dims = dims;
-    g.ntx = (dims + TX - 1) / TX;
-    g.nty = (dims + TY - 1) / TY;
-    g.ntz = (dims + TZ - 1) / TZ;
-    g.ntiles = (long long)g.ntx * g.nty * g.ntz;
+    g.nt = (dims + TB - 1) / TB;
+    g.ntiles = (long long)g.nt * g.nt * g.nt;
     return g;
 }
 
 template <int MAS>
 __device__ __forceinline__ unsigned tile_key(const float *p, float inv, const TileGeom &g)
 {
-    float C[4];
-    const int cx = wrap_index(axis_weights<MAS>(p[0], inv, C), g.dims);
-    const int cy = wrap_index(axis_weights<MAS>(p[1], inv, C), g.dims);
-    const int cz = wrap_index(axis_weights<MAS>(p[2], inv, C), g.dims);
-    return (unsigned)(((long long)(cx / TX) * g.nty + cy / TY) * g.ntz + cz / TZ);
+    const int cx = wrap_index(axis_first<MAS>(p[0], inv), g.dims);
+    const int cy = wrap_index(axis_first<MAS>(p[1], inv), g.dims);
+    const int cz = wrap_index(axis_first<MAS>(p[2], inv), g.dims);
+    return (unsigned)(((long long)(cx / TB) * g.nt + cy / TB) * g.nt + cz / TB);
 }
 
+template <int MAS>
+__global__ void __launch_bounds__(1024) chunk_hist_kernel(const float *__restrict__ pos, long long n,
+                                                          long long chunk, float inv, TileGeom g,
+                                                          unsigned *__restrict__ hist)
+{
+    extern __shared__ unsigned cnt[];
+    const int T = (int)g.ntiles;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0;
+    __syncthreads();
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    for (long long i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
+        atomicAdd(cnt + tile_key<MAS>(p, inv, g), 1u);
+    }
+    __syncthreads();
+    unsigned *row = hist + (long long)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = cnt[t];
+}
+
+// hist[c][t] <- exclusive prefix over c; total[t] <- column sum.  Thread per tile.
+__global__ void __launch_bounds__(256) colscan_kernel(unsigned *__restrict__ hist, int C, int T,
+                                                      unsigned *__restrict__ total)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    unsigned run = 0;
+    int c = 0;
+    for (; c + 8 <= C; c += 8) {
+        unsigned v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = hist[(long long)(c + j) * T + t];
+#pragma unroll
+        for (int j = 0; j < 8; j++) { hist[(long long)(c + j) * T + t] = run; run += v[j]; }
+    }
+    for (; c < C; c++) {
+        const unsigned v = hist[(long long)c * T + t];
+        hist[(long long)c * T + t] = run;
+        run += v;
+    }
+    total[t] = run;
+}
+
+template <int MAS, bool WEIGHTED>
+__global__ void __launch_bounds__(1024) chunk_scatter_kernel(
+    const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk,
+    float inv, TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
+    float *__restrict__ bpos, float *__restrict__ bw)
+{
+    extern __shared__ unsigned cur[];
+    const int T = (int)g.ntiles;
+    const unsigned *row = colpre + (long long)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) cur[t] = offsets[t] + row[t];
+    __syncthreads();
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    for (long long i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
+        const unsigned slot = atomicAdd(cur + tile_key<MAS>(p, inv, g), 1u);
+        bpos[3ull * slot] = p[0];
+        bpos[3ull * slot + 1] = p[1];
+        bpos[3ull * slot + 2] = p[2];
+        if (WEIGHTED) bw[slot] = __ldg(w + i);
+    }
+}
+
+// Fallback binning for grids with more tiles than one CTA's shared memory can count.
 template <int MAS>
 __global__ void __launch_bounds__(256) tile_count_kernel(const float *__restrict__ pos, long long n,
                                                          float inv, TileGeom g,
@@ -193,8 +286,24 @@ __global__ void __launch_bounds__(256) tile_count_kernel(const float *__restrict
     }
 }
 
-// Exclusive scan of `n` counts into offsets[0..n] and a copy into cursor[0..n-1],
-// by one CTA of 1024 threads (n up to a few million tiles).
+template <int MAS, bool WEIGHTED>
+__global__ void __launch_bounds__(256) tile_scatter_kernel(
+    const float *__restrict__ pos, const float *__restrict__ w, long long n, float inv, TileGeom g,
+    unsigned *__restrict__ cursor, float *__restrict__ bpos, float *__restrict__ bw)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
+        const unsigned slot = atomicAdd(cursor + tile_key<MAS>(p, inv, g), 1u);
+        bpos[3ull * slot] = p[0];
+        bpos[3ull * slot + 1] = p[1];
+        bpos[3ull * slot + 2] = p[2];
+        if (WEIGHTED) bw[slot] = __ldg(w + i);
+    }
+}
+
+// Exclusive scan of `n` counts into offsets[0..n] (and a copy into cursor when
+// non-null), by one CTA of 1024 threads.
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *__restrict__ counts,
                                                          long long n, unsigned *__restrict__ offsets,
                                                          unsigned *__restrict__ cursor)
@@ -215,112 +324,114 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *__restr
     unsigned long long run = part[threadIdx.x] - s;
     for (long long i = b; i < e; i++) {
         offsets[i] = (unsigned)run;
-        cursor[i] = (unsigned)run;
+        if (cursor) cursor[i] = (unsigned)run;
         run += counts[i];
     }
     if (threadIdx.x == blockDim.x - 1) offsets[n] = (unsigned)part[threadIdx.x];
 }
 
-template <int MAS, bool WEIGHTED>
-__global__ void __launch_bounds__(256) tile_scatter_kernel(
-    const float *__restrict__ pos, const float *__restrict__ w, long long n, float inv, TileGeom g,
-    unsigned *__restrict__ cursor, float *__restrict__ bpos, float *__restrict__ bw)
-{
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
-        const unsigned slot = atomicAdd(cursor + tile_key<MAS>(p, inv, g), 1u);
-        bpos[3ull * slot] = p[0];
-        bpos[3ull * slot + 1] = p[1];
-        bpos[3ull * slot + 2] = p[2];
-        if (WEIGHTED) bw[slot] = __ldg(w + i);
-    }
-}
-
-template <int MAS, bool INTERLACED>
+// Deposit sub-tile: half a bin along x (TB/2 x TB x TB cells) plus the halo.
+template <int MAS, bool SHIFT>
 struct TileShape {
-    static constexpr int H = Support<MAS>::S - 1 + (INTERLACED ? 1 : 0);   // halo on the + side
-    static constexpr int EX = TX + H, EY = TY + H, EZ = TZ + H;
-    static constexpr int CELLS = EX * EY * EZ;
-    static constexpr size_t SMEM = sizeof(float) * CELLS * (INTERLACED ? 2 : 1);
+    static constexpr int H = Support<MAS>::S - 1 + (SHIFT ? 1 : 0);   // halo on the + side
+    static constexpr int HX = TB / 2;
+    static constexpr int EX = HX + H, E = TB + H;
+    static constexpr int CELLS = EX * E * E;
+    static constexpr size_t SMEM = 2 * sizeof(unsigned) * CELLS;    // lo + hi words
 };
 
-template <int MAS, bool WEIGHTED, bool INTERLACED>
-__global__ void __launch_bounds__(512) tile_deposit_kernel(
+// Exact signed 64-bit fixed-point accumulation (2^-32 units) from two 32-bit
+// shared-memory integer atomics: the low word's carry goes to the high word.
+// Integer sums do not depend on the order of the adds.
+__device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int c, float v)
+{
+    const unsigned long long q = (unsigned long long)__float2ll_rn(v * 4294967296.0f);
+    const unsigned ql = (unsigned)q, qh = (unsigned)(q >> 32);
+    unsigned carry = 0;
+    if (ql) {
+        const unsigned old = atomicAdd(lo + c, ql);
+        carry = (unsigned)(old + ql) < old ? 1u : 0u;
+    }
+    if (qh + carry) atomicAdd(hi + c, qh + carry);
+}
+
+__device__ __forceinline__ float fx_value(unsigned lo, unsigned hi)
+{
+    const long long s = (long long)(((unsigned long long)hi << 32) | lo);
+    return __ll2float_rn(s) * 2.3283064365386963e-10f;   // exact scaling by 2^-32
+}
+
+// One CTA per (bin, x-half); one grid per launch (SHIFT: the half-cell-shifted,
+// interlaced grid).  Unweighted deposits accumulate in exact fixed point
+// (order-independent); weighted ones in float32 shared-memory atomics.
+template <int MAS, bool WEIGHTED, bool SHIFT>
+__global__ void __launch_bounds__(1024) tile_deposit_kernel(
     const float *__restrict__ bpos, const float *__restrict__ bw,
     const unsigned *__restrict__ offsets, TileGeom g, float inv, float halfcell,
-    float *__restrict__ grid, float *__restrict__ grid2)
+    float *__restrict__ grid)
 {
-    using TS = TileShape<MAS, INTERLACED>;
-    constexpr int S = Support<MAS>::S;
-    extern __shared__ float smem[];
-    const long long tile = blockIdx.x;
+    using TS = TileShape<MAS, SHIFT>;
+    constexpr int S = Support<MAS>::S, E = TS::E, EX = TS::EX, HX = TS::HX;
+    extern __shared__ unsigned smw[];
+    unsigned *lo = smw, *hi = smw + TS::CELLS;
+    float *facc = (float *)smw;
+    const long long tile = blockIdx.x >> 1;
+    const int half = blockIdx.x & 1;
     const unsigned begin = offsets[tile], end = offsets[tile + 1];
     if (begin == end) return;
-    const int tz = (int)(tile % g.ntz);
-    const int ty = (int)((tile / g.ntz) % g.nty);
-    const int tx = (int)(tile / ((long long)g.ntz * g.nty));
-    const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
-    for (int c = threadIdx.x; c < TS::CELLS * (INTERLACED ? 2 : 1); c += blockDim.x) smem[c] = 0.0f;
+    const int tz = (int)(tile % g.nt);
+    const int ty = (int)((tile / g.nt) % g.nt);
+    const int tx = (int)(tile / ((long long)g.nt * g.nt));
+    const int o[3] = {tx * TB + half * HX, ty * TB, tz * TB};
+    if (o[0] >= g.dims) return;                  // ragged last bin: no second half
+    for (int c = threadIdx.x; c < (WEIGHTED ? 1 : 2) * TS::CELLS; c += blockDim.x) smw[c] = 0u;
     __syncthreads();
 
     for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
         const float p[3] = {bpos[3ull * i], bpos[3ull * i + 1], bpos[3ull * i + 2]};
+        const long long fx0 = axis_first<MAS>(p[0], inv);
+        const int lx = wrap_index(fx0, g.dims) - o[0];
+        if (lx < 0 || lx >= HX) continue;        // the other half's particle
         const float wi = WEIGHTED ? bw[i] : 1.0f;
-        int base[3];
-        long long f0[3];
+        float C[3][S];
+        int loc[3];
 #pragma unroll
-        for (int g2 = 0; g2 < (INTERLACED ? 2 : 1); g2++) {
-            float C[3][S];
-            int loc[3];
+        for (int a = 0; a < 3; a++) {
+            const long long f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
+            loc[a] = a == 0 ? lx : wrap_index(f0, g.dims) - o[a];
+            if (SHIFT) {
+                // the half-cell shift moves the first cell by 0 or +1; the clamp only
+                // matters for non-finite or astronomically large positions
+                const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+                loc[a] += f > f0 ? 1 : 0;
+            } else {
+                axis_weights<MAS>(p[a], inv, C[a]);
+            }
+        }
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const float q = g2 == 0 ? p[a] : __fadd_rn(p[a], halfcell);
-                const long long f = axis_weights<MAS>(q, inv, C[a]);
-                if (g2 == 0) {
-                    // local coordinate of the first cell inside the tile
-                    const int o = a == 0 ? ox : (a == 1 ? oy : oz);
-                    f0[a] = f;
-                    base[a] = wrap_index(f, g.dims) - o;
-                    loc[a] = base[a];
-                } else {
-                    // the half-cell shift moves the first cell by 0 or +1; the clamp
-                    // only matters for non-finite or astronomically large positions
-                    const long long df = f - f0[a];
-                    loc[a] = base[a] + (df <= 0 ? 0 : 1);
+        for (int l = 0; l < S; l++)
+#pragma unroll
+            for (int m = 0; m < S; m++) {
+                const float c01 = __fmul_rn(C[0][l], C[1][m]);
+                const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
+#pragma unroll
+                for (int q = 0; q < S; q++) {
+                    float v = __fmul_rn(c01, C[2][q]);
+                    if (WEIGHTED) atomicAdd(facc + row + q, __fmul_rn(v, wi));
+                    else fx_add(lo, hi, row + q, v);
                 }
             }
-            float *t = smem + (g2 ? TS::CELLS : 0);
-#pragma unroll
-            for (int l = 0; l < S; l++)
-#pragma unroll
-                for (int m = 0; m < S; m++) {
-                    const float c01 = __fmul_rn(C[0][l], C[1][m]);
-                    float *row = t + ((loc[0] + l) * TS::EY + (loc[1] + m)) * TS::EZ + loc[2];
-#pragma unroll
-                    for (int q = 0; q < S; q++) {
-                        float v = __fmul_rn(c01, C[2][q]);
-                        if (WEIGHTED) v = __fmul_rn(v, wi);
-                        atomicAdd(row + q, v);
-                    }
-                }
-        }
     }
     __syncthreads();
     const long long d = g.dims;
-    for (int gi = 0; gi < (INTERLACED ? 2 : 1); gi++) {
-        const float *t = smem + (gi ? TS::CELLS : 0);
-        float *out = gi ? grid2 : grid;
-        for (int c = threadIdx.x; c < TS::CELLS; c += blockDim.x) {
-            const float v = t[c];
-            if (v == 0.0f) continue;
-            const int lz = c % TS::EZ;
-            const int ly = (c / TS::EZ) % TS::EY;
-            const int lx = c / (TS::EZ * TS::EY);
-            const long long gx = (ox + lx) % d, gy = (oy + ly) % d, gz = (oz + lz) % d;
-            atomicAdd(out + (gx * d + gy) * d + gz, v);
-        }
+    for (int c = threadIdx.x; c < TS::CELLS; c += blockDim.x) {
+        const float v = WEIGHTED ? facc[c] : fx_value(lo[c], hi[c]);
+        if (v == 0.0f) continue;
+        const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+        const long long gx = (o[0] + lx) % d, gy = (o[1] + ly) % d, gz = (o[2] + lz) % d;
+        atomicAdd(grid + (gx * d + gy) * d + gz, v);
     }
+    (void)EX;
 }
 
 __global__ void scale_kernel(float *g, long long n, float div)
@@ -352,8 +463,10 @@ int launch_atomic(const float *pos, const float *w, long long n, float *grid, fl
 }
 
 struct TiledWs {
-    unsigned *counts, *offsets, *cursor;
+    unsigned *hist, *total, *offsets;
     float *bpos, *bw;
+    int chunks;
+    bool smem_hist;
     size_t bytes;
 };
 
@@ -363,11 +476,14 @@ TiledWs tiled_layout(void *base, long long n, int dims, bool weighted)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws;
+    ws.smem_hist = g.ntiles <= HIST_MAX_TILES;
+    ws.chunks = num_sms() < MAX_CHUNKS ? num_sms() : MAX_CHUNKS;
+    const size_t hist_len = ws.smem_hist ? (size_t)MAX_CHUNKS * g.ntiles : (size_t)g.ntiles;
     size_t off = 0;
     char *b = (char *)base;
-    ws.counts = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
+    ws.hist = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * hist_len, 256);
+    ws.total = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.offsets = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * (g.ntiles + 1), 256);
-    ws.cursor = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.bpos = (float *)(b + off); off = align_up(off + sizeof(float) * 3 * (size_t)n, 256);
     ws.bw = weighted ? (float *)(b + off) : nullptr;
     if (weighted) off = align_up(off + sizeof(float) * (size_t)n, 256);
@@ -375,16 +491,14 @@ TiledWs tiled_layout(void *base, long long n, int dims, bool weighted)
     return ws;
 }
 
-template <int MAS, bool W, bool I>
-int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                   float *grid2, cudaStream_t st)
+template <int MAS, bool W, bool SHIFT>
+int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid, cudaStream_t st)
 {
-    using TS = TileShape<MAS, I>;
-    auto kern = tile_deposit_kernel<MAS, W, I>;
+    using TS = TileShape<MAS, SHIFT>;
+    auto kern = tile_deposit_kernel<MAS, W, SHIFT>;
     static size_t done = 0;
     PYL_CUDA(ensure_smem(kern, TS::SMEM, &done));
-    kern<<<(unsigned)g.ntiles, 512, TS::SMEM, st>>>(ws.bpos, ws.bw, ws.offsets, g, inv, halfcell,
-                                                     grid, grid2);
+    kern<<<(unsigned)(2 * g.ntiles), 1024, TS::SMEM, st>>>(ws.bpos, ws.bw, ws.offsets, g, inv, halfcell, grid);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
@@ -395,19 +509,45 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws = tiled_layout(workspace, n, dims, w != nullptr);
-    PYL_CUDA(cudaMemsetAsync(ws.counts, 0, sizeof(unsigned) * g.ntiles, st));
-    const int blocks = grid_blocks(n, 256, 16);
-    tile_count_kernel<MAS><<<blocks, 256, 0, st>>>(pos, n, inv, g, ws.counts);
-    PYL_LAUNCH_CHECK();
-    tile_scan_kernel<<<1, 1024, 0, st>>>(ws.counts, g.ntiles, ws.offsets, ws.cursor);
-    PYL_LAUNCH_CHECK();
-    if (w) tile_scatter_kernel<MAS, true><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.cursor, ws.bpos, ws.bw);
-    else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.cursor, ws.bpos, ws.bw);
-    PYL_LAUNCH_CHECK();
-    if (w) return grid2 ? launch_deposit<MAS, true, true>(ws, g, inv, halfcell, grid, grid2, st)
-                        : launch_deposit<MAS, true, false>(ws, g, inv, halfcell, grid, grid2, st);
-    return grid2 ? launch_deposit<MAS, false, true>(ws, g, inv, halfcell, grid, grid2, st)
-                 : launch_deposit<MAS, false, false>(ws, g, inv, halfcell, grid, grid2, st);
+    const int T = (int)g.ntiles;
+    if (ws.smem_hist) {
+        const int C = ws.chunks;
+        const long long chunk = (n + C - 1) / C;
+        const size_t sm = sizeof(unsigned) * T;
+        static size_t d1 = 0, d2 = 0, d3 = 0;
+        PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm, &d1));
+        chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
+        PYL_LAUNCH_CHECK();
+        colscan_kernel<<<(T + 255) / 256, 256, 0, st>>>(ws.hist, C, T, ws.total);
+        PYL_LAUNCH_CHECK();
+        tile_scan_kernel<<<1, 1024, 0, st>>>(ws.total, T, ws.offsets, nullptr);
+        PYL_LAUNCH_CHECK();
+        if (w) {
+            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
+            chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                 ws.offsets, ws.bpos, ws.bw);
+        } else {
+            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm, &d3));
+            chunk_scatter_kernel<MAS, false><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                  ws.offsets, ws.bpos, ws.bw);
+        }
+        PYL_LAUNCH_CHECK();
+    } else {
+        PYL_CUDA(cudaMemsetAsync(ws.hist, 0, sizeof(unsigned) * g.ntiles, st));
+        const int blocks = grid_blocks(n, 256, 16);
+        tile_count_kernel<MAS><<<blocks, 256, 0, st>>>(pos, n, inv, g, ws.hist);
+        PYL_LAUNCH_CHECK();
+        tile_scan_kernel<<<1, 1024, 0, st>>>(ws.hist, g.ntiles, ws.offsets, ws.total);
+        PYL_LAUNCH_CHECK();
+        if (w) tile_scatter_kernel<MAS, true><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.bpos, ws.bw);
+        else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.bpos, ws.bw);
+        PYL_LAUNCH_CHECK();
+    }
+    int rc = w ? launch_deposit<MAS, true, false>(ws, g, inv, halfcell, grid, st)
+               : launch_deposit<MAS, false, false>(ws, g, inv, halfcell, grid, st);
+    if (rc || !grid2) return rc;
+    return w ? launch_deposit<MAS, true, true>(ws, g, inv, halfcell, grid2, st)
+             : launch_deposit<MAS, false, true>(ws, g, inv, halfcell, grid2, st);
 }
 
 inline int pick_strategy(int strategy, int ndim, int dims, long long n)
