@@ -42,11 +42,24 @@ static inline int num_sms()
     return n;
 }
 
-// Non-negative modulo: the cell index of any integer on a periodic axis.
+// Non-negative modulo: the cell index of any integer on a periodic axis.  The
+// 64-bit division only runs for indices more than one period outside [0, n).
 __device__ __forceinline__ int wrap_index(long long i, int n)
 {
+    if ((unsigned long long)i < (unsigned long long)n) return (int)i;
+    if (i >= n && i < 2LL * n) return (int)(i - n);
+    if (i < 0 && i >= -(long long)n) return (int)(i + n);
     long long r = i % n;
     return (int)(r < 0 ? r + n : r);
+}
+
+// (a + b) mod n for 0 <= a < n and 0 <= b (b usually < n).
+__device__ __forceinline__ long long add_wrap(long long a, long long b, long long n)
+{
+    long long s = a + b;
+    if (s >= n) s -= n;
+    if (s >= n) s %= n;
+    return s;
 }
 
 // Signed frequency of FFT index i on an axis of n points (Pk_library.pyx:315).

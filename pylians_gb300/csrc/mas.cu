@@ -25,6 +25,8 @@
 //           per tile instead of once per particle.
 #include <cuda_runtime.h>
 
+#include <stdlib.h>
+
 #include "common.cuh"
 
 namespace pyl {
@@ -255,7 +257,7 @@ template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk,
     float inv, TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
-    float *__restrict__ bpos, float *__restrict__ bw)
+    float4 *__restrict__ rec)
 {
     extern __shared__ unsigned cur[];
     const int T = (int)g.ntiles;
@@ -263,13 +265,26 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
     for (int t = threadIdx.x; t < T; t += blockDim.x) cur[t] = offsets[t] + row[t];
     __syncthreads();
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
-    for (long long i = b + threadIdx.x; i < e; i += blockDim.x) {
-        const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
-        const unsigned slot = atomicAdd(cur + tile_key<MAS>(p, inv, g), 1u);
-        bpos[3ull * slot] = p[0];
-        bpos[3ull * slot + 1] = p[1];
-        bpos[3ull * slot + 2] = p[2];
-        if (WEIGHTED) bw[slot] = __ldg(w + i);
+    constexpr int U = 4;            // particles in flight per thread
+    const long long step = (long long)blockDim.x * U;
+    for (long long i0 = b + threadIdx.x; i0 < e; i0 += step) {
+        float4 r[U];
+        unsigned key[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long long i = i0 + (long long)u * blockDim.x;
+            if (i < e) {
+                r[u] = make_float4(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2),
+                                   WEIGHTED ? __ldg(w + i) : 1.0f);
+                const float p[3] = {r[u].x, r[u].y, r[u].z};
+                key[u] = tile_key<MAS>(p, inv, g);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long long i = i0 + (long long)u * blockDim.x;
+            if (i < e) rec[atomicAdd(cur + key[u], 1u)] = r[u];
+        }
     }
 }
 
@@ -289,16 +304,13 @@ __global__ void __launch_bounds__(256) tile_count_kernel(const float *__restrict
 template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(256) tile_scatter_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, float inv, TileGeom g,
-    unsigned *__restrict__ cursor, float *__restrict__ bpos, float *__restrict__ bw)
+    unsigned *__restrict__ cursor, float4 *__restrict__ rec)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
         const unsigned slot = atomicAdd(cursor + tile_key<MAS>(p, inv, g), 1u);
-        bpos[3ull * slot] = p[0];
-        bpos[3ull * slot + 1] = p[1];
-        bpos[3ull * slot + 2] = p[2];
-        if (WEIGHTED) bw[slot] = __ldg(w + i);
+        rec[slot] = make_float4(p[0], p[1], p[2], WEIGHTED ? __ldg(w + i) : 1.0f);
     }
 }
 
@@ -331,13 +343,14 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *__restr
 }
 
 // Deposit sub-tile: half a bin along x (TB/2 x TB x TB cells) plus the halo.
-template <int MAS, bool SHIFT>
+template <int MAS, bool INTER, bool FIXED>
 struct TileShape {
-    static constexpr int H = Support<MAS>::S - 1 + (SHIFT ? 1 : 0);   // halo on the + side
+    static constexpr int H = Support<MAS>::S - 1 + (INTER ? 1 : 0);   // halo on the + side
     static constexpr int HX = TB / 2;
     static constexpr int EX = HX + H, E = TB + H;
     static constexpr int CELLS = EX * E * E;
-    static constexpr size_t SMEM = 2 * sizeof(unsigned) * CELLS;    // lo + hi words
+    // FIXED: lo + hi words of one grid at a time; float: one word per grid, both grids
+    static constexpr size_t SMEM = sizeof(unsigned) * CELLS * (FIXED ? 2 : (INTER ? 2 : 1));
 };
 
 // Exact signed 64-bit fixed-point accumulation (2^-32 units) from two 32-bit
@@ -361,77 +374,102 @@ __device__ __forceinline__ float fx_value(unsigned lo, unsigned hi)
     return __ll2float_rn(s) * 2.3283064365386963e-10f;   // exact scaling by 2^-32
 }
 
-// One CTA per (bin, x-half); one grid per launch (SHIFT: the half-cell-shifted,
-// interlaced grid).  Unweighted deposits accumulate in exact fixed point
-// (order-independent); weighted ones in float32 shared-memory atomics.
-template <int MAS, bool WEIGHTED, bool SHIFT>
-__global__ void __launch_bounds__(1024) tile_deposit_kernel(
-    const float *__restrict__ bpos, const float *__restrict__ bw,
-    const unsigned *__restrict__ offsets, TileGeom g, float inv, float halfcell,
-    float *__restrict__ grid)
+// Weights and local first cells of one particle for the plain (G=0) or the
+// half-cell-shifted (G=1) grid; loc relative to the sub-tile origin o.
+template <int MAS, int G>
+__device__ __forceinline__ void particle_support(const float *p, float inv, float halfcell, int dims,
+                                                 const int *o, int lx0, long long fx0,
+                                                 float (*C)[Support<MAS>::S], int *loc)
 {
-    using TS = TileShape<MAS, SHIFT>;
-    constexpr int S = Support<MAS>::S, E = TS::E, EX = TS::EX, HX = TS::HX;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const long long f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
+        loc[a] = a == 0 ? lx0 : wrap_index(f0, dims) - o[a];
+        if (G == 1) {
+            // the half-cell shift moves the first cell by 0 or +1; the clamp only
+            // matters for non-finite or astronomically large positions
+            const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+            loc[a] += f > f0 ? 1 : 0;
+        } else {
+            axis_weights<MAS>(p[a], inv, C[a]);
+        }
+    }
+}
+
+// One CTA per TB^3 bin.  The bin is deposited as two x-halves; each half is a
+// shared-memory block with the + side halo, added to the grid(s) with coalesced
+// red.global.add when done.  FIXED (unweighted only): exact order-independent
+// fixed-point sums, one grid per pass over the bin's particles; otherwise float32
+// shared atomics, both grids in one pass.  Re-reads of a bin's particles hit L2.
+template <int MAS, bool WEIGHTED, bool INTER, bool FIXED>
+__global__ void __launch_bounds__(1024) bin_deposit_kernel(
+    const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2)
+{
+    using TS = TileShape<MAS, INTER, FIXED>;
+    constexpr int S = Support<MAS>::S, E = TS::E, HX = TS::HX, CELLS = TS::CELLS;
     extern __shared__ unsigned smw[];
-    unsigned *lo = smw, *hi = smw + TS::CELLS;
-    float *facc = (float *)smw;
-    const long long tile = blockIdx.x >> 1;
-    const int half = blockIdx.x & 1;
+    const long long tile = blockIdx.x;
     const unsigned begin = offsets[tile], end = offsets[tile + 1];
     if (begin == end) return;
     const int tz = (int)(tile % g.nt);
     const int ty = (int)((tile / g.nt) % g.nt);
     const int tx = (int)(tile / ((long long)g.nt * g.nt));
-    const int o[3] = {tx * TB + half * HX, ty * TB, tz * TB};
-    if (o[0] >= g.dims) return;                  // ragged last bin: no second half
-    for (int c = threadIdx.x; c < (WEIGHTED ? 1 : 2) * TS::CELLS; c += blockDim.x) smw[c] = 0u;
-    __syncthreads();
-
-    for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
-        const float p[3] = {bpos[3ull * i], bpos[3ull * i + 1], bpos[3ull * i + 2]};
-        const long long fx0 = axis_first<MAS>(p[0], inv);
-        const int lx = wrap_index(fx0, g.dims) - o[0];
-        if (lx < 0 || lx >= HX) continue;        // the other half's particle
-        const float wi = WEIGHTED ? bw[i] : 1.0f;
-        float C[3][S];
-        int loc[3];
+    const long long d = g.dims;
+    constexpr int PASSES = FIXED && INTER ? 2 : 1;
+    for (int half = 0; half < 2; half++) {
+        const int o[3] = {tx * TB + half * HX, ty * TB, tz * TB};
+        if (o[0] >= g.dims) break;                  // ragged last bin: no second half
+        for (int pass = 0; pass < PASSES; pass++) {
+            constexpr int WORDS = FIXED ? 2 * CELLS : (INTER ? 2 : 1) * CELLS;
+            for (int c = threadIdx.x; c < WORDS; c += blockDim.x) smw[c] = 0u;
+            __syncthreads();
+            for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
+                const float4 r = rec[i];
+                const float p[3] = {r.x, r.y, r.z};
+                const long long fx0 = axis_first<MAS>(p[0], inv);
+                const int lx0 = wrap_index(fx0, g.dims) - o[0];
+                if (lx0 < 0 || lx0 >= HX) continue;          // the other half's particle
+                float C[3][S];
+                int loc[3];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const long long f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
-            loc[a] = a == 0 ? lx : wrap_index(f0, g.dims) - o[a];
-            if (SHIFT) {
-                // the half-cell shift moves the first cell by 0 or +1; the clamp only
-                // matters for non-finite or astronomically large positions
-                const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
-                loc[a] += f > f0 ? 1 : 0;
-            } else {
-                axis_weights<MAS>(p[a], inv, C[a]);
-            }
-        }
+                for (int gi = 0; gi < (FIXED ? 1 : (INTER ? 2 : 1)); gi++) {
+                    const int G = FIXED ? pass : gi;
+                    if (G == 0) particle_support<MAS, 0>(p, inv, halfcell, g.dims, o, lx0, fx0, C, loc);
+                    else        particle_support<MAS, 1>(p, inv, halfcell, g.dims, o, lx0, fx0, C, loc);
+                    float *facc = (float *)smw + gi * CELLS;
 #pragma unroll
-        for (int l = 0; l < S; l++)
+                    for (int l = 0; l < S; l++)
 #pragma unroll
-            for (int m = 0; m < S; m++) {
-                const float c01 = __fmul_rn(C[0][l], C[1][m]);
-                const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
+                        for (int m = 0; m < S; m++) {
+                            const float c01 = __fmul_rn(C[0][l], C[1][m]);
+                            const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
 #pragma unroll
-                for (int q = 0; q < S; q++) {
-                    float v = __fmul_rn(c01, C[2][q]);
-                    if (WEIGHTED) atomicAdd(facc + row + q, __fmul_rn(v, wi));
-                    else fx_add(lo, hi, row + q, v);
+                            for (int q = 0; q < S; q++) {
+                                float v = __fmul_rn(c01, C[2][q]);
+                                if (WEIGHTED) v = __fmul_rn(v, r.w);
+                                if (FIXED) fx_add(smw, smw + CELLS, row + q, v);
+                                else atomicAdd(facc + row + q, v);
+                            }
+                        }
                 }
             }
+            __syncthreads();
+            for (int gi = 0; gi < (FIXED ? 1 : (INTER ? 2 : 1)); gi++) {
+                float *out = (FIXED ? pass : gi) == 0 ? grid : grid2;
+                const float *facc = (const float *)smw + gi * CELLS;
+                for (int c = threadIdx.x; c < CELLS; c += blockDim.x) {
+                    const float v = FIXED ? fx_value(smw[c], smw[CELLS + c]) : facc[c];
+                    if (v == 0.0f) continue;
+                    const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+                    const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
+                                    gz = add_wrap(o[2], lz, d);
+                    atomicAdd(out + (gx * d + gy) * d + gz, v);
+                }
+            }
+            __syncthreads();
+        }
     }
-    __syncthreads();
-    const long long d = g.dims;
-    for (int c = threadIdx.x; c < TS::CELLS; c += blockDim.x) {
-        const float v = WEIGHTED ? facc[c] : fx_value(lo[c], hi[c]);
-        if (v == 0.0f) continue;
-        const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-        const long long gx = (o[0] + lx) % d, gy = (o[1] + ly) % d, gz = (o[2] + lz) % d;
-        atomicAdd(grid + (gx * d + gy) * d + gz, v);
-    }
-    (void)EX;
 }
 
 __global__ void scale_kernel(float *g, long long n, float div)
@@ -464,7 +502,7 @@ int launch_atomic(const float *pos, const float *w, long long n, float *grid, fl
 
 struct TiledWs {
     unsigned *hist, *total, *offsets;
-    float *bpos, *bw;
+    float4 *rec;                 // binned particles: x, y, z, weight
     int chunks;
     bool smem_hist;
     size_t bytes;
@@ -472,7 +510,7 @@ struct TiledWs {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-TiledWs tiled_layout(void *base, long long n, int dims, bool weighted)
+TiledWs tiled_layout(void *base, long long n, int dims)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws;
@@ -484,23 +522,34 @@ TiledWs tiled_layout(void *base, long long n, int dims, bool weighted)
     ws.hist = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * hist_len, 256);
     ws.total = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.offsets = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * (g.ntiles + 1), 256);
-    ws.bpos = (float *)(b + off); off = align_up(off + sizeof(float) * 3 * (size_t)n, 256);
-    ws.bw = weighted ? (float *)(b + off) : nullptr;
-    if (weighted) off = align_up(off + sizeof(float) * (size_t)n, 256);
+    ws.rec = (float4 *)(b + off); off = align_up(off + sizeof(float4) * (size_t)n, 256);
     ws.bytes = off;
     return ws;
 }
 
-template <int MAS, bool W, bool SHIFT>
-int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid, cudaStream_t st)
+template <int MAS, bool W, bool I, bool FX>
+int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
+                   float *grid2, cudaStream_t st)
 {
-    using TS = TileShape<MAS, SHIFT>;
-    auto kern = tile_deposit_kernel<MAS, W, SHIFT>;
+    using TS = TileShape<MAS, I, FX>;
+    auto kern = bin_deposit_kernel<MAS, W, I, FX>;
     static size_t done = 0;
     PYL_CUDA(ensure_smem(kern, TS::SMEM, &done));
-    kern<<<(unsigned)(2 * g.ntiles), 1024, TS::SMEM, st>>>(ws.bpos, ws.bw, ws.offsets, g, inv, halfcell, grid);
+    kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
+}
+
+// Fixed-point accumulation for unweighted deposits unless PYL_FLOAT_DEPOSIT is set
+// (a switch kept for measuring the two accumulators against each other).
+inline bool use_fixed_point()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("PYL_FLOAT_DEPOSIT");
+        v = (e && e[0] == '1') ? 0 : 1;
+    }
+    return v == 1;
 }
 
 template <int MAS>
@@ -508,7 +557,7 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
                  int dims, float inv, float halfcell, void *workspace, cudaStream_t st)
 {
     TileGeom g = tile_geom(dims);
-    TiledWs ws = tiled_layout(workspace, n, dims, w != nullptr);
+    TiledWs ws = tiled_layout(workspace, n, dims);
     const int T = (int)g.ntiles;
     if (ws.smem_hist) {
         const int C = ws.chunks;
@@ -525,11 +574,11 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         if (w) {
             PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
             chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                 ws.offsets, ws.bpos, ws.bw);
+                                                                 ws.offsets, ws.rec);
         } else {
             PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm, &d3));
             chunk_scatter_kernel<MAS, false><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                  ws.offsets, ws.bpos, ws.bw);
+                                                                  ws.offsets, ws.rec);
         }
         PYL_LAUNCH_CHECK();
     } else {
@@ -539,15 +588,17 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         PYL_LAUNCH_CHECK();
         tile_scan_kernel<<<1, 1024, 0, st>>>(ws.hist, g.ntiles, ws.offsets, ws.total);
         PYL_LAUNCH_CHECK();
-        if (w) tile_scatter_kernel<MAS, true><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.bpos, ws.bw);
-        else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.bpos, ws.bw);
+        if (w) tile_scatter_kernel<MAS, true><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.rec);
+        else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.rec);
         PYL_LAUNCH_CHECK();
     }
-    int rc = w ? launch_deposit<MAS, true, false>(ws, g, inv, halfcell, grid, st)
-               : launch_deposit<MAS, false, false>(ws, g, inv, halfcell, grid, st);
-    if (rc || !grid2) return rc;
-    return w ? launch_deposit<MAS, true, true>(ws, g, inv, halfcell, grid2, st)
-             : launch_deposit<MAS, false, true>(ws, g, inv, halfcell, grid2, st);
+    if (w) return grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, st)
+                        : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, st);
+    if (use_fixed_point())
+        return grid2 ? launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, st)
+                     : launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, st);
+    return grid2 ? launch_deposit<MAS, false, true, false>(ws, g, inv, halfcell, grid, grid2, st)
+                 : launch_deposit<MAS, false, false, false>(ws, g, inv, halfcell, grid, grid2, st);
 }
 
 inline int pick_strategy(int strategy, int ndim, int dims, long long n)
@@ -572,7 +623,7 @@ extern "C" size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims,
     if (n_particles < 0 || dims <= 0) return 0;
     const int s = pick_strategy(strategy, ndim, dims, n_particles);
     if (s == PYL_STRATEGY_TILED && ndim == 3)
-        return tiled_layout(nullptr, n_particles, dims, true).bytes;
+        return tiled_layout(nullptr, n_particles, dims).bytes;
     return 0;
 }
 
@@ -595,7 +646,7 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
     if (s == PYL_STRATEGY_SORTED) s = PYL_STRATEGY_TILED;
     if (s == PYL_STRATEGY_TILED && (ndim != 3 || n > 0xFFFFFFF0ll)) s = PYL_STRATEGY_ATOMIC;
     if (s == PYL_STRATEGY_TILED) {
-        const size_t need = tiled_layout(nullptr, n, dims, weights != nullptr).bytes;
+        const size_t need = tiled_layout(nullptr, n, dims).bytes;
         if (workspace_bytes < need || workspace == nullptr) {
             set_error("pyl_ma: tiled strategy needs " + std::to_string(need) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
