@@ -72,6 +72,22 @@ int pyl_ma(const float *pos, const float *weights, int64_t n_particles, int ndim
            int strategy, int renormalize_2d, void *workspace, size_t workspace_bytes,
            void *stream);
 
+/* Allocation-free mass assignment.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory around the call (code running
+ * during CUDA-graph capture, plugins inside a host framework that owns the
+ * device allocator, real-time loops that allocate nothing after start-up).
+ * Same deposit as pyl_ma with the tiled strategy (3D grids only, grid +=,
+ * optional interlaced grid), but the binning scratch lives in a fixed 16 MiB
+ * array compiled into the library, held by every GPU that loads it until the
+ * process exits.  Limits: n_particles <= 524288 and dims <= 512; larger
+ * requests return PYL_ERR_INVALID.  The first call on a device looks up the
+ * array's device address and sets kernel attributes; make that first call
+ * before any stream capture.  All calls share the one array, so calls that
+ * overlap on the GPU (different streams, or different host threads) race and
+ * must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
+int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n_particles, float *grid,
+                   float *grid_interlaced, int dims, float box_size, int mas, void *stream);
+
 /* ---- overdensity --------------------------------------------------------------
  * Replaces the callers' normalisation `delta /= mean; delta -= 1.0`
  * (library/Pk_library/Pk_snapshot.py:80-88, documentation/Documentation.md:93).

@@ -27,6 +27,8 @@
 
 #include <stdlib.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace pyl {
@@ -684,4 +686,79 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
         }
     }
     return PYL_OK;
+}
+
+// ------------------------------------------------------- allocation-free variant
+// Some callers cannot allocate device memory around a call: code that runs
+// while a CUDA graph is being captured (cudaMalloc is not a capturable
+// operation), plugins hosted by a framework whose allocator owns all device
+// memory, and real-time loops that forbid allocation after start-up.  For them,
+// pyl_ma_noalloc deposits through the same tiled kernels as pyl_ma but keeps
+// the binning scratch in a fixed array compiled into this library.
+namespace pyl {
+namespace {
+constexpr long long NOALLOC_MAX_PARTICLES = 1LL << 19;   // 524,288 particles
+constexpr int NOALLOC_MAX_DIMS = 512;                    // <= (512/32)^3 = 4096 bins
+constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;      // 16 MiB per device
+
+// Held by every GPU that loads the library until the process exits.
+__device__ __align__(256) unsigned char g_ma_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_scratch_mu;
+void *g_scratch_addr[64] = {};
+
+// Device address of g_ma_scratch on the current device (looked up once per device).
+int scratch_address(void **out)
+{
+    int dev = 0;
+    PYL_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("pyl_ma_noalloc: device index out of range");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        PYL_CUDA(cudaGetSymbolAddress(&p, g_ma_scratch));
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return PYL_OK;
+}
+}  // namespace
+}  // namespace pyl
+
+extern "C" int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n, float *grid,
+                              float *grid_interlaced, int dims, float box_size, int mas, void *stream)
+{
+    PYL_CHECK_ARG(mas >= PYL_MAS_NGP && mas <= PYL_MAS_PCS, "MAS must be NGP, CIC, TSC or PCS");
+    PYL_CHECK_ARG(grid != nullptr, "grid is NULL");
+    PYL_CHECK_ARG(n >= 0, "negative particle count");
+    PYL_CHECK_ARG(n == 0 || pos != nullptr, "pos is NULL");
+    PYL_CHECK_ARG(box_size > 0.0f && isfinite(box_size), "BoxSize must be positive and finite");
+    if (n > NOALLOC_MAX_PARTICLES || dims < 1 || dims > NOALLOC_MAX_DIMS) {
+        set_error("pyl_ma_noalloc: at most " + std::to_string(NOALLOC_MAX_PARTICLES) +
+                  " particles and dims <= " + std::to_string(NOALLOC_MAX_DIMS) +
+                  " (got " + std::to_string(n) + " particles, dims " + std::to_string(dims) +
+                  "); use pyl_ma with a workspace for larger inputs");
+        return PYL_ERR_INVALID;
+    }
+    const size_t need = tiled_layout(nullptr, n, dims).bytes;
+    if (need > NOALLOC_SCRATCH_BYTES) {
+        set_error("pyl_ma_noalloc: request needs " + std::to_string(need) + " scratch bytes");
+        return PYL_ERR_INVALID;
+    }
+    void *scratch = nullptr;
+    int rc = scratch_address(&scratch);
+    if (rc) return rc;
+    if (n == 0) return PYL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float inv = (float)dims / box_size;
+    const float halfcell = (float)(0.5 * (double)box_size / dims);
+    switch (mas) {
+        case PYL_MAS_NGP: return launch_tiled<PYL_MAS_NGP>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
+        case PYL_MAS_CIC: return launch_tiled<PYL_MAS_CIC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
+        case PYL_MAS_TSC: return launch_tiled<PYL_MAS_TSC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
+        default:          return launch_tiled<PYL_MAS_PCS>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
+    }
 }
