@@ -299,7 +299,7 @@ def stage_times(pp, pos, reps):
         _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, 2, st)
         ev[4].record()
         _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]), 1, pp.dk[0].numel(), d, pp.axis,
-                  pp.mas_p, ptr(pp.sums), None, 0, st)
+                  pp.mas_p, ptr(pp.sums), ptr(pp.pk_ws), pp.pk_ws_bytes, st)
         ev[5].record()
         torch.cuda.synchronize()
         acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]

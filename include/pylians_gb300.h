@@ -131,6 +131,8 @@ int pyl_fft_cache_clear(void);
  * pyl_pk_geometry fills the data-independent part (device, float64, zeroed):
  *   K1 [nb1] sum |k_par|, N1 [nb1], N2 [nb2], K3 [nb3] sum |k|, N3 [nb3]
  * (mode counts are exact integers stored as float64).
+ * Both take a workspace of pyl_pk_workspace_size() bytes (non-zero for axis 2
+ * only, where the rows are visited in k_per order).
  */
 int64_t pyl_pk_sums_len(int dims, int n_fields);
 int64_t pyl_pk_geometry_len(int dims);
@@ -138,7 +140,8 @@ size_t pyl_pk_workspace_size(int dims, int n_fields, int axis);
 int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_fields, int64_t field_stride,
                int dims, int axis, const int *host_mas_p, double *sums, void *workspace,
                size_t workspace_bytes, void *stream);
-int pyl_pk_geometry(int dims, int axis, double *geom, void *stream);
+int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t workspace_bytes,
+                    void *stream);
 
 /* In place: d <- (interlace-combined d) * W(k)^-1 as float32, on every stored
  * mode (Pk_library.pyx:353-355; bispectrum_library.pyx:107-109).  This is the

@@ -26,7 +26,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import as_device_c64, as_device_f32, is_torch, ptr, require_cuda, stream_ptr
+from ._device import as_device_c64, as_device_f32, is_torch, ptr, require_cuda, stream_ptr, workspace
 
 __all__ = ['frequencies', 'MAS_function', 'check_number_modes', 'FFT3Dr_f', 'IFFT3Dr_f',
            'Pk', 'XPk', 'Bk', 'Bk_triangles', 'pk_sums_device', 'finalize_pk', 'geometry']
@@ -93,7 +93,9 @@ def geometry(dims, axis, device=None):
         L = _lib.load()
         n = L.pyl_pk_geometry_len(dims)
         t = torch.empty(n, dtype=torch.float64, device=dev)
-        _lib.call('pyl_pk_geometry', dims, axis, ptr(t), stream_ptr())
+        nbytes = L.pyl_pk_workspace_size(dims, 1, axis)
+        ws = workspace.get(nbytes)
+        _lib.call('pyl_pk_geometry', dims, axis, ptr(t), ptr(ws), nbytes, stream_ptr())
         g = t.cpu().numpy()
         _GEOM[key] = g
     return g
@@ -125,8 +127,10 @@ def pk_sums_device(dk, dims, axis, mas_list, dk_interlaced=None, out=None, strea
         out = torch.empty(n, dtype=torch.float64, device=dk.device)
     mp, keep = ctypes_int_array(mas_list)
     fstride = dims * dims * (dims // 2 + 1)
+    nbytes = L.pyl_pk_workspace_size(dims, F, axis)
+    ws = workspace.get(nbytes)
     _lib.call('pyl_pk_bin', ptr(dk), ptr(dk_interlaced), F, fstride, dims, axis, mp, ptr(out),
-              None, 0, stream_ptr(stream))
+              ptr(ws), nbytes, stream_ptr(stream))
     del keep
     return out
 
@@ -209,10 +213,7 @@ class Pk(object):
         dk = _fields_to_dk([delta], dev)
         dk2 = _fields_to_dk([interlaced], dev) if interlaced is not None else None
         p = MAS_function(MAS)
-        mp = ctypes_int_array([p])
-        s = torch.empty(_lib.load().pyl_pk_sums_len(dims, 1), dtype=torch.float64, device=dev)
-        _lib.call('pyl_pk_bin', ptr(dk), ptr(dk2), 1, dk[0].numel(), dims, axis, mp[0], ptr(s),
-                  None, 0, stream_ptr())
+        s = pk_sums_device(dk, dims, axis, [p], dk2)
         geom = geometry(dims, axis)
         r = finalize_pk(s.cpu().numpy(), geom, BoxSize, dims, 1, cross=False)
         self.__dict__.update(r.__dict__)

@@ -1,0 +1,677 @@
+// Fused P(k) / XPk binning over cuFFT's R2C output, and the mode geometry.
+//
+// Restates the mode loops of library/Pk_library/Pk_library.pyx: Pk 311-381 and
+// XPk 625-737 (frequencies 59-64, MAS_correction 86-87, Hermitian-plane skip
+// 327-330, 1D bins for |k| <= N/2 364-367, 2D index (kmax_par+1)*k_per+k_par
+// 371, 3D l=0,2,4 and phase sums 376-381).  Bin indices are exact integer
+// square roots of kx^2+ky^2+kz^2, equal to the reference's (int)sqrt(double).
+//
+// Mapping: a warp walks a row (fixed kx, ky) 32 consecutive kz at a time, so
+// its loads are coalesced.  Along kz the 3D bin, and for axis 0/1 the 2D bin
+// k_per, never decrease, so a warp-level segmented sum (shuffles) collapses
+// each run of equal bins and only the run's last lane adds to shared memory.
+//   axis 0/1: a CTA owns rows of one plane (fixed kx for axis 0, ky for axis 1),
+//             which share k_par: 1D sums stay in registers, 2D sums (by k_per)
+//             in shared memory.
+//   axis 2:   k_par = kz.  Rows are visited in order of their k_per ring
+//             (a counting sort of the rows, done on the device each call), and
+//             each warp keeps private kz-indexed 2D and 1D sums in shared
+//             memory, flushed to float64 global sums when its ring changes.
+// Per-CTA float32 partial sums are flushed into the float64 `sums` with
+// float64 atomics.
+#include <cuda_runtime.h>
+
+#include "pk_common.cuh"
+
+namespace pyl {
+namespace {
+
+constexpr int MAX_FIELDS = 4;
+constexpr int MAX_CH = MAX_FIELDS + MAX_FIELDS * (MAX_FIELDS - 1) / 2;
+constexpr int NW = 8;                    // warps per CTA (256 threads)
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int KEY_NONE = 0x7fffffff;
+
+struct Seg {
+    int start;
+    bool tail;
+};
+
+// Segments of equal keys across the lanes of a warp (keys non-decreasing).
+__device__ __forceinline__ Seg seg_of(int key)
+{
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(FULL, key, 1);
+    const bool head = lane == 0 || key != prev;
+    const unsigned hm = __ballot_sync(FULL, head);
+    Seg s;
+    s.start = 31 - __clz(hm & (FULL >> (31 - lane)));
+    s.tail = lane == 31 || ((hm >> (lane + 1)) & 1u);
+    return s;
+}
+
+// Inclusive segmented sum; a segment's total sits on its tail lane.
+template <typename T>
+__device__ __forceinline__ T seg_sum(T v, int start)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const T y = __shfl_up_sync(FULL, v, o);
+        if (lane - o >= start) v += y;
+    }
+    return v;
+}
+
+struct BinArgs {
+    const float2 *dk, *dk2;
+    long long fstride;
+    int F, C, axis;
+    int mas_p[MAX_FIELDS];
+    double *sums;        // P3 | PH | P1 | P2 (float64)
+    double *geom;        // K1 | N1 | N2 | K3 | N3 (geometry kernel)
+    PkDims d;
+    const unsigned *rows;  // axis 2: row ids (kxx*dims + kyy) sorted by k_per ring
+    int chunks;            // axis 0/1: CTAs per plane
+    int rows_per_cta;      // axis 2: table entries per CTA
+    int warp_arrays;       // axis 2: per-warp kz arrays in shared memory
+};
+
+struct BinSmem {
+    int corr, ph, acc3, acc1, acc2, w, total;
+};
+
+__host__ __device__ inline BinSmem bin_smem(const PkDims &d, int F, int C, int axis, bool inter,
+                                            int warp_arrays)
+{
+    BinSmem s;
+    int o = 0;
+    s.corr = o; o += F * d.dims;
+    o = (o + 3) & ~3;                   // 16-byte aligned float2 phase table
+    s.ph = o; o += inter ? 2 * d.dims : 0;
+    s.acc3 = o; o += d.nb3 * (3 * C + F);
+    s.acc1 = o; o += d.nb1 * C;
+    s.acc2 = o; o += axis == 2 ? 0 : (d.kmax_per + 1) * C;
+    s.w = o; o += (axis == 2 && warp_arrays) ? NW * 2 * d.nz * C : 0;
+    s.total = o;
+    return s;
+}
+
+// Row sequence of CTA blockIdx.x: axis 0/1 interleave the rows of one plane
+// among the warps; axis 2 gives each warp a contiguous run of the ring table.
+struct RowIter {
+    int first, step, count;    // positions: first, first+step, ... (count of them)
+    int plane;
+};
+
+__device__ __forceinline__ RowIter row_iter(const BinArgs &a, int warp)
+{
+    RowIter it;
+    const int dims = a.d.dims;
+    if (a.axis != 2) {
+        it.plane = blockIdx.x / a.chunks;
+        const int chunk = blockIdx.x % a.chunks;
+        const int per = (dims + a.chunks - 1) / a.chunks;
+        const int r0 = chunk * per, r1 = min(dims, r0 + per);
+        it.first = r0 + warp;
+        it.step = NW;
+        it.count = it.first < r1 ? (r1 - it.first + NW - 1) / NW : 0;
+    } else {
+        it.plane = 0;
+        const long long total = (long long)dims * dims;
+        const long long b = (long long)blockIdx.x * a.rows_per_cta;
+        const long long e = min(total, b + a.rows_per_cta);
+        const int L = (a.rows_per_cta + NW - 1) / NW;
+        const long long wb = b + (long long)warp * L;
+        it.first = (int)wb;
+        it.step = 1;
+        it.count = wb < e ? (int)min((long long)L, e - wb) : 0;
+    }
+    return it;
+}
+
+__device__ __forceinline__ void row_coords(const BinArgs &a, const RowIter &it, int pos, int &kxx, int &kyy)
+{
+    const int dims = a.d.dims;
+    if (a.axis == 0)      { kxx = it.plane; kyy = pos; }
+    else if (a.axis == 1) { kxx = pos; kyy = it.plane; }
+    else {
+        const unsigned r = a.rows[pos];
+        kxx = (int)(r / (unsigned)dims);
+        kyy = (int)(r % (unsigned)dims);
+    }
+}
+
+template <bool INTER, int AXIS>
+__global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
+{
+    extern __shared__ float sm[];
+    const PkDims d = a.d;
+    const int F = a.F, C = a.C, dims = d.dims, nz = d.nz;
+    const BinSmem L = bin_smem(d, F, C, AXIS, INTER, a.warp_arrays);
+    float *corr = sm + L.corr;
+    float2 *ph = (float2 *)(sm + L.ph);
+    float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
+    const int slots3 = 3 * C + F;
+    for (int i = threadIdx.x; i < F * dims; i += blockDim.x) {
+        const int f = i / dims;
+        corr[i] = (float)mas_corr_d(freq_of(i % dims, dims), dims, a.mas_p[f]);
+    }
+    if (INTER) {
+        for (int i = threadIdx.x; i < dims; i += blockDim.x) {
+            double s, c;
+            sincospi((double)freq_of(i, dims) / dims, &s, &c);
+            ph[i] = make_float2((float)c, (float)s);
+        }
+    }
+    for (int i = L.acc3 + threadIdx.x; i < L.total; i += blockDim.x) sm[i] = 0.0f;
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long m2 = (long long)d.middle * d.middle;
+    double *P3 = a.sums;
+    double *PH = P3 + (long long)d.nb3 * 3 * C;
+    double *P1 = PH + (long long)d.nb3 * F;
+    double *P2 = P1 + (long long)d.nb1 * C;
+    float *w2 = sm + L.w + warp * 2 * nz * C;      // axis 2 with warp arrays
+    float *w1 = w2 + nz * C;
+    float r1[MAX_CH];
+#pragma unroll
+    for (int c = 0; c < MAX_CH; c++) r1[c] = 0.0f;
+    int cur_ring = -1;
+
+    const RowIter it = row_iter(a, warp);
+    for (int q = 0; q < it.count; q++) {
+        int kxx, kyy;
+        row_coords(a, it, it.first + q * it.step, kxx, kyy);
+        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
+        const long long row = ((long long)kxx * dims + kyy) * nz;
+        float cxy[MAX_FIELDS];
+#pragma unroll
+        for (int f = 0; f < MAX_FIELDS; f++)
+            cxy[f] = f < F ? __fmul_rn(corr[f * dims + kxx], corr[f * dims + kyy]) : 0.0f;
+        float2 pxy = make_float2(1.0f, 0.0f);
+        if (INTER) {
+            const float2 px = ph[kxx], py = ph[kyy];
+            pxy = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
+        }
+        const int ring = AXIS == 2 ? isqrt_exact(kx * kx + ky * ky) : 0;
+        if (AXIS == 2 && a.warp_arrays && ring != cur_ring) {
+            if (cur_ring >= 0) {
+                for (int kz = lane; kz < nz; kz += 32)
+                    for (int c = 0; c < C; c++) {
+                        const float v = w2[kz * C + c];
+                        if (v != 0.0f) {
+                            atomicAdd(P2 + ((long long)(d.kmax_par + 1) * cur_ring + kz) * C + c, (double)v);
+                            w2[kz * C + c] = 0.0f;
+                        }
+                    }
+            }
+            cur_ring = ring;
+        }
+        for (int kz0 = 0; kz0 < nz; kz0 += 32) {
+            const int kz = kz0 + lane;
+            const bool valid = kz < nz;
+            const bool live = valid && !hermitian_skip(kx, ky, kz, d);
+            const int n2 = kx * kx + ky * ky + kz * kz;
+            const int ki = valid ? isqrt_exact(n2) : KEY_NONE;
+            int kpar, kper;
+            if (AXIS == 0)      { kpar = kx; kper = isqrt_exact(ky * ky + kz * kz); }
+            else if (AXIS == 1) { kpar = ky; kper = isqrt_exact(kx * kx + kz * kz); }
+            else                { kpar = kz; kper = ring; }
+            const float mu2 = n2 ? __fdiv_rn((float)(kpar * kpar), (float)n2) : 0.0f;
+            const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
+            const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
+            if (kpar < 0) kpar = -kpar;
+            const bool in1d = (long long)n2 <= m2;
+            float re[MAX_FIELDS], im[MAX_FIELDS];
+            float2 pz = make_float2(1.0f, 0.0f);
+            if (INTER && valid) {
+                const float2 t = ph[kz];
+                pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
+            }
+#pragma unroll
+            for (int f = 0; f < MAX_FIELDS; f++) {
+                re[f] = 0.0f;
+                im[f] = 0.0f;
+                if (f < F && live) {
+                    float2 v = __ldg(a.dk + f * a.fstride + row + kz);
+                    if (INTER) {
+                        const float2 w = __ldg(a.dk2 + f * a.fstride + row + kz);
+                        v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
+                        v.y = 0.5f * (v.y + (w.x * pz.y + w.y * pz.x));
+                    }
+                    const float mf = __fmul_rn(cxy[f], corr[f * dims + kz]);
+                    re[f] = __fmul_rn(v.x, mf);
+                    im[f] = __fmul_rn(v.y, mf);
+                }
+            }
+            // channel values: autos then cross pairs (i<j)
+            float val[MAX_CH];
+#pragma unroll
+            for (int c = 0; c < MAX_CH; c++) val[c] = 0.0f;
+            {
+                int c = 0;
+#pragma unroll
+                for (int f = 0; f < MAX_FIELDS; f++)
+                    if (f < F) val[c++] = re[f] * re[f] + im[f] * im[f];
+#pragma unroll
+                for (int i = 0; i < MAX_FIELDS; i++)
+#pragma unroll
+                    for (int j = i + 1; j < MAX_FIELDS; j++)
+                        if (j < F) val[c++] = re[i] * re[j] + im[i] * im[j];
+            }
+            // 3D: segmented sums by |k| bin
+            const Seg s3 = seg_of(ki);
+            float *b3 = acc3 + (ki == KEY_NONE ? 0 : ki) * slots3;
+            const bool t3 = s3.tail && ki != KEY_NONE;
+#pragma unroll
+            for (int c = 0; c < MAX_CH; c++) {
+                if (c >= C) break;
+                const float v0 = seg_sum(val[c], s3.start);
+                const float v2 = seg_sum(val[c] * l2, s3.start);
+                const float v4 = seg_sum(val[c] * l4, s3.start);
+                if (t3) {
+                    atomicAdd(b3 + 3 * c, v0);
+                    atomicAdd(b3 + 3 * c + 1, v2);
+                    atomicAdd(b3 + 3 * c + 2, v4);
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < MAX_FIELDS; f++) {
+                if (f >= F) break;
+                const float p2 = val[f];
+                const float phase = p2 > 0.0f ? atanf(re[f] * rsqrtf(p2)) : 0.0f;
+                const float vph = seg_sum(phase * phase, s3.start);
+                if (t3) atomicAdd(b3 + 3 * C + f, vph);
+            }
+            if (AXIS != 2) {
+                // 2D by k_per (shared memory), 1D by the plane's k_par (registers)
+                const Seg s2 = seg_of(valid ? kper : KEY_NONE);
+                const bool t2 = s2.tail && valid;
+#pragma unroll
+                for (int c = 0; c < MAX_CH; c++) {
+                    if (c >= C) break;
+                    const float v = seg_sum(val[c], s2.start);
+                    if (t2) atomicAdd(acc2 + kper * C + c, v);
+                    if (in1d) r1[c] += val[c];
+                }
+            } else if (a.warp_arrays) {
+                if (valid) {
+#pragma unroll
+                    for (int c = 0; c < MAX_CH; c++) {
+                        if (c >= C) break;
+                        w2[kz * C + c] += val[c];
+                        if (in1d) w1[kz * C + c] += val[c];
+                    }
+                }
+            } else if (live) {
+#pragma unroll
+                for (int c = 0; c < MAX_CH; c++) {
+                    if (c >= C) break;
+                    atomicAdd(P2 + ((long long)(d.kmax_par + 1) * ring + kz) * C + c, (double)val[c]);
+                    if (in1d) atomicAdd(P1 + (long long)kz * C + c, (double)val[c]);
+                }
+            }
+        }
+    }
+    // per-warp flushes
+    if (AXIS != 2) {
+#pragma unroll
+        for (int c = 0; c < MAX_CH; c++) {
+            if (c >= C) break;
+            float v = r1[c];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+            if (lane == 0 && v != 0.0f) atomicAdd(acc1 + abs(freq_of(it.plane, dims)) * C + c, v);
+        }
+    } else if (a.warp_arrays) {
+        for (int kz = lane; kz < nz; kz += 32)
+            for (int c = 0; c < C; c++) {
+                const float v2 = w2[kz * C + c];
+                if (cur_ring >= 0 && v2 != 0.0f)
+                    atomicAdd(P2 + ((long long)(d.kmax_par + 1) * cur_ring + kz) * C + c, (double)v2);
+                const float v1 = w1[kz * C + c];
+                if (v1 != 0.0f) atomicAdd(P1 + (long long)kz * C + c, (double)v1);
+            }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d.nb3 * slots3; i += blockDim.x) {
+        const float v = acc3[i];
+        if (v == 0.0f) continue;
+        const int bin = i / slots3, s = i % slots3;
+        if (s < 3 * C) atomicAdd(P3 + ((long long)bin * 3 + s % 3) * C + s / 3, (double)v);
+        else atomicAdd(PH + (long long)bin * F + (s - 3 * C), (double)v);
+    }
+    if (AXIS != 2) {
+        for (int i = threadIdx.x; i < d.nb1 * C; i += blockDim.x) {
+            const float v = acc1[i];
+            if (v != 0.0f) atomicAdd(P1 + i, (double)v);
+        }
+        const int kpar = abs(freq_of(it.plane, dims));
+        for (int i = threadIdx.x; i < (d.kmax_per + 1) * C; i += blockDim.x) {
+            const float v = acc2[i];
+            if (v == 0.0f) continue;
+            atomicAdd(P2 + ((long long)(d.kmax_par + 1) * (i / C) + kpar) * C + i % C, (double)v);
+        }
+    }
+}
+
+// Data-independent per-bin sums with the same traversal: N3 and K3 = sum |k|
+// by 3D bin, N1 by |k_par| for |k| <= N/2 (K1 = |k_par| N1), N2 by 2D bin.
+// shared memory (doubles): N3[nb3] K3[nb3] N1[nb1] N2[kmax_per+1] (axis 0/1) or
+// per-warp kz arrays c2[NW][nz] c1[NW][nz] (axis 2).
+template <int AXIS>
+__global__ void __launch_bounds__(256) pk_geometry_kernel(BinArgs a)
+{
+    extern __shared__ double gs[];
+    const PkDims d = a.d;
+    const int dims = d.dims, nz = d.nz;
+    double *N3 = gs, *K3 = N3 + d.nb3, *N1 = K3 + d.nb3, *N2 = N1 + d.nb1;
+    const int nsm = 2 * d.nb3 + d.nb1 + (AXIS == 2 ? 2 * NW * nz : d.kmax_per + 1);
+    for (int i = threadIdx.x; i < nsm; i += blockDim.x) gs[i] = 0.0;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long m2 = (long long)d.middle * d.middle;
+    double *gK1 = a.geom, *gN1 = gK1 + d.nb1, *gN2 = gN1 + d.nb1, *gK3 = gN2 + d.nb2, *gN3 = gK3 + d.nb3;
+    double *c2 = N2 + warp * 2 * nz, *c1 = c2 + nz;   // axis 2
+    float n1reg = 0.0f;
+    int cur_ring = -1;
+    const RowIter it = row_iter(a, warp);
+    for (int q = 0; q < it.count; q++) {
+        int kxx, kyy;
+        row_coords(a, it, it.first + q * it.step, kxx, kyy);
+        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
+        const int ring = AXIS == 2 ? isqrt_exact(kx * kx + ky * ky) : 0;
+        if (AXIS == 2 && ring != cur_ring) {
+            if (cur_ring >= 0)
+                for (int kz = lane; kz < nz; kz += 32)
+                    if (c2[kz] != 0.0) {
+                        atomicAdd(gN2 + (long long)(d.kmax_par + 1) * cur_ring + kz, c2[kz]);
+                        c2[kz] = 0.0;
+                    }
+            cur_ring = ring;
+        }
+        for (int kz0 = 0; kz0 < nz; kz0 += 32) {
+            const int kz = kz0 + lane;
+            const bool valid = kz < nz;
+            const bool live = valid && !hermitian_skip(kx, ky, kz, d);
+            const int n2 = kx * kx + ky * ky + kz * kz;
+            const int ki = valid ? isqrt_exact(n2) : KEY_NONE;
+            const Seg s3 = seg_of(ki);
+            const float cnt = seg_sum(live ? 1.0f : 0.0f, s3.start);
+            const double ks = seg_sum(live ? sqrt((double)n2) : 0.0, s3.start);
+            if (s3.tail && ki != KEY_NONE && cnt != 0.0f) {
+                atomicAdd(N3 + ki, (double)cnt);
+                atomicAdd(K3 + ki, ks);
+            }
+            const bool in1d = live && (long long)n2 <= m2;
+            if (AXIS != 2) {
+                const int kper = AXIS == 0 ? isqrt_exact(ky * ky + kz * kz) : isqrt_exact(kx * kx + kz * kz);
+                const Seg s2 = seg_of(valid ? kper : KEY_NONE);
+                const float c = seg_sum(live ? 1.0f : 0.0f, s2.start);
+                if (s2.tail && valid && c != 0.0f) atomicAdd(N2 + kper, (double)c);
+                if (in1d) n1reg += 1.0f;
+            } else if (live) {
+                c2[kz] += 1.0;
+                if (in1d) c1[kz] += 1.0;
+            }
+        }
+    }
+    if (AXIS != 2) {
+        float v = n1reg;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(N1 + abs(freq_of(it.plane, dims)), (double)v);
+    } else {
+        for (int kz = lane; kz < nz; kz += 32) {
+            if (cur_ring >= 0 && c2[kz] != 0.0)
+                atomicAdd(gN2 + (long long)(d.kmax_par + 1) * cur_ring + kz, c2[kz]);
+            if (c1[kz] != 0.0) {
+                atomicAdd(gN1 + kz, c1[kz]);
+                atomicAdd(gK1 + kz, c1[kz] * kz);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d.nb3; i += blockDim.x)
+        if (N3[i] != 0.0) { atomicAdd(gN3 + i, N3[i]); atomicAdd(gK3 + i, K3[i]); }
+    if (AXIS != 2) {
+        for (int i = threadIdx.x; i < d.nb1; i += blockDim.x)
+            if (N1[i] != 0.0) { atomicAdd(gN1 + i, N1[i]); atomicAdd(gK1 + i, N1[i] * i); }
+        const int kpar = abs(freq_of(it.plane, dims));
+        for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x)
+            if (N2[i] != 0.0) atomicAdd(gN2 + (long long)(d.kmax_par + 1) * i + kpar, N2[i]);
+    }
+}
+
+// ---- ring table for axis 2: rows (kxx*dims + kyy) sorted by k_per = isqrt(kx^2+ky^2)
+__global__ void __launch_bounds__(256) ring_count_kernel(PkDims d, unsigned *cnt)
+{
+    extern __shared__ unsigned h[];
+    for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const long long total = (long long)d.dims * d.dims;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < total;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int kx = freq_of((int)(r / d.dims), d.dims), ky = freq_of((int)(r % d.dims), d.dims);
+        atomicAdd(h + isqrt_exact(kx * kx + ky * ky), 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x)
+        if (h[i]) atomicAdd(cnt + i, h[i]);
+}
+
+__global__ void __launch_bounds__(1024) ring_scan_kernel(const unsigned *cnt, int n, unsigned *cursor)
+{
+    __shared__ unsigned part[1024];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(n, b + per);
+    unsigned s = 0;
+    for (int i = b; i < e; i++) s += cnt[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const unsigned v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = part[threadIdx.x] - s;
+    for (int i = b; i < e; i++) { cursor[i] = run; run += cnt[i]; }
+}
+
+__global__ void __launch_bounds__(256) ring_fill_kernel(PkDims d, unsigned *cursor, unsigned *rows)
+{
+    const long long total = (long long)d.dims * d.dims;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < total;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int kx = freq_of((int)(r / d.dims), d.dims), ky = freq_of((int)(r % d.dims), d.dims);
+        rows[atomicAdd(cursor + isqrt_exact(kx * kx + ky * ky), 1u)] = (unsigned)r;
+    }
+}
+
+inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+struct RingWs {
+    unsigned *rows, *cnt, *cursor;
+    size_t bytes;
+};
+
+RingWs ring_layout(void *base, const PkDims &d)
+{
+    RingWs w;
+    char *b = (char *)base;
+    size_t off = 0;
+    w.rows = (unsigned *)(b + off); off = align256(off + sizeof(unsigned) * (size_t)d.dims * d.dims);
+    w.cnt = (unsigned *)(b + off); off = align256(off + sizeof(unsigned) * (d.kmax_per + 1));
+    w.cursor = (unsigned *)(b + off); off = align256(off + sizeof(unsigned) * (d.kmax_per + 1));
+    w.bytes = off;
+    return w;
+}
+
+int build_rings(const PkDims &d, const RingWs &w, cudaStream_t st)
+{
+    const int n = d.kmax_per + 1;
+    PYL_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned) * n, st));
+    const long long total = (long long)d.dims * d.dims;
+    int blocks = (int)min((total + 255) / 256, (long long)num_sms() * 4);
+    if (blocks < 1) blocks = 1;
+    ring_count_kernel<<<blocks, 256, sizeof(unsigned) * n, st>>>(d, w.cnt);
+    PYL_LAUNCH_CHECK();
+    ring_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, n, w.cursor);
+    PYL_LAUNCH_CHECK();
+    ring_fill_kernel<<<blocks, 256, 0, st>>>(d, w.cursor, w.rows);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
+inline int plane_chunks(int dims)
+{
+    int chunks = 1;
+    while ((long long)dims * chunks < 2LL * num_sms() && chunks * 8 < dims) chunks *= 2;
+    return chunks;
+}
+
+constexpr int RING_ROWS_PER_CTA = 256;
+constexpr size_t SMEM_LIMIT = 200 * 1024;
+
+}  // namespace
+}  // namespace pyl
+
+using namespace pyl;
+
+extern "C" size_t pyl_pk_workspace_size(int dims, int n_fields, int axis)
+{
+    (void)n_fields;
+    if (dims < 2 || axis != 2) return 0;
+    return ring_layout(nullptr, pk_dims(dims)).bytes;
+}
+
+extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_fields, int64_t field_stride,
+                          int dims, int axis, const int *host_mas_p, double *sums, void *workspace,
+                          size_t workspace_bytes, void *stream)
+{
+    PYL_CHECK_ARG(dk != nullptr && sums != nullptr && host_mas_p != nullptr, "null pointer");
+    PYL_CHECK_ARG(dims >= 2 && dims <= 8192, "dims out of range");
+    PYL_CHECK_ARG(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+    PYL_CHECK_ARG(n_fields >= 1, "need at least one field");
+    if (n_fields > MAX_FIELDS) {
+        set_error("pyl_pk_bin: at most 4 fields per call; bin larger sets pairwise");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    const PkDims d = pk_dims(dims);
+    const long long half = (long long)dims * dims * d.nz;
+    PYL_CHECK_ARG(n_fields == 1 || field_stride >= half, "field_stride smaller than one field");
+    BinArgs a;
+    a.dk = (const float2 *)dk;
+    a.dk2 = (const float2 *)dk_interlaced;
+    a.fstride = field_stride;
+    a.F = n_fields;
+    a.C = n_fields + n_fields * (n_fields - 1) / 2;
+    a.axis = axis;
+    a.sums = sums;
+    a.geom = nullptr;
+    a.d = d;
+    a.rows = nullptr;
+    for (int f = 0; f < MAX_FIELDS; f++) {
+        a.mas_p[f] = f < n_fields ? host_mas_p[f] : 0;
+        PYL_CHECK_ARG(a.mas_p[f] >= 0 && a.mas_p[f] <= 4, "MAS exponent must be 0..4");
+    }
+    const bool inter = dk_interlaced != nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned blocks;
+    if (axis == 2) {
+        const RingWs w = ring_layout(workspace, d);
+        if (workspace == nullptr || workspace_bytes < w.bytes) {
+            set_error("pyl_pk_bin: axis 2 needs " + std::to_string(w.bytes) + " workspace bytes");
+            return PYL_ERR_WORKSPACE;
+        }
+        int rc = build_rings(d, w, st);
+        if (rc) return rc;
+        a.rows = w.rows;
+        a.rows_per_cta = RING_ROWS_PER_CTA;
+        a.chunks = 1;
+        blocks = (unsigned)(((long long)dims * dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
+        a.warp_arrays = sizeof(float) * bin_smem(d, a.F, a.C, axis, inter, 1).total <= SMEM_LIMIT;
+    } else {
+        a.chunks = plane_chunks(dims);
+        a.rows_per_cta = 0;
+        a.warp_arrays = 0;
+        blocks = (unsigned)(dims * a.chunks);
+    }
+    const size_t smem = sizeof(float) * (size_t)bin_smem(d, a.F, a.C, axis, inter, a.warp_arrays).total;
+    if (smem > SMEM_LIMIT) {
+        set_error("pyl_pk_bin: bins for this grid and field count exceed shared memory");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, n_fields), st));
+#define PYL_BIN(I, A)                                                              \
+    do {                                                                           \
+        static size_t done = 0;                                                    \
+        PYL_CUDA(ensure_smem(pk_bin_kernel<I, A>, smem, &done));                   \
+        pk_bin_kernel<I, A><<<blocks, 256, smem, st>>>(a);                         \
+    } while (0)
+    if (inter) {
+        if (axis == 0) PYL_BIN(true, 0); else if (axis == 1) PYL_BIN(true, 1); else PYL_BIN(true, 2);
+    } else {
+        if (axis == 0) PYL_BIN(false, 0); else if (axis == 1) PYL_BIN(false, 1); else PYL_BIN(false, 2);
+    }
+#undef PYL_BIN
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
+extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t workspace_bytes,
+                               void *stream)
+{
+    PYL_CHECK_ARG(geom != nullptr, "null pointer");
+    PYL_CHECK_ARG(dims >= 2 && dims <= 8192, "dims out of range");
+    PYL_CHECK_ARG(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+    const PkDims d = pk_dims(dims);
+    cudaStream_t st = (cudaStream_t)stream;
+    BinArgs a;
+    a.dk = a.dk2 = nullptr;
+    a.fstride = 0;
+    a.F = a.C = 1;
+    a.axis = axis;
+    a.sums = nullptr;
+    a.geom = geom;
+    a.d = d;
+    a.rows = nullptr;
+    for (int f = 0; f < MAX_FIELDS; f++) a.mas_p[f] = 0;
+    unsigned blocks;
+    if (axis == 2) {
+        const RingWs w = ring_layout(workspace, d);
+        if (workspace == nullptr || workspace_bytes < w.bytes) {
+            set_error("pyl_pk_geometry: axis 2 needs " + std::to_string(w.bytes) + " workspace bytes");
+            return PYL_ERR_WORKSPACE;
+        }
+        int rc = build_rings(d, w, st);
+        if (rc) return rc;
+        a.rows = w.rows;
+        a.rows_per_cta = RING_ROWS_PER_CTA;
+        a.chunks = 1;
+        a.warp_arrays = 1;
+        blocks = (unsigned)(((long long)dims * dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
+    } else {
+        a.chunks = plane_chunks(dims);
+        a.rows_per_cta = 0;
+        a.warp_arrays = 0;
+        blocks = (unsigned)(dims * a.chunks);
+    }
+    const size_t smem = sizeof(double) * (2 * d.nb3 + d.nb1 + (axis == 2 ? 2 * NW * d.nz : d.kmax_per + 1));
+    if (smem > SMEM_LIMIT) {
+        set_error("pyl_pk_geometry: grid too large for the shared-memory bins");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    PYL_CUDA(cudaMemsetAsync(geom, 0, sizeof(double) * pyl_pk_geometry_len(dims), st));
+#define PYL_GEOM(A)                                                                \
+    do {                                                                           \
+        static size_t done = 0;                                                    \
+        PYL_CUDA(ensure_smem(pk_geometry_kernel<A>, smem, &done));                 \
+        pk_geometry_kernel<A><<<blocks, 256, smem, st>>>(a);                       \
+    } while (0)
+    if (axis == 0) PYL_GEOM(0); else if (axis == 1) PYL_GEOM(1); else PYL_GEOM(2);
+#undef PYL_GEOM
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}

@@ -39,6 +39,9 @@ class ParticlePk(object):
         self.mas_p, self._keep = PKL.ctypes_int_array([_lib.MAS_INDEX[MAS]])
         self.ws_bytes = 0
         self.ws = None
+        self.pk_ws_bytes = L.pyl_pk_workspace_size(d, 1, self.axis)
+        self.pk_ws = (torch.empty(self.pk_ws_bytes, dtype=torch.uint8, device=self.device)
+                      if self.pk_ws_bytes else None)
         self.reserve(max_particles, weighted)
         self.geom = PKL.geometry(d, self.axis, self.device)
         self.graph = None
@@ -78,7 +81,7 @@ class ParticlePk(object):
         _lib.call('pyl_fft_r2c', ptr(self.grids), ptr(self.dk), d, ng, st)
         dk2 = self.dk[1] if self.interlaced else None
         _lib.call('pyl_pk_bin', ptr(self.dk[0]), ptr(dk2), 1, self.dk[0].numel(), d, self.axis,
-                  self.mas_p, ptr(self.sums), None, 0, st)
+                  self.mas_p, ptr(self.sums), ptr(self.pk_ws), self.pk_ws_bytes, st)
         return self.sums
 
     def capture(self, pos, W=None):
