@@ -529,6 +529,135 @@ TiledWs tiled_layout(void *base, long long n, int dims)
     return ws;
 }
 
+// ---- full-bin fixed-point deposit (unweighted) ------------------------------
+// Shared memory per cell: a 32-bit low word (fraction, 2^-32 units) and an 8-bit
+// high byte (integer part) packed four to a word, 5 bytes per cell, so a whole
+// TB^3 bin plus halo fits one CTA.  The grids (plain, then interlaced) are
+// deposited one after the other; the second pass reads the bin's particles from
+// L2.  A contribution outside [0, 255) or a high byte that would pass 255 sets
+// a flag and the pass is redone with float32 shared atomics.
+template <int MAS, bool INTER>
+struct FxShape {
+    static constexpr int H = Support<MAS>::S - 1 + (INTER ? 1 : 0);
+    static constexpr int E = TB + H;
+    static constexpr int CELLS = E * E * E;
+    static constexpr int HIW = (CELLS + 3) / 4;
+    static constexpr size_t SMEM = sizeof(unsigned) * (CELLS + HIW);
+    static constexpr bool FITS = SMEM <= 227 * 1024;
+};
+
+__device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, float v, int *ovf)
+{
+    const unsigned long long q = __float2ull_rn(v * 4294967296.0f);
+    const unsigned ql = (unsigned)q, qh = (unsigned)(q >> 32);
+    unsigned carry = 0;
+    if (ql) {
+        const unsigned old = atomicAdd(lo + c, ql);
+        carry = (unsigned)(old + ql) < old ? 1u : 0u;
+    }
+    const unsigned inc = qh + carry;
+    if (inc) {
+        const int sh = 8 * (c & 3);
+        const unsigned old = atomicAdd(hiw + (c >> 2), inc << sh);
+        if (((old >> sh) & 0xffu) + inc > 255u) *ovf = 1;
+    }
+}
+
+template <int MAS, bool INTER>
+__global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
+    const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2)
+{
+    using FS = FxShape<MAS, INTER>;
+    constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
+    extern __shared__ unsigned smw[];
+    __shared__ int ovf;
+    unsigned *lo = smw, *hiw = smw + CELLS;
+    float *facc = (float *)smw;
+    const long long tile = blockIdx.x;
+    const unsigned begin = offsets[tile], end = offsets[tile + 1];
+    if (begin == end) return;
+    const int tz = (int)(tile % g.nt);
+    const int ty = (int)((tile / g.nt) % g.nt);
+    const int tx = (int)(tile / ((long long)g.nt * g.nt));
+    const int o[3] = {tx * TB, ty * TB, tz * TB};
+    const long long d = g.dims;
+    for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
+        for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
+            const int words = mode == 0 ? CELLS + FS::HIW : CELLS;
+            for (int c = threadIdx.x; c < words; c += blockDim.x) smw[c] = 0u;
+            if (threadIdx.x == 0) ovf = 0;
+            __syncthreads();
+            for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
+                const float4 r = rec[i];
+                const float p[3] = {r.x, r.y, r.z};
+                float C[3][S];
+                int loc[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const long long f0 = axis_first<MAS>(p[a], inv);
+                    loc[a] = wrap_index(f0, g.dims) - o[a];
+                    if (pass == 1) {
+                        const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+                        loc[a] += f > f0 ? 1 : 0;
+                    } else {
+                        axis_weights<MAS>(p[a], inv, C[a]);
+                    }
+                }
+#pragma unroll
+                for (int l = 0; l < S; l++)
+#pragma unroll
+                    for (int m = 0; m < S; m++) {
+                        const float c01 = __fmul_rn(C[0][l], C[1][m]);
+                        const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
+#pragma unroll
+                        for (int q = 0; q < S; q++) {
+                            const float v = __fmul_rn(c01, C[2][q]);
+                            if (mode == 1) atomicAdd(facc + row + q, v);
+                            else if (v >= 0.0f && v < 255.0f) fx8_add(lo, hiw, row + q, v, &ovf);
+                            else ovf = 1;
+                        }
+                    }
+            }
+            __syncthreads();
+            if (mode == 0 && ovf) {            // redo this pass in float32
+                __syncthreads();
+                continue;
+            }
+            float *out = pass == 0 ? grid : grid2;
+            for (int c = threadIdx.x; c < CELLS; c += blockDim.x) {
+                float v;
+                if (mode == 0) {
+                    const unsigned hb = (hiw[c >> 2] >> (8 * (c & 3))) & 0xffu;
+                    v = __ull2float_rn(((unsigned long long)hb << 32) | lo[c]) * 2.3283064365386963e-10f;
+                } else {
+                    v = facc[c];
+                }
+                if (v == 0.0f) continue;
+                const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+                const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
+                                gz = add_wrap(o[2], lz, d);
+                atomicAdd(out + (gx * d + gy) * d + gz, v);
+            }
+            __syncthreads();
+            break;
+        }
+    }
+}
+
+template <int MAS, bool I>
+int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
+                      float *grid2, cudaStream_t st)
+{
+    using FS = FxShape<MAS, I>;
+    auto kern = bin_deposit_fx_kernel<MAS, I>;
+    static size_t done = 0;
+    PYL_CUDA(ensure_smem(kern, FS::SMEM, &done));
+    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
 template <int MAS, bool W, bool I, bool FX>
 int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
                    float *grid2, cudaStream_t st)
@@ -540,18 +669,6 @@ int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, flo
     kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
-}
-
-// Fixed-point accumulation for unweighted deposits unless PYL_FLOAT_DEPOSIT is set
-// (a switch kept for measuring the two accumulators against each other).
-inline bool use_fixed_point()
-{
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("PYL_FLOAT_DEPOSIT");
-        v = (e && e[0] == '1') ? 0 : 1;
-    }
-    return v == 1;
 }
 
 template <int MAS>
@@ -596,11 +713,12 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
     }
     if (w) return grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, st)
                         : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, st);
-    if (use_fixed_point())
-        return grid2 ? launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, st)
-                     : launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, st);
-    return grid2 ? launch_deposit<MAS, false, true, false>(ws, g, inv, halfcell, grid, grid2, st)
-                 : launch_deposit<MAS, false, false, false>(ws, g, inv, halfcell, grid, grid2, st);
+    if (grid2) {
+        if (FxShape<MAS, true>::FITS) return launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, st);
+        return launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, st);
+    }
+    if (FxShape<MAS, false>::FITS) return launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, st);
+    return launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, st);
 }
 
 inline int pick_strategy(int strategy, int ndim, int dims, long long n)

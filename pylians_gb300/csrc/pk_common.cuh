@@ -47,4 +47,15 @@ __device__ __forceinline__ double mas_corr_d(int k, int dims, int p)
     return v;
 }
 
+// Same in float32: (x / sinf x)^p, x = pi k / dims.
+__device__ __forceinline__ float mas_corr_f(int k, int dims, int p)
+{
+    if (k == 0 || p == 0) return 1.0f;
+    const float x = (float)(M_PI / dims) * (float)k;
+    const float r = x / sinf(x);
+    float v = 1.0f;
+    for (int i = 0; i < p; i++) v *= r;
+    return v;
+}
+
 }  // namespace pyl

@@ -153,15 +153,17 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
     float2 *ph = (float2 *)(sm + L.ph);
     float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
     const int slots3 = 3 * C + F;
+    // Per-axis tables in float32 (fp64 is slow on this part; each factor is within
+    // an ulp of the reference's float64 value before the float32 product).
     for (int i = threadIdx.x; i < F * dims; i += blockDim.x) {
         const int f = i / dims;
-        corr[i] = (float)mas_corr_d(freq_of(i % dims, dims), dims, a.mas_p[f]);
+        corr[i] = mas_corr_f(freq_of(i % dims, dims), dims, a.mas_p[f]);
     }
     if (INTER) {
         for (int i = threadIdx.x; i < dims; i += blockDim.x) {
-            double s, c;
-            sincospi((double)freq_of(i, dims) / dims, &s, &c);
-            ph[i] = make_float2((float)c, (float)s);
+            float s, c;
+            sincospif((float)freq_of(i, dims) / (float)dims, &s, &c);
+            ph[i] = make_float2(c, s);
         }
     }
     for (int i = L.acc3 + threadIdx.x; i < L.total; i += blockDim.x) sm[i] = 0.0f;
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
             if (AXIS == 0)      { kpar = kx; kper = isqrt_exact(ky * ky + kz * kz); }
             else if (AXIS == 1) { kpar = ky; kper = isqrt_exact(kx * kx + kz * kz); }
             else                { kpar = kz; kper = ring; }
-            const float mu2 = n2 ? __fdiv_rn((float)(kpar * kpar), (float)n2) : 0.0f;
+            const float mu2 = n2 ? __fdividef((float)(kpar * kpar), (float)n2) : 0.0f;
             const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
             const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
             if (kpar < 0) kpar = -kpar;
