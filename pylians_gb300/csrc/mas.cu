@@ -37,50 +37,51 @@ namespace {
 template <int MAS>
 struct Support { static constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS; };
 
-// First cell (unwrapped) of the support of one particle coordinate.
+// First cell (unwrapped) of the support of one particle coordinate.  Cell
+// arithmetic is 32-bit (float->int64 conversions run on the slow fp64 pipe):
+// coordinates must satisfy |x * dims / BoxSize| < 2^31; beyond that the
+// conversion saturates and the cell still wraps into the grid.
 template <int MAS>
-__device__ __forceinline__ long long axis_first(float p, float inv)
+__device__ __forceinline__ int axis_first(float p, float inv)
 {
     const float dist = __fmul_rn(p, inv);
-    if (MAS == PYL_MAS_CIC) return (long long)truncf(dist);
+    if (MAS == PYL_MAS_CIC) return __float2int_rz(dist);
     const float fl = floorf(dist);
     const float frac = __fsub_rn(dist, fl);
+    const int fi = __float2int_rz(fl);
     if (MAS == PYL_MAS_NGP) {
-        long long k = (long long)fl + (frac >= 0.5f ? 1 : 0);
-        if (dist < -0.5f && frac != 0.5f) k += 1;
+        int k = fi + (frac >= 0.5f ? 1 : 0);              // floor(dist + 0.5)
+        if (dist < -0.5f && frac != 0.5f) k += 1;         // trunc for negative sums
         return k;
     }
-    if (MAS == PYL_MAS_TSC) return (long long)fl - 1 + (frac >= 0.5f ? 1 : 0);
-    return (long long)fl - 1;   // PCS
+    if (MAS == PYL_MAS_TSC) return fi - 1 + (frac >= 0.5f ? 1 : 0);
+    return fi - 1;                                        // PCS
 }
 
 // Per-axis support of one particle coordinate: first cell f (unwrapped) and the
 // S weights of cells f, f+1, ..., f+S-1.  f equals axis_first<MAS>(p, inv).
 template <int MAS>
-__device__ __forceinline__ long long axis_weights(float p, float inv, float *C)
+__device__ __forceinline__ int axis_weights(float p, float inv, float *C)
 {
     const float dist = __fmul_rn(p, inv);
     if (MAS == PYL_MAS_NGP) {
-        // <int>(dist + 0.5) with the sum in double (exact), truncation toward 0.
-        const float fl = floorf(dist);
-        const float frac = __fsub_rn(dist, fl);
-        long long k = (long long)fl + (frac >= 0.5f ? 1 : 0);       // floor(dist + 0.5)
-        if (dist < -0.5f && frac != 0.5f) k += 1;                  // trunc for negative sums
         C[0] = 1.0f;
-        return k;
+        return axis_first<MAS>(p, inv);
     } else if (MAS == PYL_MAS_CIC) {
-        const long long k = (long long)truncf(dist);
-        const float u = __fsub_rn(dist, truncf(dist));
+        // <int>dist truncates toward zero; u = dist - <int>dist, d = 1 - u
+        const float t = truncf(dist);
+        const float u = __fsub_rn(dist, t);
         C[0] = __fsub_rn(1.0f, u);
         C[1] = u;
-        return k;
+        return __float2int_rz(t);
     } else if (MAS == PYL_MAS_TSC) {
         const float fl = floorf(dist);
         const float frac = __fsub_rn(dist, fl);
-        const long long mn = (long long)fl - 2 + (frac >= 0.5f ? 1 : 0);  // floor(dist - 1.5)
+        const int mn = __float2int_rz(fl) - 2 + (frac >= 0.5f ? 1 : 0);  // floor(dist - 1.5)
+        const float fmn = __fsub_rn(__fadd_rn(fl, frac >= 0.5f ? 1.0f : 0.0f), 2.0f);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const float diff = fabsf(__fsub_rn((float)(mn + j + 1), dist));
+            const float diff = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
             float c;
             if (diff < 0.5f) {
                 c = __fsub_rn(0.75f, __fmul_rn(diff, diff));
@@ -94,10 +95,12 @@ __device__ __forceinline__ long long axis_weights(float p, float inv, float *C)
         }
         return mn + 1;
     } else {  // PCS
-        const long long mn = (long long)floorf(dist) - 2;  // floor(dist - 2)
+        const float fl = floorf(dist);
+        const int mn = __float2int_rz(fl) - 2;            // floor(dist - 2)
+        const float fmn = __fsub_rn(fl, 2.0f);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const float d = fabsf(__fsub_rn((float)(mn + j + 1), dist));
+            const float d = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
             float c;
             if (d < 1.0f) {
                 const float a = __fmul_rn(__fmul_rn(6.0f, d), d);
@@ -138,9 +141,9 @@ __global__ void __launch_bounds__(256) ma_atomic_kernel(
 #pragma unroll
             for (int a = 0; a < NDIM; a++) {
                 const float q = g == 0 ? p[a] : __fadd_rn(p[a], halfcell);
-                const long long f = axis_weights<MAS>(q, inv, C[a]);
+                const int f = axis_weights<MAS>(q, inv, C[a]);
 #pragma unroll
-                for (int j = 0; j < S; j++) idx[a][j] = wrap_index(f + j, dims);
+                for (int j = 0; j < S; j++) idx[a][j] = wrap_index((long long)f + j, dims);
             }
             if (NDIM == 3) {
 #pragma unroll
@@ -360,8 +363,10 @@ struct TileShape {
 // Integer sums do not depend on the order of the adds.
 __device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int c, float v)
 {
-    const unsigned long long q = (unsigned long long)__float2ll_rn(v * 4294967296.0f);
-    const unsigned ql = (unsigned)q, qh = (unsigned)(q >> 32);
+    // signed: floor gives the (possibly negative) integer part, the fraction is in [0, 1)
+    const float fi = floorf(v);
+    const unsigned qh = (unsigned)__float2int_rz(fi);
+    const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
     unsigned carry = 0;
     if (ql) {
         const unsigned old = atomicAdd(lo + c, ql);
@@ -372,25 +377,24 @@ __device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int c, float 
 
 __device__ __forceinline__ float fx_value(unsigned lo, unsigned hi)
 {
-    const long long s = (long long)(((unsigned long long)hi << 32) | lo);
-    return __ll2float_rn(s) * 2.3283064365386963e-10f;   // exact scaling by 2^-32
+    return __fadd_rn((float)(int)hi, __uint2float_rn(lo) * 2.3283064365386963e-10f);
 }
 
 // Weights and local first cells of one particle for the plain (G=0) or the
 // half-cell-shifted (G=1) grid; loc relative to the sub-tile origin o.
 template <int MAS, int G>
 __device__ __forceinline__ void particle_support(const float *p, float inv, float halfcell, int dims,
-                                                 const int *o, int lx0, long long fx0,
+                                                 const int *o, int lx0, int fx0,
                                                  float (*C)[Support<MAS>::S], int *loc)
 {
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const long long f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
+        const int f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
         loc[a] = a == 0 ? lx0 : wrap_index(f0, dims) - o[a];
         if (G == 1) {
             // the half-cell shift moves the first cell by 0 or +1; the clamp only
             // matters for non-finite or astronomically large positions
-            const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+            const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
             loc[a] += f > f0 ? 1 : 0;
         } else {
             axis_weights<MAS>(p[a], inv, C[a]);
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_kernel(
             for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
                 const float4 r = rec[i];
                 const float p[3] = {r.x, r.y, r.z};
-                const long long fx0 = axis_first<MAS>(p[0], inv);
+                const int fx0 = axis_first<MAS>(p[0], inv);
                 const int lx0 = wrap_index(fx0, g.dims) - o[0];
                 if (lx0 < 0 || lx0 >= HX) continue;          // the other half's particle
                 float C[3][S];
@@ -548,8 +552,11 @@ struct FxShape {
 
 __device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, float v, int *ovf)
 {
-    const unsigned long long q = __float2ull_rn(v * 4294967296.0f);
-    const unsigned ql = (unsigned)q, qh = (unsigned)(q >> 32);
+    // 0 <= v < 255: integer part to the high byte, the exact fraction (2^-32 units,
+    // rounded for fractions below 2^-8) to the low word; 32-bit conversions only
+    const float fi = floorf(v);
+    const unsigned qh = (unsigned)__float2int_rz(fi);
+    const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
     unsigned carry = 0;
     if (ql) {
         const unsigned old = atomicAdd(lo + c, ql);
@@ -595,10 +602,10 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
                 int loc[3];
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
-                    const long long f0 = axis_first<MAS>(p[a], inv);
+                    const int f0 = axis_first<MAS>(p[a], inv);
                     loc[a] = wrap_index(f0, g.dims) - o[a];
                     if (pass == 1) {
-                        const long long f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+                        const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
                         loc[a] += f > f0 ? 1 : 0;
                     } else {
                         axis_weights<MAS>(p[a], inv, C[a]);
@@ -629,7 +636,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
                 float v;
                 if (mode == 0) {
                     const unsigned hb = (hiw[c >> 2] >> (8 * (c & 3))) & 0xffu;
-                    v = __ull2float_rn(((unsigned long long)hb << 32) | lo[c]) * 2.3283064365386963e-10f;
+                    v = __fadd_rn((float)hb, __uint2float_rn(lo[c]) * 2.3283064365386963e-10f);
                 } else {
                     v = facc[c];
                 }

@@ -216,10 +216,10 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
             const bool valid = kz < nz;
             const bool live = valid && !hermitian_skip(kx, ky, kz, d);
             const int n2 = kx * kx + ky * ky + kz * kz;
-            const int ki = valid ? isqrt_exact(n2) : KEY_NONE;
+            const int ki = valid ? isqrt_fast(n2) : KEY_NONE;
             int kpar, kper;
-            if (AXIS == 0)      { kpar = kx; kper = isqrt_exact(ky * ky + kz * kz); }
-            else if (AXIS == 1) { kpar = ky; kper = isqrt_exact(kx * kx + kz * kz); }
+            if (AXIS == 0)      { kpar = kx; kper = isqrt_fast(ky * ky + kz * kz); }
+            else if (AXIS == 1) { kpar = ky; kper = isqrt_fast(kx * kx + kz * kz); }
             else                { kpar = kz; kper = ring; }
             const float mu2 = n2 ? __fdividef((float)(kpar * kpar), (float)n2) : 0.0f;
             const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
@@ -283,7 +283,8 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
             for (int f = 0; f < MAX_FIELDS; f++) {
                 if (f >= F) break;
                 const float p2 = val[f];
-                const float phase = p2 > 0.0f ? atanf(re[f] * rsqrtf(p2)) : 0.0f;
+                // phase = atan2(Re d, |d|) = atan(Re d / |d|), |Re d / |d|| <= 1
+                const float phase = p2 > 0.0f ? atan_unit(re[f] * rsqrtf(p2)) : 0.0f;
                 const float vph = seg_sum(phase * phase, s3.start);
                 if (t3) atomicAdd(b3 + 3 * C + f, vph);
             }
