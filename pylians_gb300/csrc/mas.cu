@@ -194,8 +194,8 @@ constexpr int HIST_MAX_TILES = 49152;
 constexpr int MAX_CHUNKS = 256;
 
 struct TileGeom {
-    int dims, nt;          // grid side, tiles per axis
-    long long ntiles;
+    int dims, nt, nc;      // grid side, tiles per axis, coarse blocks (4^3 tiles) per axis
+    long long ntiles;      // number of tile keys: nc^3 * 64 (keys of tiles past the grid stay empty)
 };
 
 __host__ __device__ inline TileGeom tile_geom(int dims)
@@ -203,8 +203,27 @@ __host__ __device__ inline TileGeom tile_geom(int dims)
     TileGeom g;
     g.dims = dims;
     g.nt = (dims + TB - 1) / TB;
-    g.ntiles = (long long)g.nt * g.nt * g.nt;
+    g.nc = (g.nt + 3) / 4;
+    g.ntiles = (long long)g.nc * g.nc * g.nc * 64;
     return g;
+}
+
+// Tile keys are coarse-major: key = coarse * 64 + local, coarse = (tx/4, ty/4, tz/4),
+// local = (tx%4, ty%4, tz%4), so the 64 tiles of a coarse block are contiguous.
+__host__ __device__ inline unsigned tile_key_of(int tx, int ty, int tz, const TileGeom &g)
+{
+    const unsigned coarse = ((unsigned)(tx >> 2) * g.nc + (ty >> 2)) * g.nc + (tz >> 2);
+    return coarse * 64u + (unsigned)(((tx & 3) << 4) | ((ty & 3) << 2) | (tz & 3));
+}
+
+__device__ __forceinline__ void tile_coords(long long key, const TileGeom &g, int &tx, int &ty, int &tz)
+{
+    const int local = (int)(key & 63);
+    const long long coarse = key >> 6;
+    const int cz = (int)(coarse % g.nc), cy = (int)((coarse / g.nc) % g.nc), cx = (int)(coarse / ((long long)g.nc * g.nc));
+    tx = cx * 4 + (local >> 4);
+    ty = cy * 4 + ((local >> 2) & 3);
+    tz = cz * 4 + (local & 3);
 }
 
 template <int MAS>
@@ -213,7 +232,7 @@ __device__ __forceinline__ unsigned tile_key(const float *p, float inv, const Ti
     const int cx = wrap_index(axis_first<MAS>(p[0], inv), g.dims);
     const int cy = wrap_index(axis_first<MAS>(p[1], inv), g.dims);
     const int cz = wrap_index(axis_first<MAS>(p[2], inv), g.dims);
-    return (unsigned)(((long long)(cx / TB) * g.nt + cy / TB) * g.nt + cz / TB);
+    return tile_key_of(cx / TB, cy / TB, cz / TB, g);
 }
 
 template <int MAS>
@@ -290,6 +309,186 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
             const long long i = i0 + (long long)u * blockDim.x;
             if (i < e) rec[atomicAdd(cur + key[u], 1u)] = r[u];
         }
+    }
+}
+
+// ---- two-level placement for grids with more than TWO_LEVEL_TILES tiles -----
+// Writing each particle straight to its tile leaves one partly filled L2 line
+// per (CTA, tile) open; past a few thousand tiles they no longer fit L2 and
+// every 16-byte record costs a DRAM read-modify-write.  So: level A sorts each
+// 4096-particle batch of a chunk by coarse block (4^3 tiles) in shared memory
+// and writes coalesced runs into a temporary buffer laid out [coarse][chunk];
+// level B splits each (chunk, coarse) segment into its 64 tiles, again through
+// a shared-memory sort, into the final [tile][chunk] layout.  Both levels place
+// exactly where the single-level scatter would (same per-(chunk, tile) ranges).
+constexpr int TWO_LEVEL_TILES = 4096;
+constexpr int LA_THREADS = 1024, LA_U = 4, LA_BATCH = LA_THREADS * LA_U;
+constexpr int LB_THREADS = 512, LB_U = 8, LB_BATCH = LB_THREADS * LB_U;
+
+// Exclusive scan of n <= blockDim.x values in place; returns nothing, needs a
+// 32-entry scratch.  All threads of the block must call it.
+__device__ __forceinline__ void block_exclusive_scan(unsigned *v, int n, unsigned *warp_tot)
+{
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = (blockDim.x + 31) >> 5;
+    unsigned x = t < n ? v[t] : 0u;
+    unsigned inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        unsigned wt = lane < nw ? warp_tot[lane] : 0u;
+        unsigned wi = wt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < nw) warp_tot[lane] = wi - wt;
+    }
+    __syncthreads();
+    if (t < n) v[t] = inc - x + warp_tot[w];
+    __syncthreads();
+}
+
+template <int MAS, bool WEIGHTED>
+__global__ void __launch_bounds__(LA_THREADS) level_a_kernel(
+    const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
+    TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
+    float4 *__restrict__ tmp)
+{
+    extern __shared__ unsigned la[];
+    const int NCO = g.nc * g.nc * g.nc;
+    const int T = (int)g.ntiles;
+    unsigned *cur = la, *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
+    float4 *stage = (float4 *)(la + ((3 * NCO + 32 + 3) & ~3));
+    unsigned short *sco = (unsigned short *)(stage + LA_BATCH);
+    const unsigned *row = colpre + (long long)blockIdx.x * T;
+    for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
+        unsigned sacc = 0;
+        for (int l = 0; l < 64; l++) sacc += row[co * 64 + l];
+        cur[co] = offsets[co * 64] + sacc;            // this chunk's slot in the coarse block
+    }
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    for (long long s0 = b; s0 < e; s0 += LA_BATCH) {
+        for (int co = threadIdx.x; co < NCO; co += blockDim.x) bcnt[co] = 0u;
+        __syncthreads();
+        float4 r[LA_U];
+        unsigned co_u[LA_U], rank[LA_U];
+#pragma unroll
+        for (int u = 0; u < LA_U; u++) {
+            const long long i = s0 + threadIdx.x + (long long)u * LA_THREADS;
+            co_u[u] = 0xffffffffu;
+            if (i < e) {
+                r[u] = make_float4(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2),
+                                   WEIGHTED ? __ldg(w + i) : 1.0f);
+                const float p[3] = {r[u].x, r[u].y, r[u].z};
+                co_u[u] = tile_key<MAS>(p, inv, g) >> 6;
+                rank[u] = atomicAdd(bcnt + co_u[u], 1u);
+            }
+        }
+        __syncthreads();
+        for (int co = threadIdx.x; co < NCO; co += blockDim.x) {   // global start of this batch's runs
+            gst[co] = cur[co];
+            cur[co] += bcnt[co];
+        }
+        __syncthreads();
+        block_exclusive_scan(bcnt, NCO, wt);                         // NCO <= 768 < blockDim.x
+#pragma unroll
+        for (int u = 0; u < LA_U; u++) {
+            if (co_u[u] != 0xffffffffu) {
+                const unsigned slot = bcnt[co_u[u]] + rank[u];
+                stage[slot] = r[u];
+                sco[slot] = (unsigned short)co_u[u];
+            }
+        }
+        __syncthreads();
+        const int nb = (int)min((long long)LA_BATCH, e - s0);
+        for (int sidx = threadIdx.x; sidx < nb; sidx += blockDim.x) {
+            const unsigned co = sco[sidx];
+            tmp[gst[co] + (sidx - bcnt[co])] = stage[sidx];
+        }
+        __syncthreads();
+    }
+}
+
+template <int MAS>
+__global__ void __launch_bounds__(LB_THREADS) level_b_kernel(
+    const float4 *__restrict__ tmp, int C, float inv, TileGeom g, const unsigned *__restrict__ colpre,
+    const unsigned *__restrict__ total, const unsigned *__restrict__ offsets, float4 *__restrict__ rec)
+{
+    __shared__ unsigned fcur[64], bcnt[64], gst[64], wt[32];
+    __shared__ unsigned seg_start, seg_len;
+    extern __shared__ float4 stage[];                       // LB_BATCH records, then slo
+    unsigned char *slo = (unsigned char *)(stage + LB_BATCH);
+    const int NCO = g.nc * g.nc * g.nc;
+    const int T = (int)g.ntiles;
+    const int c = blockIdx.x / NCO, co = blockIdx.x % NCO;
+    if (threadIdx.x < 32) {
+        // this chunk's segment of the coarse block: starts after the earlier chunks
+        unsigned pre = 0, len = 0;
+        for (int l = threadIdx.x; l < 64; l += 32) {
+            const int t = co * 64 + l;
+            const unsigned cp = colpre[(long long)c * T + t];
+            const unsigned nx = c + 1 < C ? colpre[(long long)(c + 1) * T + t] : total[t];
+            fcur[l] = offsets[t] + cp;
+            pre += cp;
+            len += nx - cp;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            pre += __shfl_down_sync(0xffffffffu, pre, o);
+            len += __shfl_down_sync(0xffffffffu, len, o);
+        }
+        if (threadIdx.x == 0) {
+            seg_start = offsets[co * 64] + pre;
+            seg_len = len;
+        }
+    }
+    __syncthreads();
+    const unsigned start = seg_start, len = seg_len;
+    for (unsigned s0 = 0; s0 < len; s0 += LB_BATCH) {
+        if (threadIdx.x < 64) bcnt[threadIdx.x] = 0u;
+        __syncthreads();
+        float4 r[LB_U];
+        int lo_u[LB_U];
+        unsigned rank[LB_U];
+#pragma unroll
+        for (int u = 0; u < LB_U; u++) {
+            const unsigned i = s0 + threadIdx.x + u * LB_THREADS;
+            lo_u[u] = -1;
+            if (i < len) {
+                r[u] = tmp[start + i];
+                const float p[3] = {r[u].x, r[u].y, r[u].z};
+                lo_u[u] = (int)(tile_key<MAS>(p, inv, g) & 63u);
+                rank[u] = atomicAdd(bcnt + lo_u[u], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 64) {
+            gst[threadIdx.x] = fcur[threadIdx.x];
+            fcur[threadIdx.x] += bcnt[threadIdx.x];
+        }
+        __syncthreads();
+        block_exclusive_scan(bcnt, 64, wt);
+#pragma unroll
+        for (int u = 0; u < LB_U; u++) {
+            if (lo_u[u] >= 0) {
+                const unsigned slot = bcnt[lo_u[u]] + rank[u];
+                stage[slot] = r[u];
+                slo[slot] = (unsigned char)lo_u[u];
+            }
+        }
+        __syncthreads();
+        const int nb = (int)min((unsigned)LB_BATCH, len - s0);
+        for (int sidx = threadIdx.x; sidx < nb; sidx += blockDim.x) {
+            const int l = slo[sidx];
+            rec[gst[l] + (sidx - bcnt[l])] = stage[sidx];
+        }
+        __syncthreads();
     }
 }
 
@@ -418,9 +617,8 @@ __global__ void __launch_bounds__(1024) bin_deposit_kernel(
     const long long tile = blockIdx.x;
     const unsigned begin = offsets[tile], end = offsets[tile + 1];
     if (begin == end) return;
-    const int tz = (int)(tile % g.nt);
-    const int ty = (int)((tile / g.nt) % g.nt);
-    const int tx = (int)(tile / ((long long)g.nt * g.nt));
+    int tx, ty, tz;
+    tile_coords(tile, g, tx, ty, tz);
     const long long d = g.dims;
     constexpr int PASSES = FIXED && INTER ? 2 : 1;
     for (int half = 0; half < 2; half++) {
@@ -509,6 +707,7 @@ int launch_atomic(const float *pos, const float *w, long long n, float *grid, fl
 struct TiledWs {
     unsigned *hist, *total, *offsets;
     float4 *rec;                 // binned particles: x, y, z, weight
+    float4 *tmp;                 // two-level placement: the coarse-block layout
     int chunks;
     bool smem_hist;
     size_t bytes;
@@ -529,6 +728,11 @@ TiledWs tiled_layout(void *base, long long n, int dims)
     ws.total = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.offsets = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * (g.ntiles + 1), 256);
     ws.rec = (float4 *)(b + off); off = align_up(off + sizeof(float4) * (size_t)n, 256);
+    ws.tmp = nullptr;
+    if (ws.smem_hist && g.ntiles > TWO_LEVEL_TILES) {
+        ws.tmp = (float4 *)(b + off);
+        off = align_up(off + sizeof(float4) * (size_t)n, 256);
+    }
     ws.bytes = off;
     return ws;
 }
@@ -584,9 +788,8 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     const long long tile = blockIdx.x;
     const unsigned begin = offsets[tile], end = offsets[tile + 1];
     if (begin == end) return;
-    const int tz = (int)(tile % g.nt);
-    const int ty = (int)((tile / g.nt) % g.nt);
-    const int tx = (int)(tile / ((long long)g.nt * g.nt));
+    int tx, ty, tz;
+    tile_coords(tile, g, tx, ty, tz);
     const int o[3] = {tx * TB, ty * TB, tz * TB};
     const long long d = g.dims;
     for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
@@ -697,7 +900,26 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         PYL_LAUNCH_CHECK();
         tile_scan_kernel<<<1, 1024, 0, st>>>(ws.total, T, ws.offsets, nullptr);
         PYL_LAUNCH_CHECK();
-        if (w) {
+        if (ws.tmp) {
+            const int NCO = g.nc * g.nc * g.nc;
+            const size_t sa = sizeof(unsigned) * ((3 * NCO + 32 + 3) & ~3) + sizeof(float4) * LA_BATCH +
+                              sizeof(unsigned short) * LA_BATCH;
+            const size_t sb = sizeof(float4) * LB_BATCH + LB_BATCH;
+            static size_t da = 0, db = 0, dc = 0;
+            if (w) {
+                PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa, &da));
+                level_a_kernel<MAS, true><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                    ws.offsets, ws.tmp);
+            } else {
+                PYL_CUDA(ensure_smem(level_a_kernel<MAS, false>, sa, &db));
+                level_a_kernel<MAS, false><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                     ws.offsets, ws.tmp);
+            }
+            PYL_LAUNCH_CHECK();
+            PYL_CUDA(ensure_smem(level_b_kernel<MAS>, sb, &dc));
+            level_b_kernel<MAS><<<(unsigned)(C * NCO), LB_THREADS, sb, st>>>(ws.tmp, C, inv, g, ws.hist,
+                                                                           ws.total, ws.offsets, ws.rec);
+        } else if (w) {
             PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
             chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                  ws.offsets, ws.rec);

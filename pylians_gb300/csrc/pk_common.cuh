@@ -47,12 +47,13 @@ __device__ __forceinline__ double mas_corr_d(int k, int dims, int p)
     return v;
 }
 
-// Same in float32: (x / sinf x)^p, x = pi k / dims.
+// Same in float32: (x / sin x)^p, x = pi t, t = k / dims (sinpif needs no
+// large-argument reduction, so no local-memory path).
 __device__ __forceinline__ float mas_corr_f(int k, int dims, int p)
 {
     if (k == 0 || p == 0) return 1.0f;
-    const float x = (float)(M_PI / dims) * (float)k;
-    const float r = x / sinf(x);
+    const float t = (float)k / (float)dims;
+    const float r = ((float)M_PI * t) / sinpif(t);
     float v = 1.0f;
     for (int i = 0; i < p; i++) v *= r;
     return v;

@@ -27,7 +27,6 @@ namespace pyl {
 namespace {
 
 constexpr int MAX_FIELDS = 4;
-constexpr int MAX_CH = MAX_FIELDS + MAX_FIELDS * (MAX_FIELDS - 1) / 2;
 constexpr int NW = 8;                    // warps per CTA (256 threads)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int KEY_NONE = 0x7fffffff;
@@ -142,12 +141,13 @@ __device__ __forceinline__ void row_coords(const BinArgs &a, const RowIter &it, 
     }
 }
 
-template <bool INTER, int AXIS>
+template <bool INTER, int AXIS, int F>
 __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
 {
+    constexpr int C = F + F * (F - 1) / 2;          // autos, then cross pairs
     extern __shared__ float sm[];
     const PkDims d = a.d;
-    const int F = a.F, C = a.C, dims = d.dims, nz = d.nz;
+    const int dims = d.dims, nz = d.nz;
     const BinSmem L = bin_smem(d, F, C, AXIS, INTER, a.warp_arrays);
     float *corr = sm + L.corr;
     float2 *ph = (float2 *)(sm + L.ph);
@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
     // an ulp of the reference's float64 value before the float32 product).
     for (int i = threadIdx.x; i < F * dims; i += blockDim.x) {
         const int f = i / dims;
-        corr[i] = mas_corr_f(freq_of(i % dims, dims), dims, a.mas_p[f]);
+        const int p = f == 0 ? a.mas_p[0] : f == 1 ? a.mas_p[1] : f == 2 ? a.mas_p[2] : a.mas_p[3];
+        corr[i] = mas_corr_f(freq_of(i % dims, dims), dims, p);
     }
     if (INTER) {
         for (int i = threadIdx.x; i < dims; i += blockDim.x) {
@@ -177,9 +178,9 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
     double *P2 = P1 + (long long)d.nb1 * C;
     float *w2 = sm + L.w + warp * 2 * nz * C;      // axis 2 with warp arrays
     float *w1 = w2 + nz * C;
-    float r1[MAX_CH];
+    float r1[C];
 #pragma unroll
-    for (int c = 0; c < MAX_CH; c++) r1[c] = 0.0f;
+    for (int c = 0; c < C; c++) r1[c] = 0.0f;
     int cur_ring = -1;
 
     const RowIter it = row_iter(a, warp);
@@ -188,10 +189,9 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
         row_coords(a, it, it.first + q * it.step, kxx, kyy);
         const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
         const long long row = ((long long)kxx * dims + kyy) * nz;
-        float cxy[MAX_FIELDS];
+        float cxy[F];
 #pragma unroll
-        for (int f = 0; f < MAX_FIELDS; f++)
-            cxy[f] = f < F ? __fmul_rn(corr[f * dims + kxx], corr[f * dims + kyy]) : 0.0f;
+        for (int f = 0; f < F; f++) cxy[f] = __fmul_rn(corr[f * dims + kxx], corr[f * dims + kyy]);
         float2 pxy = make_float2(1.0f, 0.0f);
         if (INTER) {
             const float2 px = ph[kxx], py = ph[kyy];
@@ -226,17 +226,17 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
             const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
             if (kpar < 0) kpar = -kpar;
             const bool in1d = (long long)n2 <= m2;
-            float re[MAX_FIELDS], im[MAX_FIELDS];
+            float re[F], im[F];
             float2 pz = make_float2(1.0f, 0.0f);
             if (INTER && valid) {
                 const float2 t = ph[kz];
                 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
             }
 #pragma unroll
-            for (int f = 0; f < MAX_FIELDS; f++) {
+            for (int f = 0; f < F; f++) {
                 re[f] = 0.0f;
                 im[f] = 0.0f;
-                if (f < F && live) {
+                if (live) {
                     float2 v = __ldg(a.dk + f * a.fstride + row + kz);
                     if (INTER) {
                         const float2 w = __ldg(a.dk2 + f * a.fstride + row + kz);
@@ -249,27 +249,19 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
                 }
             }
             // channel values: autos then cross pairs (i<j)
-            float val[MAX_CH];
+            float val[C];
 #pragma unroll
-            for (int c = 0; c < MAX_CH; c++) val[c] = 0.0f;
-            {
-                int c = 0;
+            for (int f = 0; f < F; f++) val[f] = re[f] * re[f] + im[f] * im[f];
 #pragma unroll
-                for (int f = 0; f < MAX_FIELDS; f++)
-                    if (f < F) val[c++] = re[f] * re[f] + im[f] * im[f];
+            for (int i = 0, c = F; i < F; i++)
 #pragma unroll
-                for (int i = 0; i < MAX_FIELDS; i++)
-#pragma unroll
-                    for (int j = i + 1; j < MAX_FIELDS; j++)
-                        if (j < F) val[c++] = re[i] * re[j] + im[i] * im[j];
-            }
+                for (int j = i + 1; j < F; j++, c++) val[c] = re[i] * re[j] + im[i] * im[j];
             // 3D: segmented sums by |k| bin
             const Seg s3 = seg_of(ki);
             float *b3 = acc3 + (ki == KEY_NONE ? 0 : ki) * slots3;
             const bool t3 = s3.tail && ki != KEY_NONE;
 #pragma unroll
-            for (int c = 0; c < MAX_CH; c++) {
-                if (c >= C) break;
+            for (int c = 0; c < C; c++) {
                 const float v0 = seg_sum(val[c], s3.start);
                 const float v2 = seg_sum(val[c] * l2, s3.start);
                 const float v4 = seg_sum(val[c] * l4, s3.start);
@@ -280,8 +272,7 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
                 }
             }
 #pragma unroll
-            for (int f = 0; f < MAX_FIELDS; f++) {
-                if (f >= F) break;
+            for (int f = 0; f < F; f++) {
                 const float p2 = val[f];
                 // phase = atan2(Re d, |d|) = atan(Re d / |d|), |Re d / |d|| <= 1
                 const float phase = p2 > 0.0f ? atan_unit(re[f] * rsqrtf(p2)) : 0.0f;
@@ -293,8 +284,7 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
                 const Seg s2 = seg_of(valid ? kper : KEY_NONE);
                 const bool t2 = s2.tail && valid;
 #pragma unroll
-                for (int c = 0; c < MAX_CH; c++) {
-                    if (c >= C) break;
+                for (int c = 0; c < C; c++) {
                     const float v = seg_sum(val[c], s2.start);
                     if (t2) atomicAdd(acc2 + kper * C + c, v);
                     if (in1d) r1[c] += val[c];
@@ -302,16 +292,14 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
             } else if (a.warp_arrays) {
                 if (valid) {
 #pragma unroll
-                    for (int c = 0; c < MAX_CH; c++) {
-                        if (c >= C) break;
+                    for (int c = 0; c < C; c++) {
                         w2[kz * C + c] += val[c];
                         if (in1d) w1[kz * C + c] += val[c];
                     }
                 }
             } else if (live) {
 #pragma unroll
-                for (int c = 0; c < MAX_CH; c++) {
-                    if (c >= C) break;
+                for (int c = 0; c < C; c++) {
                     atomicAdd(P2 + ((long long)(d.kmax_par + 1) * ring + kz) * C + c, (double)val[c]);
                     if (in1d) atomicAdd(P1 + (long long)kz * C + c, (double)val[c]);
                 }
@@ -321,8 +309,7 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
     // per-warp flushes
     if (AXIS != 2) {
 #pragma unroll
-        for (int c = 0; c < MAX_CH; c++) {
-            if (c >= C) break;
+        for (int c = 0; c < C; c++) {
             float v = r1[c];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
             if (lane == 0 && v != 0.0f) atomicAdd(acc1 + abs(freq_of(it.plane, dims)) * C + c, v);
@@ -607,17 +594,27 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
         return PYL_ERR_UNSUPPORTED;
     }
     PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, n_fields), st));
-#define PYL_BIN(I, A)                                                              \
+#define PYL_BIN(I, A, FF)                                                          \
     do {                                                                           \
         static size_t done = 0;                                                    \
-        PYL_CUDA(ensure_smem(pk_bin_kernel<I, A>, smem, &done));                   \
-        pk_bin_kernel<I, A><<<blocks, 256, smem, st>>>(a);                         \
+        PYL_CUDA(ensure_smem(pk_bin_kernel<I, A, FF>, smem, &done));               \
+        pk_bin_kernel<I, A, FF><<<blocks, 256, smem, st>>>(a);                     \
+    } while (0)
+#define PYL_BIN_F(I, A)                                                            \
+    do {                                                                           \
+        switch (n_fields) {                                                        \
+            case 1: PYL_BIN(I, A, 1); break;                                       \
+            case 2: PYL_BIN(I, A, 2); break;                                       \
+            case 3: PYL_BIN(I, A, 3); break;                                       \
+            default: PYL_BIN(I, A, 4); break;                                      \
+        }                                                                          \
     } while (0)
     if (inter) {
-        if (axis == 0) PYL_BIN(true, 0); else if (axis == 1) PYL_BIN(true, 1); else PYL_BIN(true, 2);
+        if (axis == 0) PYL_BIN_F(true, 0); else if (axis == 1) PYL_BIN_F(true, 1); else PYL_BIN_F(true, 2);
     } else {
-        if (axis == 0) PYL_BIN(false, 0); else if (axis == 1) PYL_BIN(false, 1); else PYL_BIN(false, 2);
+        if (axis == 0) PYL_BIN_F(false, 0); else if (axis == 1) PYL_BIN_F(false, 1); else PYL_BIN_F(false, 2);
     }
+#undef PYL_BIN_F
 #undef PYL_BIN
     PYL_LAUNCH_CHECK();
     return PYL_OK;

@@ -179,3 +179,25 @@ def test_bad_input_raises(MASL):
         MASL.MA(np.zeros((4, 2), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'CIC')
     with pytest.raises(ValueError):
         MASL.MA(np.zeros((4, 3), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'XYZ')
+
+
+@pytest.mark.parametrize('mas', ['NGP', 'CIC'])
+def test_two_level_placement_matches_atomic(MASL, mas):
+    """Grids with more than 4096 tiles place particles in two levels (coarse blocks,
+    then tiles); 544^3 has 17^3 tiles in ragged 4^3 coarse blocks.  Weighted and
+    unweighted, plain and interlaced grids must equal the atomic strategy's."""
+    rng = np.random.default_rng(11)
+    N, L, n = 544, 1000.0, 3_000_000
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    w = torch.from_numpy((rng.random(n) * 2).astype(np.float32)).cuda()
+    for W in (None, w):
+        a1 = torch.zeros((N, N, N), device='cuda'); a2 = torch.zeros((N, N, N), device='cuda')
+        b1 = torch.zeros((N, N, N), device='cuda'); b2 = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(pos, a1, L, mas, W, interlaced=a2, strategy='atomic')
+        MASL.MA(pos, b1, L, mas, W, interlaced=b2, strategy='tiled')
+        for a, b in ((a1, b1), (a2, b2)):
+            if mas == 'NGP' and W is None:
+                assert torch.equal(a, b)
+            else:
+                assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
+        del a1, a2, b1, b2
