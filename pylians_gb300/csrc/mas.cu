@@ -754,23 +754,28 @@ struct FxShape {
     static constexpr bool FITS = SMEM <= 227 * 1024;
 };
 
+__device__ __forceinline__ void fx8_carry(unsigned *hiw, int c, unsigned inc, int *ovf)
+{
+    const int sh = 8 * (c & 3);
+    const unsigned old = atomicAdd(hiw + (c >> 2), inc << sh);
+    if (((old >> sh) & 0xffu) + inc > 255u) *ovf = 1;
+}
+
+// Adds v (0 <= v < 255) to cell c.  Hot path v < 1: one returning atomic on the
+// low word, the high byte only on a carry.
 __device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, float v, int *ovf)
 {
-    // 0 <= v < 255: integer part to the high byte, the exact fraction (2^-32 units,
-    // rounded for fractions below 2^-8) to the low word; 32-bit conversions only
-    const float fi = floorf(v);
-    const unsigned qh = (unsigned)__float2int_rz(fi);
-    const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
-    unsigned carry = 0;
-    if (ql) {
+    if (v < 1.0f) {
+        const unsigned ql = __float2uint_rn(v * 4294967296.0f);   // < 2^32 for v < 1
         const unsigned old = atomicAdd(lo + c, ql);
-        carry = (unsigned)(old + ql) < old ? 1u : 0u;
-    }
-    const unsigned inc = qh + carry;
-    if (inc) {
-        const int sh = 8 * (c & 3);
-        const unsigned old = atomicAdd(hiw + (c >> 2), inc << sh);
-        if (((old >> sh) & 0xffu) + inc > 255u) *ovf = 1;
+        if (old + ql < old) fx8_carry(hiw, c, 1u, ovf);
+    } else if (v < 255.0f) {
+        const float fi = floorf(v);
+        const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
+        const unsigned old = atomicAdd(lo + c, ql);
+        fx8_carry(hiw, c, (unsigned)__float2int_rz(fi) + (old + ql < old ? 1u : 0u), ovf);
+    } else {
+        *ovf = 1;                                   // includes NaN
     }
 }
 
@@ -781,7 +786,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
 {
     using FS = FxShape<MAS, INTER>;
     constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
-    extern __shared__ unsigned smw[];
+    extern __shared__ __align__(16) unsigned smw[];
     __shared__ int ovf;
     unsigned *lo = smw, *hiw = smw + CELLS;
     float *facc = (float *)smw;
@@ -792,40 +797,43 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     tile_coords(tile, g, tx, ty, tz);
     const int o[3] = {tx * TB, ty * TB, tz * TB};
     const long long d = g.dims;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
         for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
             const int words = mode == 0 ? CELLS + FS::HIW : CELLS;
-            for (int c = threadIdx.x; c < words; c += blockDim.x) smw[c] = 0u;
+            uint4 *z4 = (uint4 *)smw;
+            for (int c = threadIdx.x; c < words / 4; c += blockDim.x) z4[c] = make_uint4(0u, 0u, 0u, 0u);
+            for (int c = (words / 4) * 4 + threadIdx.x; c < words; c += blockDim.x) smw[c] = 0u;
             if (threadIdx.x == 0) ovf = 0;
             __syncthreads();
             for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
                 const float4 r = rec[i];
                 const float p[3] = {r.x, r.y, r.z};
                 float C[3][S];
-                int loc[3];
+                int base = 0;
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
-                    const int f0 = axis_first<MAS>(p[a], inv);
-                    loc[a] = wrap_index(f0, g.dims) - o[a];
+                    int loc;
                     if (pass == 1) {
+                        const int f0 = axis_first<MAS>(p[a], inv);
                         const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
-                        loc[a] += f > f0 ? 1 : 0;
+                        loc = wrap_index(f0, g.dims) - o[a] + (f > f0 ? 1 : 0);
                     } else {
-                        axis_weights<MAS>(p[a], inv, C[a]);
+                        loc = wrap_index(axis_weights<MAS>(p[a], inv, C[a]), g.dims) - o[a];
                     }
+                    base = base * E + loc;
                 }
 #pragma unroll
                 for (int l = 0; l < S; l++)
 #pragma unroll
                     for (int m = 0; m < S; m++) {
                         const float c01 = __fmul_rn(C[0][l], C[1][m]);
-                        const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
+                        const int row = base + (l * E + m) * E;
 #pragma unroll
                         for (int q = 0; q < S; q++) {
                             const float v = __fmul_rn(c01, C[2][q]);
                             if (mode == 1) atomicAdd(facc + row + q, v);
-                            else if (v >= 0.0f && v < 255.0f) fx8_add(lo, hiw, row + q, v, &ovf);
-                            else ovf = 1;
+                            else fx8_add(lo, hiw, row + q, v, &ovf);
                         }
                     }
             }
@@ -835,19 +843,20 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
                 continue;
             }
             float *out = pass == 0 ? grid : grid2;
-            for (int c = threadIdx.x; c < CELLS; c += blockDim.x) {
-                float v;
-                if (mode == 0) {
-                    const unsigned hb = (hiw[c >> 2] >> (8 * (c & 3))) & 0xffu;
-                    v = __fadd_rn((float)hb, __uint2float_rn(lo[c]) * 2.3283064365386963e-10f);
-                } else {
-                    v = facc[c];
+            for (int rr = warp; rr < E * E; rr += nwarps) {    // rows (lx, ly), lanes along z
+                const int lx = rr / E, ly = rr - lx * E;
+                const long long grow = (add_wrap(o[0], lx, d) * d + add_wrap(o[1], ly, d)) * d;
+                for (int lz = lane; lz < E; lz += 32) {
+                    const int c = rr * E + lz;
+                    float v;
+                    if (mode == 0) {
+                        const unsigned hb = (hiw[c >> 2] >> (8 * (c & 3))) & 0xffu;
+                        v = __fadd_rn((float)hb, __uint2float_rn(lo[c]) * 2.3283064365386963e-10f);
+                    } else {
+                        v = facc[c];
+                    }
+                    if (v != 0.0f) atomicAdd(out + grow + add_wrap(o[2], lz, d), v);
                 }
-                if (v == 0.0f) continue;
-                const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
-                                gz = add_wrap(o[2], lz, d);
-                atomicAdd(out + (gx * d + gy) * d + gz, v);
             }
             __syncthreads();
             break;
