@@ -765,17 +765,17 @@ __device__ __forceinline__ void fx8_carry(unsigned *hiw, int c, unsigned inc, in
 // low word, the high byte only on a carry.
 __device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, float v, int *ovf)
 {
-    if (v < 1.0f) {
+    if (v >= 0.0f && v < 1.0f) {
         const unsigned ql = __float2uint_rn(v * 4294967296.0f);   // < 2^32 for v < 1
         const unsigned old = atomicAdd(lo + c, ql);
         if (old + ql < old) fx8_carry(hiw, c, 1u, ovf);
-    } else if (v < 255.0f) {
+    } else if (v >= 1.0f && v < 255.0f) {
         const float fi = floorf(v);
         const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
         const unsigned old = atomicAdd(lo + c, ql);
         fx8_carry(hiw, c, (unsigned)__float2int_rz(fi) + (old + ql < old ? 1u : 0u), ovf);
     } else {
-        *ovf = 1;                                   // includes NaN
+        *ovf = 1;                                   // negative (positions below 0), huge, or NaN
     }
 }
 

@@ -53,11 +53,13 @@ def test_ma_golden_3d(MASL, ma, mas, tag, strategy):
 @pytest.mark.parametrize('mas', MAS_LIST)
 @pytest.mark.parametrize('tag', ['', 'W'])
 def test_ma_golden_2d(MASL, ma, mas, tag):
+    """2D grids take S^3 adds per particle into dims^2 cells (about 330 float adds per
+    cell here), so two summation orders differ by tens of ulps: tolerance 1e-5."""
     pos, W = ma['grid_pos'], ma['grid_W']
     N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
     d2 = np.zeros((N, N), np.float32)
     MASL.MA(np.ascontiguousarray(pos[:, :2]), d2, L, mas, W if tag else None)
-    close(d2, ma['MA2D_%s%s' % (mas, tag)], exact=(mas == 'NGP' and not tag))
+    close(d2, ma['MA2D_%s%s' % (mas, tag)], exact=(mas == 'NGP' and not tag), tol=1e-5)
 
 
 @pytest.mark.parametrize('mas', MAS_LIST)
