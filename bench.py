@@ -272,52 +272,47 @@ def main():
         print(json.dumps(line))
 
 
-# our kernels per step: tile count, scan, scatter, deposit, 2 overdensity, bin
-KERNELS_PER_STEP = 7
+# our kernels per step: 2 fills, histogram, column scan, tile scan, level-A and level-B
+# placement, deposit, P(k) bin
+KERNELS_PER_STEP = 9
 
 
 def stage_times(pp, pos, reps):
+    """CUDA-event durations of each C-ABI call of one step, on the launching stream."""
     import torch
     from pylians_gb300 import _lib
     from pylians_gb300._device import ptr, stream_ptr
     d = pp.dims
     n = pos.shape[0]
-    cells = d ** 3
     st = stream_ptr()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-    acc = np.zeros(5)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    acc = np.zeros(3)
     for _ in range(reps):
         ev[0].record()
-        pp.grids.zero_()
+        _lib.call('pyl_ma_overdensity', ptr(pos), None, n, ptr(pp.grids[0]), ptr(pp.grids[1]), d,
+                  pp.BoxSize, _lib.MAS_INDEX[pp.MAS], _lib.STRATEGY[pp.strategy], ptr(pp.ws),
+                  pp.ws_bytes, st)
         ev[1].record()
-        _lib.call('pyl_ma', ptr(pos), None, n, 3, ptr(pp.grids[0]), ptr(pp.grids[1]), d, pp.BoxSize,
-                  _lib.MAS_INDEX[pp.MAS], _lib.STRATEGY[pp.strategy], 0, ptr(pp.ws), pp.ws_bytes, st)
-        ev[2].record()
-        for i in range(2):
-            _lib.call('pyl_overdensity', ptr(pp.grids[i]), cells, None, float(n) / cells, st)
-        ev[3].record()
         _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, 2, st)
-        ev[4].record()
+        ev[2].record()
         _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]), 1, pp.dk[0].numel(), d, pp.axis,
                   pp.mas_p, ptr(pp.sums), ptr(pp.pk_ws), pp.pk_ws_bytes, st)
-        ev[5].record()
+        ev[3].record()
         torch.cuda.synchronize()
-        acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]
+        acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
     acc /= reps
-    return dict(zero=acc[0], scatter=acc[1], overdensity=acc[2], fft_r2c=acc[3], pk_bin=acc[4])
+    return dict(density=acc[0], fft_r2c=acc[1], pk_bin=acc[2])
 
 
 def roofline(stages, n, dims, hbm, src):
-    """Algorithmic HBM bytes per launch of each stage (see DESIGN.md):
-    scatter: 12 B/particle read + 2 grids x 4 B/cell written;
-    overdensity: 2 grids x 8 B/cell; fft_r2c: 2 x (4 B/cell + 8 B/mode);
-    pk_bin: 2 fields x 8 B/mode."""
+    """Algorithmic HBM bytes per launch of each stage:
+    density (particles -> two overdensity grids): 12 B/particle read + 2 grids x 4 B/cell written;
+    fft_r2c: 2 x (4 B/cell read + 8 B/mode written); pk_bin: 2 fields x 8 B/mode read."""
     cells = dims ** 3
     modes = dims * dims * (dims // 2 + 1)
-    alg = dict(scatter=12.0 * n + 2 * 4.0 * cells, overdensity=2 * 8.0 * cells,
-               fft_r2c=2 * (4.0 * cells + 8.0 * modes), pk_bin=2 * 8.0 * modes,
-               zero=2 * 4.0 * cells)
-    top = max((k for k in alg if k != 'zero'), key=lambda k: stages[k])
+    alg = dict(density=12.0 * n + 2 * 4.0 * cells, fft_r2c=2 * (4.0 * cells + 8.0 * modes),
+               pk_bin=2 * 8.0 * modes)
+    top = max(alg, key=lambda k: stages[k])
     achieved = alg[top] / (stages[top] / 1e3) / 1e9
     return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
                 frac=achieved / hbm, traffic=None, peak_source=src,

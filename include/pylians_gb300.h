@@ -72,6 +72,16 @@ int pyl_ma(const float *pos, const float *weights, int64_t n_particles, int ndim
            int strategy, int renormalize_2d, void *workspace, size_t workspace_bytes,
            void *stream);
 
+/* Particles straight to the overdensity: grid (and grid_interlaced) are
+ * OVERWRITTEN with delta = n/mean - 1, where n is the deposit and mean =
+ * n_particles/dims^3, or sum(weights)/dims^3 (float64) with weights — the
+ * callers' convention in library/Pk_library/Pk_snapshot.py:70-88.  One pass:
+ * the grids are filled with -1 and every deposit is scaled by 1/mean.  3D only;
+ * workspace as for pyl_ma (pyl_ma_workspace_size). */
+int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n_particles, float *grid,
+                       float *grid_interlaced, int dims, float box_size, int mas, int strategy,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
 /* Allocation-free mass assignment.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory around the call (code running
  * during CUDA-graph capture, plugins inside a host framework that owns the

@@ -29,7 +29,7 @@ from ._device import as_device_f32, is_torch, ptr, require_cuda, stream_ptr, wor
 __all__ = ['MA', 'NGP', 'CIC', 'TSC', 'PCS', 'NGPW', 'CICW', 'TSCW', 'PCSW', 'FLOAT_type',
            'NGPc3D', 'CICc3D', 'TSCc3D', 'PCSc3D', 'NGPWc3D', 'CICWc3D', 'TSCWc3D', 'PCSWc3D',
            'NGPc2D', 'CICc2D', 'TSCc2D', 'PCSc2D', 'NGPWc2D', 'CICWc2D', 'TSCWc2D', 'PCSWc2D',
-           'ma_device']
+           'ma_device', 'overdensity_device']
 
 
 def FLOAT_type():
@@ -65,6 +65,25 @@ def ma_device(pos, grid, BoxSize, MAS, W=None, grid_interlaced=None, renormalize
     _lib.call('pyl_ma', ptr(pos), ptr(W), n, ndim, ptr(grid), ptr(grid_interlaced), dims,
               float(BoxSize), mas, strat, int(bool(renormalize_2D)), ptr(ws), nbytes,
               stream_ptr(stream))
+
+
+def overdensity_device(pos, grid, BoxSize, MAS='CIC', W=None, grid_interlaced=None, strategy='auto',
+                       stream=None):
+    """Particles straight to the overdensity (CUDA tensors): grid (and grid_interlaced) are
+    overwritten with delta = n/mean - 1, mean = N/dims^3 or sum(W)/dims^3, the convention of
+    library/Pk_library/Pk_snapshot.py:70-88, in one deposit pass."""
+    require_cuda()
+    if MAS not in _lib.MAS_INDEX:
+        raise ValueError('option not valid: MAS=%r' % (MAS,))
+    if pos.dim() != 2 or pos.shape[1] != 3 or grid.dim() != 3:
+        raise ValueError('pos must be (N,3) and the grid 3D')
+    dims, n = grid.shape[0], pos.shape[0]
+    mas, strat = _lib.MAS_INDEX[MAS], _lib.STRATEGY[strategy]
+    L = _lib.load()
+    nbytes = L.pyl_ma_workspace_size(n, 3, dims, mas, strat, int(grid_interlaced is not None))
+    ws = workspace.get(nbytes)
+    _lib.call('pyl_ma_overdensity', ptr(pos), ptr(W), n, ptr(grid), ptr(grid_interlaced), dims,
+              float(BoxSize), mas, strat, ptr(ws), nbytes, stream_ptr(stream))
 
 
 def MA(pos, number, BoxSize, MAS='CIC', W=None, verbose=False, renormalize_2D=True, *,

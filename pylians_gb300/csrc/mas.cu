@@ -37,6 +37,16 @@ namespace {
 template <int MAS>
 struct Support { static constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS; };
 
+// Factor applied to every deposited value: 1 for MA(), dims^3 / sum(mass) when
+// the deposit writes the overdensity directly (read from device memory when the
+// mass sum is computed on the device).
+struct OutScale {
+    float host;
+    const float *dev;
+};
+
+__device__ __forceinline__ float out_scale(const OutScale &s) { return s.dev ? *s.dev : s.host; }
+
 // First cell (unwrapped) of the support of one particle coordinate.  Cell
 // arithmetic is 32-bit (float->int64 conversions run on the slow fp64 pipe):
 // coordinates must satisfy |x * dims / BoxSize| < 2^31; beyond that the
@@ -122,9 +132,10 @@ __device__ __forceinline__ int axis_weights(float p, float inv, float *C)
 template <int MAS, int NDIM, bool WEIGHTED, bool INTERLACED>
 __global__ void __launch_bounds__(256) ma_atomic_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n,
-    float *__restrict__ grid, float *__restrict__ grid2, int dims, float inv, float halfcell)
+    float *__restrict__ grid, float *__restrict__ grid2, int dims, float inv, float halfcell, OutScale sc)
 {
     constexpr int S = Support<MAS>::S;
+    const float scale = out_scale(sc);
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long sa = NDIM == 3 ? (long long)dims * dims : dims;
     const long long sb = NDIM == 3 ? dims : 1;
@@ -156,7 +167,7 @@ __global__ void __launch_bounds__(256) ma_atomic_kernel(
                         for (int q = 0; q < S; q++) {
                             float v = __fmul_rn(c01, C[NDIM - 1][q]);
                             if (WEIGHTED) v = __fmul_rn(v, wi);
-                            atomicAdd(out + row + idx[NDIM - 1][q], v);
+                            atomicAdd(out + row + idx[NDIM - 1][q], __fmul_rn(v, scale));
                         }
                     }
             } else {
@@ -168,6 +179,7 @@ __global__ void __launch_bounds__(256) ma_atomic_kernel(
                     for (int m = 0; m < S; m++) {
                         float v = __fmul_rn(C[0][l], C[1][m]);
                         if (WEIGHTED) v = __fmul_rn(v, wi);
+                        v = __fmul_rn(v, scale);
                         float *cell = out + idx[0][l] * sa + idx[1][m];
                         for (int q = 0; q < S; q++) atomicAdd(cell, v);
                     }
@@ -609,9 +621,10 @@ __device__ __forceinline__ void particle_support(const float *p, float inv, floa
 template <int MAS, bool WEIGHTED, bool INTER, bool FIXED>
 __global__ void __launch_bounds__(1024) bin_deposit_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2)
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc)
 {
     using TS = TileShape<MAS, INTER, FIXED>;
+    const float scale = out_scale(sc);
     constexpr int S = Support<MAS>::S, E = TS::E, HX = TS::HX, CELLS = TS::CELLS;
     extern __shared__ unsigned smw[];
     const long long tile = blockIdx.x;
@@ -668,7 +681,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_kernel(
                     const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
                     const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
                                     gz = add_wrap(o[2], lz, d);
-                    atomicAdd(out + (gx * d + gy) * d + gz, v);
+                    atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
                 }
             }
             __syncthreads();
@@ -692,11 +705,11 @@ inline int grid_blocks(long long n, int threads, int per_sm = 8)
 
 template <int MAS, int NDIM>
 int launch_atomic(const float *pos, const float *w, long long n, float *grid, float *grid2,
-                  int dims, float inv, float halfcell, cudaStream_t st)
+                  int dims, float inv, float halfcell, OutScale sc, cudaStream_t st)
 {
     const int blocks = grid_blocks(n, 256, 16);
 #define PYL_ATOMIC(WW, II) \
-    ma_atomic_kernel<MAS, NDIM, WW, II><<<blocks, 256, 0, st>>>(pos, w, n, grid, grid2, dims, inv, halfcell)
+    ma_atomic_kernel<MAS, NDIM, WW, II><<<blocks, 256, 0, st>>>(pos, w, n, grid, grid2, dims, inv, halfcell, sc)
     if (w) { if (grid2) PYL_ATOMIC(true, true); else PYL_ATOMIC(true, false); }
     else   { if (grid2) PYL_ATOMIC(false, true); else PYL_ATOMIC(false, false); }
 #undef PYL_ATOMIC
@@ -782,9 +795,10 @@ __device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, floa
 template <int MAS, bool INTER>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2)
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc)
 {
     using FS = FxShape<MAS, INTER>;
+    const float scale = out_scale(sc);
     constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
     extern __shared__ __align__(16) unsigned smw[];
     __shared__ int ovf;
@@ -855,7 +869,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
                     } else {
                         v = facc[c];
                     }
-                    if (v != 0.0f) atomicAdd(out + grow + add_wrap(o[2], lz, d), v);
+                    if (v != 0.0f) atomicAdd(out + grow + add_wrap(o[2], lz, d), __fmul_rn(v, scale));
                 }
             }
             __syncthreads();
@@ -866,33 +880,33 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
 
 template <int MAS, bool I>
 int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                      float *grid2, cudaStream_t st)
+                      float *grid2, OutScale sc, cudaStream_t st)
 {
     using FS = FxShape<MAS, I>;
     auto kern = bin_deposit_fx_kernel<MAS, I>;
     static size_t done = 0;
     PYL_CUDA(ensure_smem(kern, FS::SMEM, &done));
-    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2);
+    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
 
 template <int MAS, bool W, bool I, bool FX>
 int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                   float *grid2, cudaStream_t st)
+                   float *grid2, OutScale sc, cudaStream_t st)
 {
     using TS = TileShape<MAS, I, FX>;
     auto kern = bin_deposit_kernel<MAS, W, I, FX>;
     static size_t done = 0;
     PYL_CUDA(ensure_smem(kern, TS::SMEM, &done));
-    kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2);
+    kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
 
 template <int MAS>
 int launch_tiled(const float *pos, const float *w, long long n, float *grid, float *grid2,
-                 int dims, float inv, float halfcell, void *workspace, cudaStream_t st)
+                 int dims, float inv, float halfcell, void *workspace, OutScale sc, cudaStream_t st)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws = tiled_layout(workspace, n, dims);
@@ -949,14 +963,14 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.rec);
         PYL_LAUNCH_CHECK();
     }
-    if (w) return grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, st)
-                        : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, st);
+    if (w) return grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                        : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
     if (grid2) {
-        if (FxShape<MAS, true>::FITS) return launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, st);
-        return launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, st);
+        if (FxShape<MAS, true>::FITS) return launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
+        return launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
     }
-    if (FxShape<MAS, false>::FITS) return launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, st);
-    return launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, st);
+    if (FxShape<MAS, false>::FITS) return launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    return launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
 }
 
 inline int pick_strategy(int strategy, int ndim, int dims, long long n)
@@ -980,9 +994,10 @@ extern "C" size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims,
     (void)mas; (void)interlaced;
     if (n_particles < 0 || dims <= 0) return 0;
     const int s = pick_strategy(strategy, ndim, dims, n_particles);
+    // + 256 bytes at the end: the mass sum and scale of pyl_ma_overdensity
     if (s == PYL_STRATEGY_TILED && ndim == 3)
-        return tiled_layout(nullptr, n_particles, dims).bytes;
-    return 0;
+        return tiled_layout(nullptr, n_particles, dims).bytes + 256;
+    return 256;
 }
 
 extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndim, float *grid,
@@ -1000,6 +1015,7 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
     cudaStream_t st = (cudaStream_t)stream;
     const float inv = (float)dims / box_size;                 // MAS_library.pyx:282
     const float halfcell = (float)(0.5 * (double)box_size / dims);
+    const OutScale sc{1.0f, nullptr};
     int s = pick_strategy(strategy, ndim, dims, n);
     if (s == PYL_STRATEGY_SORTED) s = PYL_STRATEGY_TILED;
     if (s == PYL_STRATEGY_TILED && (ndim != 3 || n > 0xFFFFFFF0ll)) s = PYL_STRATEGY_ATOMIC;
@@ -1016,11 +1032,11 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
     case M:                                                                                          \
         if (s == PYL_STRATEGY_TILED)                                                                 \
             rc = launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,        \
-                                 workspace, st);                                                     \
+                                 workspace, sc, st);                                                 \
         else if (ndim == 3)                                                                          \
-            rc = launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, st); \
+            rc = launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st); \
         else                                                                                         \
-            rc = launch_atomic<M, 2>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, st); \
+            rc = launch_atomic<M, 2>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st); \
         break;
         switch (mas) {
             PYL_DISPATCH(PYL_MAS_NGP)
@@ -1042,6 +1058,86 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
         }
     }
     return PYL_OK;
+}
+
+// ------------------------------------------------------------ overdensity
+namespace pyl {
+namespace {
+__global__ void __launch_bounds__(256) fill_kernel(float *g, long long n, float v)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long n4 = ((((uintptr_t)g) & 15) == 0) ? n / 4 : 0;
+    float4 *g4 = (float4 *)g;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
+        g4[i] = make_float4(v, v, v, v);
+    for (long long i = n4 * 4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        g[i] = v;
+}
+
+// scale = cells / sum(mass), float64 then rounded once
+__global__ void mass_scale_kernel(const double *sum, double cells, float *scale)
+{
+    *scale = (float)(cells / *sum);
+}
+}  // namespace
+}  // namespace pyl
+
+extern "C" int pyl_grid_sum(const float *grid, int64_t n, double *d_sum, void *stream);
+
+extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n, float *grid,
+                                  float *grid_interlaced, int dims, float box_size, int mas,
+                                  int strategy, void *workspace, size_t workspace_bytes, void *stream)
+{
+    PYL_CHECK_ARG(mas >= PYL_MAS_NGP && mas <= PYL_MAS_PCS, "MAS must be NGP, CIC, TSC or PCS");
+    PYL_CHECK_ARG(dims > 0 && dims <= 65536, "dims out of range");
+    PYL_CHECK_ARG(n > 0, "need at least one particle (the mean density is zero)");
+    PYL_CHECK_ARG(grid != nullptr && pos != nullptr, "null pointer");
+    PYL_CHECK_ARG(box_size > 0.0f && isfinite(box_size), "BoxSize must be positive and finite");
+    PYL_CHECK_ARG(strategy >= PYL_STRATEGY_AUTO && strategy <= PYL_STRATEGY_SORTED, "bad strategy");
+    const size_t need = pyl_ma_workspace_size(n, 3, dims, mas, strategy, grid_interlaced != nullptr);
+    if (workspace == nullptr || workspace_bytes < need) {
+        set_error("pyl_ma_overdensity: needs " + std::to_string(need) + " workspace bytes");
+        return PYL_ERR_WORKSPACE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long cells = (long long)dims * dims * dims;
+    char *tail = (char *)workspace + need - 256;
+    double *d_sum = (double *)tail;
+    float *d_scale = (float *)(tail + 64);
+    OutScale sc{(float)((double)cells / (double)n), nullptr};    // Pk_snapshot.py:85 (mean = N/dims^3)
+    if (weights) {                                                // Pk_snapshot.py:80 (mean = sum(M)/dims^3)
+        int rc = pyl_grid_sum(weights, n, d_sum, stream);
+        if (rc) return rc;
+        mass_scale_kernel<<<1, 1, 0, st>>>(d_sum, (double)cells, d_scale);
+        PYL_LAUNCH_CHECK();
+        sc = OutScale{0.0f, d_scale};
+    }
+    const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
+    fill_kernel<<<blocks, 256, 0, st>>>(grid, cells, -1.0f);
+    PYL_LAUNCH_CHECK();
+    if (grid_interlaced) {
+        fill_kernel<<<blocks, 256, 0, st>>>(grid_interlaced, cells, -1.0f);
+        PYL_LAUNCH_CHECK();
+    }
+    const float inv = (float)dims / box_size;
+    const float halfcell = (float)(0.5 * (double)box_size / dims);
+    int s = pick_strategy(strategy, 3, dims, n);
+    if (s == PYL_STRATEGY_SORTED) s = PYL_STRATEGY_TILED;
+    if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
+    switch (mas) {
+#define PYL_OD(M)                                                                                    \
+    case M:                                                                                          \
+        return s == PYL_STRATEGY_TILED                                                               \
+                   ? launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,   \
+                                     workspace, sc, st)                                              \
+                   : launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
+        PYL_OD(PYL_MAS_NGP)
+        PYL_OD(PYL_MAS_CIC)
+        PYL_OD(PYL_MAS_TSC)
+        PYL_OD(PYL_MAS_PCS)
+#undef PYL_OD
+    }
+    return PYL_ERR_INVALID;
 }
 
 // ------------------------------------------------------- allocation-free variant
@@ -1112,9 +1208,9 @@ extern "C" int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n,
     const float inv = (float)dims / box_size;
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     switch (mas) {
-        case PYL_MAS_NGP: return launch_tiled<PYL_MAS_NGP>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
-        case PYL_MAS_CIC: return launch_tiled<PYL_MAS_CIC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
-        case PYL_MAS_TSC: return launch_tiled<PYL_MAS_TSC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
-        default:          return launch_tiled<PYL_MAS_PCS>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, st);
+        case PYL_MAS_NGP: return launch_tiled<PYL_MAS_NGP>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
+        case PYL_MAS_CIC: return launch_tiled<PYL_MAS_CIC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
+        case PYL_MAS_TSC: return launch_tiled<PYL_MAS_TSC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
+        default:          return launch_tiled<PYL_MAS_PCS>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
     }
 }

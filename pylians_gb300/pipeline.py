@@ -7,7 +7,9 @@ This is the caller-side chain the reference's drivers run around MA and Pk
     Pk(delta, BoxSize, axis, MAS)
 
 with mean = N_particles / dims^3 (or sum(W) / dims^3 with weights), plus the
-interlaced second grid when `interlaced=True`.  Every launch goes to one CUDA
+interlaced second grid when `interlaced=True`.  The deposit writes the
+overdensity directly (pyl_ma_overdensity: grids filled with -1, deposits
+scaled by 1/mean), so there is no separate normalisation pass.  Every launch goes to one CUDA
 stream, so a whole step can be captured in a CUDA graph (`capture()`), and the
 grids, FFT outputs and sums stay allocated across steps.
 """
@@ -50,34 +52,21 @@ class ParticlePk(object):
         L = _lib.load()
         need = L.pyl_ma_workspace_size(int(n), 3, self.dims, _lib.MAS_INDEX[self.MAS],
                                        _lib.STRATEGY[self.strategy], int(self.interlaced))
-        if weighted:
-            need += 4 * int(n) + 256
         if need > self.ws_bytes:
             self.ws = torch.empty(need, dtype=torch.uint8, device=self.device)
             self.ws_bytes = need
 
     def step(self, pos, W=None, stream=None):
-        """Enqueue one pass: zero grids, deposit, normalise, FFT, bin -> self.sums."""
+        """Enqueue one pass: overdensity deposit (grids overwritten), FFT, bin -> self.sums."""
         n = pos.shape[0]
         d = self.dims
-        cells = d ** 3
         st = stream_ptr(stream)
         self.reserve(n, W is not None)
-        self.grids.zero_()
         g2 = self.grids[1] if self.interlaced else None
-        _lib.call('pyl_ma', ptr(pos), ptr(W), n, 3, ptr(self.grids[0]), ptr(g2), d,
-                  self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy], 0,
+        _lib.call('pyl_ma_overdensity', ptr(pos), ptr(W), n, ptr(self.grids[0]), ptr(g2), d,
+                  self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy],
                   ptr(self.ws), self.ws_bytes, st)
         ng = self.grids.shape[0]
-        if W is None:
-            mean = float(n) / cells
-            for i in range(ng):
-                _lib.call('pyl_overdensity', ptr(self.grids[i]), cells, None, mean, st)
-        else:
-            # mean = sum(W) / dims^3 in float64 (Pk_snapshot.py:80)
-            _lib.call('pyl_grid_sum', ptr(W), n, ptr(self.wsum), st)
-            for i in range(ng):
-                _lib.call('pyl_overdensity', ptr(self.grids[i]), cells, ptr(self.wsum), 0.0, st)
         _lib.call('pyl_fft_r2c', ptr(self.grids), ptr(self.dk), d, ng, st)
         dk2 = self.dk[1] if self.interlaced else None
         _lib.call('pyl_pk_bin', ptr(self.dk[0]), ptr(dk2), 1, self.dk[0].numel(), d, self.axis,

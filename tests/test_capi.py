@@ -47,7 +47,7 @@ def test_sizes_are_host_side(lib):
     assert lib.pyl_pk_sums_len(128, 1) == 111 * 4 + 65 + 65 * 91
     assert lib.pyl_pk_sums_len(128, 2) == 111 * (3 * 3 + 2) + 65 * 3 + 65 * 91 * 3
     assert lib.pyl_pk_geometry_len(128) == 2 * 65 + 65 * 91 + 2 * 111
-    assert lib.pyl_ma_workspace_size(1000, 3, 64, 2, 1, 0) == 0          # atomic: no workspace
+    assert lib.pyl_ma_workspace_size(1000, 3, 64, 2, 1, 0) == 256        # atomic: the mass-sum tail only
     assert lib.pyl_ma_workspace_size(10 ** 6, 3, 512, 2, 2, 1) >= 12 * 10 ** 6
 
 

@@ -176,3 +176,23 @@ def test_pipeline_matches_stepwise(PKL):
     r2 = pp.result()
     np.testing.assert_array_equal(r2.Nmodes3D, r.Nmodes3D)
     np.testing.assert_allclose(r2.Pk, r.Pk, rtol=1e-6, atol=1e-6 * np.abs(r.Pk[:, 0]).max())
+
+
+@pytest.mark.parametrize('weighted', [False, True])
+def test_overdensity_deposit_matches_two_pass(weighted):
+    """pyl_ma_overdensity (fill -1, deposits scaled by 1/mean) equals MA followed by
+    delta = n/mean - 1 (Pk_snapshot.py:70-88) within a few float32 ulps of delta."""
+    import pylians_gb300.MAS_library as MASL
+    rng = np.random.default_rng(21)
+    N, L, n = 96, 1000.0, 1_500_000
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    W = torch.from_numpy((rng.random(n) * 3).astype(np.float32)).cuda() if weighted else None
+    for strategy in ('atomic', 'tiled'):
+        d1 = torch.empty((N, N, N), device='cuda'); d2 = torch.empty((N, N, N), device='cuda')
+        MASL.overdensity_device(pos, d1, L, 'CIC', W, grid_interlaced=d2, strategy=strategy)
+        g1 = torch.zeros((N, N, N), device='cuda'); g2 = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(pos, g1, L, 'CIC', W, interlaced=g2, strategy=strategy)
+        mean = (W.double().sum().item() if weighted else float(n)) / N ** 3
+        for d, g in ((d1, g1), (d2, g2)):
+            ref = g.double() / mean - 1.0
+            assert (d.double() - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
