@@ -98,6 +98,39 @@ int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n_particl
 int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n_particles, float *grid,
                    float *grid_interlaced, int dims, float box_size, int mas, void *stream);
 
+/* ---- batched realizations --------------------------------------------------------
+ * Many particle sets with uneven sizes, grids, MAS and interlacing in ONE
+ * persistent launch (no counterpart in the reference, whose drivers loop over
+ * MA() calls, e.g. library/MAS_library/MAS_gadget.py:35-76).  `reals` and
+ * `items` live in device memory; each item deposits particles
+ * [first, first+count) of realization `real`.  Grids must be pre-filled with -1
+ * (pyl_fill); with scale = dims^3 / n_particles they end as the overdensity.
+ * `counter` is one device unsigned (the work-queue head, zeroed by the call);
+ * the grid size is num_SMs * ctas_per_sm CTAs of 256 threads. */
+typedef struct pyl_batch_real {
+    const float *pos;          /* float32 [n][3] */
+    float *grid;               /* float32 [dims]^3 */
+    float *grid_interlaced;    /* NULL or float32 [dims]^3 (positions + half a cell) */
+    float inv;                 /* (float)dims / BoxSize */
+    float halfcell;            /* (float)(0.5 * BoxSize / dims) */
+    float scale;               /* factor on every deposit */
+    int dims;
+    int mas;                   /* PYL_MAS_NGP..PYL_MAS_PCS */
+    int reserved;
+} pyl_batch_real;
+
+typedef struct pyl_batch_item {
+    int64_t first;             /* first particle (index into the realization's pos) */
+    uint32_t count;            /* particles in this item */
+    uint32_t real;             /* index into reals */
+} pyl_batch_item;
+
+int pyl_ma_batch(const pyl_batch_real *reals, int n_reals, const pyl_batch_item *items, int n_items,
+                 unsigned *counter, int ctas_per_sm, void *stream);
+
+/* float32 fill of n values (grids to -1 before an overdensity deposit). */
+int pyl_fill(float *p, int64_t n, float value, void *stream);
+
 /* ---- overdensity --------------------------------------------------------------
  * Replaces the callers' normalisation `delta /= mean; delta -= 1.0`
  * (library/Pk_library/Pk_snapshot.py:80-88, documentation/Documentation.md:93).
