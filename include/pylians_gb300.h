@@ -216,6 +216,24 @@ int pyl_bk_triangles(const float *d_fields, const float *i_fields, int dims, int
                      int n_shells, const int *host_tri, int n_tri, double *num, double *den,
                      void *stream);
 
+/* ---- learned aliasing correction (no counterpart in the reference) ----------------
+ * MLP 4 -> 64 -> 64 -> 64 -> 1 with tanh hidden layers, BF16 weights and FP32
+ * accumulation.  Parameters (pyl_mlp_param_count() of them, row-major [out][in]):
+ *   W1[64][4] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[1][64] b4[1].
+ * x: float32 [batch][4]; act: float32 [batch][192] hidden activations (forward
+ * writes them when non-NULL; backward reads them); y: float32 [batch].
+ * pyl_mlp_backward: gradient of sum_s w_s (y_s - t_s)^2 / weight_sum into grad
+ * [param_count] (weights NULL = all 1); delta [batch][192] and dy [batch] are
+ * scratch.  pyl_mlp_adam: Adam step on FP32 master weights, re-rounding the
+ * BF16 copy (step counts from 1). */
+int pyl_mlp_param_count(void);
+int pyl_mlp_forward(const void *params_bf16, const float *x, int batch, float *act, float *y, void *stream);
+int pyl_mlp_backward(const void *params_bf16, const float *x, const float *act, const float *y,
+                     const float *target, const float *weights, float weight_sum, int batch, float *delta,
+                     float *dy, float *grad, void *stream);
+int pyl_mlp_adam(float *master, void *params_bf16, const float *grad, float *m, float *v, int n, float lr,
+                 float beta1, float beta2, float eps, int step, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -313,3 +313,49 @@ def Bk(delta, BoxSize, k1, k2, theta, MAS='CIC', threads=1):
 
 if __name__ == '__main__':
     print(build(force='--force' in sys.argv))
+
+
+# ----------------------------------------------------- MLP (learned correction)
+# float64 restatement of the 4 -> 64 -> 64 -> 64 -> 1 tanh network of the
+# learned aliasing correction (no counterpart in the reference): the checker of
+# the GPU forward/backward kernels' gradients.
+MLP_SHAPES = [('W1', (64, 4)), ('b1', (64,)), ('W2', (64, 64)), ('b2', (64,)),
+              ('W3', (64, 64)), ('b3', (64,)), ('W4', (1, 64)), ('b4', (1,))]
+
+
+def mlp_unpack(flat):
+    out, o = {}, 0
+    for name, shp in MLP_SHAPES:
+        n = int(np.prod(shp))
+        out[name] = np.asarray(flat[o:o + n], dtype=np.float64).reshape(shp)
+        o += n
+    return out
+
+
+def mlp_forward_backward(flat, x, t, w=None):
+    """Loss sum_s w_s (y_s - t_s)^2 / sum_s w_s, its gradient (flat, float64) and y."""
+    p = mlp_unpack(flat)
+    x = np.asarray(x, np.float64)
+    t = np.asarray(t, np.float64)
+    w = np.ones_like(t) if w is None else np.asarray(w, np.float64)
+    h1 = np.tanh(x @ p['W1'].T + p['b1'])
+    h2 = np.tanh(h1 @ p['W2'].T + p['b2'])
+    h3 = np.tanh(h2 @ p['W3'].T + p['b3'])
+    y = (h3 @ p['W4'].T + p['b4'])[:, 0]
+    ws = w.sum()
+    loss = np.sum(w * (y - t) ** 2) / ws
+    dy = 2.0 * w * (y - t) / ws
+    g = {}
+    g['W4'] = dy[None, :] @ h3
+    g['b4'] = np.array([dy.sum()])
+    d3 = (dy[:, None] * p['W4']) * (1 - h3 ** 2)
+    g['W3'] = d3.T @ h2
+    g['b3'] = d3.sum(0)
+    d2 = (d3 @ p['W3']) * (1 - h2 ** 2)
+    g['W2'] = d2.T @ h1
+    g['b2'] = d2.sum(0)
+    d1 = (d2 @ p['W2']) * (1 - h1 ** 2)
+    g['W1'] = d1.T @ x
+    g['b1'] = d1.sum(0)
+    grad = np.concatenate([g[name].ravel() for name, _ in MLP_SHAPES])
+    return loss, grad, y

@@ -45,6 +45,10 @@ SIGNATURES = {
     'pyl_mas_deconvolve': (_I, [_P, _P, _I, _I, _P]),
     'pyl_bk_shell_fill': (_I, [_P, _I, _P, _P, _I, _P, _P, _P, _P]),
     'pyl_bk_triangles': (_I, [_P, _P, _I, _I64, _I, _P, _I, _P, _P, _P]),
+    'pyl_mlp_param_count': (_I, []),
+    'pyl_mlp_forward': (_I, [_P, _P, _I, _P, _P, _P]),
+    'pyl_mlp_backward': (_I, [_P, _P, _P, _P, _P, _P, _F, _I, _P, _P, _P, _P]),
+    'pyl_mlp_adam': (_I, [_P, _P, _P, _P, _P, _I, _F, _F, _F, _F, _I, _P]),
 }
 
 _lib = None
