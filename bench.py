@@ -40,7 +40,10 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--grid', type=int, default=1024)
     ap.add_argument('--particles-side', type=int, default=1024)
-    ap.add_argument('--cpu-side', type=int, default=256, help='side of the CPU baseline sample')
+    ap.add_argument('--cpu-side', type=int, default=512, help='side of the CPU baseline sample')
+    ap.add_argument('--ref-side', type=int, default=256, help='side of each reference-arm step')
+    ap.add_argument('--no-secondary', action='store_true')
+    ap.add_argument('--batch-size', type=int, default=512)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--strategy', default='auto', choices=['auto', 'atomic', 'tiled', 'sorted'])
@@ -100,7 +103,7 @@ def reference_arm(a):
     import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    side = a.cpu_side
+    side = a.ref_side
     pos = cpu_sample(side)
     for _ in range(a.warmup):
         cpu_chain(pos, side, threads)
@@ -226,29 +229,67 @@ def main():
     # ---- per-stage durations (events between C-ABI calls on the launching stream)
     stages = stage_times(pp, pos, reps=max(2, min(a.steps, 5)))
 
-    # ---- end to end: pinned host positions -> device -> chain -> sums to host
+    # ---- end to end: pinned host positions -> device -> chain -> sums to host.
+    # Two device position buffers: the copy of step i+1 runs on a copy stream
+    # while step i computes; every step still moves its 12.9 GB and its sums.
     e2e = None
     if not a.no_e2e:
         host = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
         host.copy_(pos)
+        del pos
+        torch.cuda.empty_cache()
         sums_host = torch.empty(pp.sums.shape, dtype=torch.float64, pin_memory=True)
-        dpos = torch.empty_like(pos)
-        for _ in range(1):
-            dpos.copy_(host, non_blocking=True); pp.step(dpos); sums_host.copy_(pp.sums, non_blocking=True)
+        bufs = [torch.empty((n, 3), dtype=torch.float32, device=dev) for _ in range(2)]
+        comp = torch.cuda.current_stream()
+        cps = torch.cuda.Stream()
+        copied = [torch.cuda.Event() for _ in range(2)]
+        free = [torch.cuda.Event() for _ in range(2)]
+
+        def run(k2):
+            with torch.cuda.stream(cps):
+                bufs[0].copy_(host, non_blocking=True)
+                copied[0].record(cps)
+            for i in range(k2):
+                b = i % 2
+                comp.wait_event(copied[b])
+                pp.step(bufs[b])
+                free[b].record(comp)
+                sums_host.copy_(pp.sums, non_blocking=True)
+                if i + 1 < k2:
+                    nb = (i + 1) % 2
+                    with torch.cuda.stream(cps):
+                        if i >= 1:
+                            cps.wait_event(free[nb])
+                        bufs[nb].copy_(host, non_blocking=True)
+                        copied[nb].record(cps)
+        run(2)
         torch.cuda.synchronize(); barrier()
         k2 = a.steps
+        t0 = time.perf_counter()
         e0.record()
-        for _ in range(k2):
-            dpos.copy_(host, non_blocking=True)
-            pp.step(dpos)
-            sums_host.copy_(pp.sums, non_blocking=True)
+        run(k2)
         e1.record()
         torch.cuda.synchronize(); barrier()
         ms2 = e0.elapsed_time(e1)
+        wall = (time.perf_counter() - t0) * 1e3
         e2e = dict(value=n * k2 * world / (ms2 / 1e3), unit=UNIT,
                    h2d_bytes_per_step=int(host.numel() * 4),
-                   d2h_bytes_per_step=int(sums_host.numel() * 8), ms_per_step=ms2 / k2)
-        del host, dpos
+                   d2h_bytes_per_step=int(sums_host.numel() * 8), ms_per_step=ms2 / k2,
+                   host_wall_ms_per_step=wall / k2, overlap='h2d of step i+1 under compute of step i')
+        del host, bufs
+        torch.cuda.empty_cache()
+
+    del pp
+    torch.cuda.empty_cache()
+    secondary = {}
+    if rank == 0 and not a.no_secondary:
+        for name, fn in (('bispectrum', bench_bispectrum), ('batch', lambda: bench_batch(a.batch_size)),
+                         ('learned', bench_learned)):
+            try:
+                secondary[name] = fn()
+            except Exception as exc:     # a failed side measurement must not hide the headline line
+                secondary[name] = dict(error='%s: %s' % (type(exc).__name__, exc))
+            torch.cuda.empty_cache()
 
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
@@ -268,13 +309,87 @@ def main():
                                 interlaced=True, strategy=a.strategy, parallelism='replicas',
                                 l2_flush='inputs larger than L2 (12.9 GB positions)'),
                     e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
-                    gpu_launches=KERNELS_PER_STEP * a.steps, stages_ms=stages)
+                    gpu_launches=KERNELS_PER_STEP * a.steps, stages_ms=stages,
+                    secondary=secondary)
         print(json.dumps(line))
 
 
 # our kernels per step: 2 fills, histogram, column scan, tile scan, level-A and level-B
 # placement, deposit, P(k) bin
 KERNELS_PER_STEP = 9
+
+
+def bench_bispectrum(reps=3):
+    """Bispectra of a 256^3 CIC overdensity (1000 Mpc/h, 256^3 uniform particles): k1=0.1,
+    k2=0.2 h/Mpc with 32 theta bins, plus 20 equilateral triangles k=0.02..0.4 h/Mpc, all 52
+    triangles in one shell fill, one batched C2R and one reduction."""
+    import torch
+    import pylians_gb300.MAS_library as MASL
+    import pylians_gb300.Pk_library as PKL
+    N = 256
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(3)
+    pos = torch.rand((N ** 3, 3), generator=gen, device='cuda') * BOX
+    d = torch.empty((N, N, N), device='cuda')
+    MASL.overdensity_device(pos, d, BOX, 'CIC')
+    theta = np.linspace(0, np.pi, 32)
+    k3 = np.sqrt((0.2 * np.sin(theta)) ** 2 + (0.2 * np.cos(theta) + 0.1) ** 2)
+    tris = [(0.1, 0.2, float(x)) for x in k3] + [(float(k), float(k), float(k)) for k in np.linspace(0.02, 0.4, 20)]
+    PKL.Bk_triangles(d, BOX, tris, 'CIC')
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        PKL.Bk_triangles(d, BOX, tris, 'CIC')
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    return dict(metric='bispectra/s', value=len(tris) / t, triangles=len(tris), ms_per_call=t * 1e3,
+                workload='Bk 256^3 CIC, 32-theta sweep + 20 equilateral', timing='host wall incl. sync')
+
+
+def bench_batch(count, steps=3):
+    """Batched realizations: `count` uniform-particle sets with grids from {64,128,192,256}^3,
+    1e5..1.7e7 particles (log-uniform), MAS from {CIC,TSC,PCS}, interlacing on/off (seed 0);
+    one CUDA-graph replay per batch."""
+    import torch
+    from pylians_gb300 import batch
+    specs = batch.random_specs(count, seed=0)
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(5)
+    pos = [torch.rand((s['n'], 3), generator=gen, device='cuda') * BOX for s in specs]
+    B = batch.RealizationBatch(specs, BOX, axis=0)
+    B.capture(pos)
+    B.replay()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        B.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    npart = sum(s['n'] for s in specs)
+    out = dict(metric='realizations/s', value=count / (ms / 1e3), particles_per_s=npart / (ms / 1e3),
+               ms_per_batch=ms, realizations=count, particles=npart, ctas_per_sm=B.ctas_per_sm)
+    del B, pos
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_learned():
+    """Learned-corrected 512^3 non-interlaced CIC P(k) against the plain interlaced 1024^3
+    estimate of the same 1024^3 (expected) Poisson particles of a P ~ k^-1.5 field in a
+    1000 Mpc/h box: wall-clock of both paths and the largest deviation up to 0.8 k_Nyq."""
+    from pylians_gb300 import learned
+    r = learned.evaluate(N=512, side=1024, slope=-1.5, L=BOX)
+    keep = ('particles', 'N_coarse', 'N_fine', 'k_max', 'bins', 'max_err_learned', 'mean_err_learned',
+            'max_err_plain', 'mean_err_plain', 'ms_coarse_learned', 'ms_fine_interlaced', 'speedup',
+            'slope_est', 'shot_level_est')
+    out = {k: r[k] for k in keep}
+    out['metric'] = 'learned 512^3 vs interlaced 1024^3 P(k) wall-clock ratio'
+    return out
 
 
 def stage_times(pp, pos, reps):

@@ -30,6 +30,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "sorted.cuh"
 
 namespace pyl {
 namespace {
@@ -751,45 +752,107 @@ TiledWs tiled_layout(void *base, long long n, int dims)
 }
 
 // ---- full-bin fixed-point deposit (unweighted) ------------------------------
-// Shared memory per cell: a 32-bit low word (fraction, 2^-32 units) and an 8-bit
-// high byte (integer part) packed four to a word, 5 bytes per cell, so a whole
-// TB^3 bin plus halo fits one CTA.  The grids (plain, then interlaced) are
-// deposited one after the other; the second pass reads the bin's particles from
-// L2.  A contribution outside [0, 255) or a high byte that would pass 255 sets
-// a flag and the pass is redone with float32 shared atomics.
+// One 32-bit word per shared-memory cell, so a whole TB^3 bin plus its + side
+// halo fits one CTA for every MAS with and without interlacing.  CIC/TSC/PCS
+// accumulate 10.22 fixed point (2^-22 units, cell sums below 1024); each
+// contribution v in [0, 1] is converted by one FFMA against 1.5 * 2^23 (exact
+// round-to-nearest of v * 2^22, error <= 2^-23) and one integer add.  NGP
+// accumulates integer counts.  Integer sums do not depend on the order of the
+// adds, so the bin values are reproducible.  A negative or NaN weight (CIC
+// positions below 0, non-finite positions) or a cell sum that wraps sets a
+// flag, and the pass is redone with float32 shared atomics.  The grids (plain,
+// then interlaced) are deposited one after the other; the second pass reads the
+// bin's particles again from L2.
 template <int MAS, bool INTER>
 struct FxShape {
     static constexpr int H = Support<MAS>::S - 1 + (INTER ? 1 : 0);
     static constexpr int E = TB + H;
     static constexpr int CELLS = E * E * E;
-    static constexpr int HIW = (CELLS + 3) / 4;
-    static constexpr size_t SMEM = sizeof(unsigned) * (CELLS + HIW);
+    static constexpr size_t SMEM = sizeof(unsigned) * ((CELLS + 3) / 4 * 4);
     static constexpr bool FITS = SMEM <= 227 * 1024;
 };
 
-__device__ __forceinline__ void fx8_carry(unsigned *hiw, int c, unsigned inc, int *ovf)
+constexpr float FX_MAGIC = 12582912.0f;        // 1.5 * 2^23
+constexpr unsigned FX_MAGIC_BITS = 0x4B400000u;
+constexpr float FX_SCALE = 4194304.0f;         // 2^22
+constexpr float FX_INV = 2.384185791015625e-07f;
+
+// Weights and bin-local first cell (base, row-major over E^3) of one particle
+// for the plain (G=0) or the half-cell-shifted (G=1) grid.
+template <int MAS, int G, int E>
+__device__ __forceinline__ int fx_support(const float4 &r, float inv, float halfcell, int dims, const int *o,
+                                          float (*C)[Support<MAS>::S])
 {
-    const int sh = 8 * (c & 3);
-    const unsigned old = atomicAdd(hiw + (c >> 2), inc << sh);
-    if (((old >> sh) & 0xffu) + inc > 255u) *ovf = 1;
+    const float p[3] = {r.x, r.y, r.z};
+    int base = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int loc;
+        if (G == 1) {
+            const int f0 = axis_first<MAS>(p[a], inv);
+            const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
+            loc = wrap_index(f0, dims) - o[a] + (f > f0 ? 1 : 0);
+        } else {
+            loc = wrap_index(axis_weights<MAS>(p[a], inv, C[a]), dims) - o[a];
+        }
+        base = base * E + loc;
+    }
+    return base;
 }
 
-// Adds v (0 <= v < 255) to cell c.  Hot path v < 1: one returning atomic on the
-// low word, the high byte only on a carry.
-__device__ __forceinline__ void fx8_add(unsigned *lo, unsigned *hiw, int c, float v, int *ovf)
+// All weights non-negative and not NaN (CIC: u >= 0; TSC/PCS weights are >= 0
+// for finite positions by construction).
+template <int MAS>
+__device__ __forceinline__ bool fx_weights_ok(const float (*C)[Support<MAS>::S])
 {
-    if (v >= 0.0f && v < 1.0f) {
-        const unsigned ql = __float2uint_rn(v * 4294967296.0f);   // < 2^32 for v < 1
-        const unsigned old = atomicAdd(lo + c, ql);
-        if (old + ql < old) fx8_carry(hiw, c, 1u, ovf);
-    } else if (v >= 1.0f && v < 255.0f) {
-        const float fi = floorf(v);
-        const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
-        const unsigned old = atomicAdd(lo + c, ql);
-        fx8_carry(hiw, c, (unsigned)__float2int_rz(fi) + (old + ql < old ? 1u : 0u), ovf);
-    } else {
-        *ovf = 1;                                   // negative (positions below 0), huge, or NaN
+    if (MAS == PYL_MAS_NGP) return true;
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < Support<MAS>::S; j++) ok = ok && C[a][j] >= 0.0f;
+    return ok;
+}
+
+template <int MAS, int E>
+__device__ __forceinline__ unsigned fx_scatter(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
+{
+    constexpr int S = Support<MAS>::S;
+    if (MAS == PYL_MAS_NGP) {
+        atomicAdd(acc + base, 1u);       // a bin holds < 2^32 particles: no wrap
+        return 0u;
     }
+    unsigned wrapped = 0u;
+#pragma unroll
+    for (int l = 0; l < S; l++)
+#pragma unroll
+        for (int m = 0; m < S; m++) {
+            const float c01 = __fmul_rn(C[0][l], C[1][m]);
+            const int row = base + (l * E + m) * E;
+#pragma unroll
+            for (int q = 0; q < S; q++) {
+                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
+                const unsigned qv = __float_as_uint(x) - FX_MAGIC_BITS;
+                const unsigned old = atomicAdd(acc + row + q, qv);
+                wrapped |= (unsigned)(old + qv < old);
+            }
+        }
+    return wrapped;
+}
+
+template <int MAS, int E>
+__device__ __forceinline__ void float_scatter(float *acc, int base, const float (*C)[Support<MAS>::S])
+{
+    constexpr int S = Support<MAS>::S;
+#pragma unroll
+    for (int l = 0; l < S; l++)
+#pragma unroll
+        for (int m = 0; m < S; m++) {
+            const float c01 = __fmul_rn(C[0][l], C[1][m]);
+            const int row = base + (l * E + m) * E;
+#pragma unroll
+            for (int q = 0; q < S; q++) atomicAdd(acc + row + q, __fmul_rn(c01, C[2][q]));
+        }
 }
 
 template <int MAS, bool INTER>
@@ -801,8 +864,6 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     const float scale = out_scale(sc);
     constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
     extern __shared__ __align__(16) unsigned smw[];
-    __shared__ int ovf;
-    unsigned *lo = smw, *hiw = smw + CELLS;
     float *facc = (float *)smw;
     const long long tile = blockIdx.x;
     const unsigned begin = offsets[tile], end = offsets[tile + 1];
@@ -811,66 +872,58 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     tile_coords(tile, g, tx, ty, tz);
     const int o[3] = {tx * TB, ty * TB, tz * TB};
     const long long d = g.dims;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const unsigned T = blockDim.x;
     for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
         for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
-            const int words = mode == 0 ? CELLS + FS::HIW : CELLS;
             uint4 *z4 = (uint4 *)smw;
-            for (int c = threadIdx.x; c < words / 4; c += blockDim.x) z4[c] = make_uint4(0u, 0u, 0u, 0u);
-            for (int c = (words / 4) * 4 + threadIdx.x; c < words; c += blockDim.x) smw[c] = 0u;
-            if (threadIdx.x == 0) ovf = 0;
+            for (int c = threadIdx.x; c < FS::SMEM / 16; c += T) z4[c] = make_uint4(0u, 0u, 0u, 0u);
             __syncthreads();
-            for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
-                const float4 r = rec[i];
-                const float p[3] = {r.x, r.y, r.z};
-                float C[3][S];
-                int base = 0;
-#pragma unroll
-                for (int a = 0; a < 3; a++) {
-                    int loc;
-                    if (pass == 1) {
-                        const int f0 = axis_first<MAS>(p[a], inv);
-                        const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
-                        loc = wrap_index(f0, g.dims) - o[a] + (f > f0 ? 1 : 0);
-                    } else {
-                        loc = wrap_index(axis_weights<MAS>(p[a], inv, C[a]), g.dims) - o[a];
-                    }
-                    base = base * E + loc;
+            unsigned bad = 0u;
+            unsigned long long i = begin + threadIdx.x;
+            // two particles in flight per thread
+            for (; i + T < end; i += 2ull * T) {
+                const float4 r0 = rec[i], r1 = rec[i + T];
+                float C0[3][S], C1[3][S];
+                const int b0 = pass ? fx_support<MAS, 1, E>(r0, inv, halfcell, g.dims, o, C0)
+                                    : fx_support<MAS, 0, E>(r0, inv, halfcell, g.dims, o, C0);
+                const int b1 = pass ? fx_support<MAS, 1, E>(r1, inv, halfcell, g.dims, o, C1)
+                                    : fx_support<MAS, 0, E>(r1, inv, halfcell, g.dims, o, C1);
+                if (mode == 0) {
+                    bad |= (unsigned)!(fx_weights_ok<MAS>(C0) && fx_weights_ok<MAS>(C1));
+                    bad |= fx_scatter<MAS, E>(smw, b0, C0);
+                    bad |= fx_scatter<MAS, E>(smw, b1, C1);
+                } else {
+                    float_scatter<MAS, E>(facc, b0, C0);
+                    float_scatter<MAS, E>(facc, b1, C1);
                 }
-#pragma unroll
-                for (int l = 0; l < S; l++)
-#pragma unroll
-                    for (int m = 0; m < S; m++) {
-                        const float c01 = __fmul_rn(C[0][l], C[1][m]);
-                        const int row = base + (l * E + m) * E;
-#pragma unroll
-                        for (int q = 0; q < S; q++) {
-                            const float v = __fmul_rn(c01, C[2][q]);
-                            if (mode == 1) atomicAdd(facc + row + q, v);
-                            else fx8_add(lo, hiw, row + q, v, &ovf);
-                        }
-                    }
             }
-            __syncthreads();
-            if (mode == 0 && ovf) {            // redo this pass in float32
+            if (i < end) {
+                const float4 r0 = rec[i];
+                float C0[3][S];
+                const int b0 = pass ? fx_support<MAS, 1, E>(r0, inv, halfcell, g.dims, o, C0)
+                                    : fx_support<MAS, 0, E>(r0, inv, halfcell, g.dims, o, C0);
+                if (mode == 0) {
+                    bad |= (unsigned)!fx_weights_ok<MAS>(C0);
+                    bad |= fx_scatter<MAS, E>(smw, b0, C0);
+                } else {
+                    float_scatter<MAS, E>(facc, b0, C0);
+                }
+            }
+            if (__syncthreads_or((int)bad) && mode == 0) {   // redo this pass in float32
                 __syncthreads();
                 continue;
             }
             float *out = pass == 0 ? grid : grid2;
-            for (int rr = warp; rr < E * E; rr += nwarps) {    // rows (lx, ly), lanes along z
-                const int lx = rr / E, ly = rr - lx * E;
-                const long long grow = (add_wrap(o[0], lx, d) * d + add_wrap(o[1], ly, d)) * d;
-                for (int lz = lane; lz < E; lz += 32) {
-                    const int c = rr * E + lz;
-                    float v;
-                    if (mode == 0) {
-                        const unsigned hb = (hiw[c >> 2] >> (8 * (c & 3))) & 0xffu;
-                        v = __fadd_rn((float)hb, __uint2float_rn(lo[c]) * 2.3283064365386963e-10f);
-                    } else {
-                        v = facc[c];
-                    }
-                    if (v != 0.0f) atomicAdd(out + grow + add_wrap(o[2], lz, d), __fmul_rn(v, scale));
-                }
+            for (int c = threadIdx.x; c < CELLS; c += T) {
+                const unsigned w = smw[c];
+                if (w == 0u) continue;
+                const float v = mode == 1 ? __uint_as_float(w)
+                                          : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
+                                                                : __fmul_rn(__uint2float_rn(w), FX_INV));
+                const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+                const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
+                                gz = add_wrap(o[2], lz, d);
+                atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
             }
             __syncthreads();
             break;
@@ -995,6 +1048,8 @@ extern "C" size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims,
     if (n_particles < 0 || dims <= 0) return 0;
     const int s = pick_strategy(strategy, ndim, dims, n_particles);
     // + 256 bytes at the end: the mass sum and scale of pyl_ma_overdensity
+    if (s == PYL_STRATEGY_SORTED && ndim == 3 && sorted_supported(n_particles, dims))
+        return sorted_workspace_bytes(n_particles, dims) + 256;
     if (s == PYL_STRATEGY_TILED && ndim == 3)
         return tiled_layout(nullptr, n_particles, dims).bytes + 256;
     return 256;
@@ -1017,7 +1072,19 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     const OutScale sc{1.0f, nullptr};
     int s = pick_strategy(strategy, ndim, dims, n);
-    if (s == PYL_STRATEGY_SORTED) s = PYL_STRATEGY_TILED;
+    if (s == PYL_STRATEGY_SORTED) {
+        if (ndim != 3 || !sorted_supported(n, dims)) {
+            set_error("pyl_ma: the sorted strategy needs a 3D grid with dims^3 <= 2^32 and < 2^32 particles");
+            return PYL_ERR_UNSUPPORTED;
+        }
+        const size_t need = sorted_workspace_bytes(n, dims);
+        if (workspace_bytes < need || workspace == nullptr) {
+            set_error("pyl_ma: sorted strategy needs " + std::to_string(need) + " workspace bytes");
+            return PYL_ERR_WORKSPACE;
+        }
+        return launch_sorted(mas, pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, workspace, 1.0f,
+                             nullptr, true, st);
+    }
     if (s == PYL_STRATEGY_TILED && (ndim != 3 || n > 0xFFFFFFF0ll)) s = PYL_STRATEGY_ATOMIC;
     if (s == PYL_STRATEGY_TILED) {
         const size_t need = tiled_layout(nullptr, n, dims).bytes;
@@ -1122,7 +1189,9 @@ extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_
     const float inv = (float)dims / box_size;
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     int s = pick_strategy(strategy, 3, dims, n);
-    if (s == PYL_STRATEGY_SORTED) s = PYL_STRATEGY_TILED;
+    if (s == PYL_STRATEGY_SORTED)
+        return launch_sorted(mas, pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, workspace, sc.host,
+                             sc.dev, false, st);
     if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
     switch (mas) {
 #define PYL_OD(M)                                                                                    \

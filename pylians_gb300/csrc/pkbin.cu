@@ -346,6 +346,220 @@ __global__ void __launch_bounds__(256) pk_bin_kernel(BinArgs a)
     }
 }
 
+// Single-field P(k) (F = 1), sequential per lane.  For each row a warp first
+// computes, with coalesced loads along kz, every mode's power |d|^2 and phase^2
+// (interlacing and the MAS deconvolution included) into a per-warp staging
+// array; then each lane walks its own run of `chunk` consecutive kz, updating
+// the |k| bin and the k_per bin incrementally (along kz each grows by at most
+// one per step) and adding to shared memory only when a bin changes.  Staging:
+// mode kz at kz + kz / chunk (one pad slot per run; chunk even, so lane runs are
+// an odd number of 8-byte slots apart and the sequential reads do not conflict).
+struct SeqSmem {
+    int corr, ph, acc3, acc1, acc2, w, stage, total;
+};
+
+__host__ __device__ inline SeqSmem seq_smem(const PkDims &d, int axis, bool inter, int chunk)
+{
+    SeqSmem s;
+    int o = 0;
+    s.corr = o; o += d.dims;
+    o = (o + 3) & ~3;
+    s.ph = o; o += inter ? 2 * d.dims : 0;
+    s.acc3 = o; o += d.nb3 * 4;
+    s.acc1 = o; o += d.nb1;
+    s.acc2 = o; o += axis == 2 ? 0 : d.kmax_per + 1;
+    s.w = o; o += axis == 2 ? NW * 2 * d.nz : 0;
+    o = (o + 3) & ~3;
+    s.stage = o; o += NW * 2 * 32 * (chunk + 1);
+    s.total = o;
+    return s;
+}
+
+inline int seq_chunk(int nz)
+{
+    int c = (nz + 31) / 32;
+    return c + (c & 1);
+}
+
+template <bool INTER, int AXIS>
+__global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk)
+{
+    extern __shared__ float sm[];
+    const PkDims d = a.d;
+    const int dims = d.dims, nz = d.nz;
+    const SeqSmem L = seq_smem(d, AXIS, INTER, chunk);
+    float *corr = sm + L.corr;
+    float2 *ph = (float2 *)(sm + L.ph);
+    float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
+    for (int i = threadIdx.x; i < dims; i += blockDim.x) corr[i] = mas_corr_f(freq_of(i, dims), dims, a.mas_p[0]);
+    if (INTER) {
+        for (int i = threadIdx.x; i < dims; i += blockDim.x) {
+            float s, c;
+            sincospif((float)freq_of(i, dims) / (float)dims, &s, &c);
+            ph[i] = make_float2(c, s);
+        }
+    }
+    for (int i = L.acc3 + threadIdx.x; i < L.stage; i += blockDim.x) sm[i] = 0.0f;
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m2 = d.middle * d.middle;
+    double *P3 = a.sums;
+    double *PH = P3 + (long long)d.nb3 * 3;
+    double *P1 = PH + d.nb3;
+    double *P2 = P1 + d.nb1;
+    float2 *stage = (float2 *)(sm + L.stage) + warp * 32 * (chunk + 1);
+    float *w2 = sm + L.w + warp * 2 * nz;             // axis 2: per-warp kz arrays
+    float *w1 = w2 + nz;
+    const int kz_begin = lane * chunk;
+    const int kz_end = min(nz, kz_begin + chunk);
+    float r1 = 0.0f;
+    int cur_ring = -1;
+
+    const RowIter it = row_iter(a, warp);
+    for (int q = 0; q < it.count; q++) {
+        int kxx, kyy;
+        row_coords(a, it, it.first + q * it.step, kxx, kyy);
+        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
+        const long long row = ((long long)kxx * dims + kyy) * nz;
+        const float cxy = __fmul_rn(corr[kxx], corr[kyy]);
+        float2 pxy = make_float2(1.0f, 0.0f);
+        if (INTER) {
+            const float2 px = ph[kxx], py = ph[kyy];
+            pxy = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
+        }
+        const int ring = AXIS == 2 ? isqrt_exact(kx * kx + ky * ky) : 0;
+        if (AXIS == 2 && ring != cur_ring) {
+            __syncwarp();
+            if (cur_ring >= 0) {
+                for (int kz = lane; kz < nz; kz += 32) {
+                    const float v = w2[kz];
+                    if (v != 0.0f) {
+                        atomicAdd(P2 + (long long)(d.kmax_par + 1) * cur_ring + kz, (double)v);
+                        w2[kz] = 0.0f;
+                    }
+                }
+            }
+            cur_ring = ring;
+            __syncwarp();
+        }
+        // pass 1: per-mode power and phase^2, coalesced along kz
+        int c = 0, rem = lane;                         // kz = c * chunk + rem
+        while (rem >= chunk) { rem -= chunk; c++; }
+#pragma unroll 2
+        for (int kz = lane; kz < nz; kz += 32) {
+            float2 v = __ldg(a.dk + row + kz);
+            if (INTER) {
+                const float2 w = __ldg(a.dk2 + row + kz);
+                const float2 t = ph[kz];
+                const float2 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
+                v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
+                v.y = 0.5f * (v.y + (w.x * pz.y + w.y * pz.x));
+            }
+            const float mf = __fmul_rn(cxy, corr[kz]);
+            const float re = __fmul_rn(v.x, mf), im = __fmul_rn(v.y, mf);
+            float p2 = re * re + im * im;
+            float phase = p2 > 0.0f ? atan_unit(re * rsqrtf(p2)) : 0.0f;
+            if (hermitian_skip(kx, ky, kz, d)) { p2 = 0.0f; phase = 0.0f; }
+            stage[c * (chunk + 1) + rem] = make_float2(p2, phase * phase);
+            rem += 32;
+            while (rem >= chunk) { rem -= chunk; c++; }
+        }
+        __syncwarp();
+        // pass 2: this lane's run of kz, sums kept while the bins stay the same
+        if (kz_begin < kz_end) {
+            const int kperp2 = AXIS == 0 ? ky * ky : kx * kx;     // axes 0/1: k_per^2 - kz^2
+            const int kxy2 = kx * kx + ky * ky;
+            int kz = kz_begin;
+            int n2 = kxy2 + kz * kz;
+            int ki = isqrt_exact(n2);
+            int kp2 = kperp2 + kz * kz;
+            int kper = AXIS == 2 ? ring : isqrt_exact(kp2);
+            const int kpar_c = AXIS == 0 ? kx * kx : ky * ky;
+            float s0 = 0.0f, s2 = 0.0f, s4 = 0.0f, sp = 0.0f, sd = 0.0f;
+            const float2 *run = stage + lane * (chunk + 1);
+            for (; kz < kz_end; kz++) {
+                const float2 e = run[kz - kz_begin];
+                const float val = e.x;
+                const int kpar2 = AXIS == 2 ? kz * kz : kpar_c;
+                const float mu2 = n2 ? __fdividef((float)kpar2, (float)n2) : 0.0f;
+                const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
+                const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
+                s0 += val;
+                s2 += val * l2;
+                s4 += val * l4;
+                sp += e.y;
+                if (AXIS == 2) {
+                    w2[kz] += val;
+                    if (n2 <= m2) w1[kz] += val;
+                } else {
+                    sd += val;
+                    if (n2 <= m2) r1 += val;
+                }
+                // step to kz + 1
+                const int dn = 2 * kz + 1;
+                n2 += dn;
+                const bool new3 = (ki + 1) * (ki + 1) <= n2;
+                bool new2 = false;
+                if (AXIS != 2) {
+                    kp2 += dn;
+                    new2 = (kper + 1) * (kper + 1) <= kp2;
+                }
+                if (new3 || kz + 1 == kz_end) {
+                    float *b3 = acc3 + ki * 4;
+                    if (s0 != 0.0f) atomicAdd(b3, s0);
+                    if (s2 != 0.0f) atomicAdd(b3 + 1, s2);
+                    if (s4 != 0.0f) atomicAdd(b3 + 2, s4);
+                    if (sp != 0.0f) atomicAdd(b3 + 3, sp);
+                    s0 = s2 = s4 = sp = 0.0f;
+                    ki += new3 ? 1 : 0;
+                }
+                if (AXIS != 2 && (new2 || kz + 1 == kz_end)) {
+                    if (sd != 0.0f) atomicAdd(acc2 + kper, sd);
+                    sd = 0.0f;
+                    kper += new2 ? 1 : 0;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // per-warp flushes
+    if (AXIS != 2) {
+        float v = r1;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(acc1 + abs(freq_of(it.plane, dims)), v);
+    } else {
+        __syncwarp();
+        for (int kz = lane; kz < nz; kz += 32) {
+            const float v2 = w2[kz];
+            if (cur_ring >= 0 && v2 != 0.0f)
+                atomicAdd(P2 + (long long)(d.kmax_par + 1) * cur_ring + kz, (double)v2);
+            const float v1 = w1[kz];
+            if (v1 != 0.0f) atomicAdd(P1 + kz, (double)v1);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d.nb3 * 4; i += blockDim.x) {
+        const float v = acc3[i];
+        if (v == 0.0f) continue;
+        const int bin = i >> 2, s = i & 3;
+        if (s < 3) atomicAdd(P3 + (long long)bin * 3 + s, (double)v);
+        else atomicAdd(PH + bin, (double)v);
+    }
+    if (AXIS != 2) {
+        for (int i = threadIdx.x; i < d.nb1; i += blockDim.x) {
+            const float v = acc1[i];
+            if (v != 0.0f) atomicAdd(P1 + i, (double)v);
+        }
+        const int kpar = abs(freq_of(it.plane, dims));
+        for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) {
+            const float v = acc2[i];
+            if (v == 0.0f) continue;
+            atomicAdd(P2 + (long long)(d.kmax_par + 1) * i + kpar, (double)v);
+        }
+    }
+}
+
 // Data-independent per-bin sums with the same traversal: N3 and K3 = sum |k|
 // by 3D bin, N1 by |k_par| for |k| <= N/2 (K1 = |k_par| N1), N2 by 2D bin.
 // shared memory (doubles): N3[nb3] K3[nb3] N1[nb1] N2[kmax_per+1] (axis 0/1) or
@@ -587,6 +801,34 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
         a.rows_per_cta = 0;
         a.warp_arrays = 0;
         blocks = (unsigned)(dims * a.chunks);
+    }
+    if (n_fields == 1 && (axis != 2 || a.warp_arrays)) {
+        const int chunk = seq_chunk(d.nz);
+        if (axis != 2) {
+            // enough CTAs for several waves at 2-3 resident CTAs per SM
+            int c = 1;
+            while ((long long)dims * c < 8LL * num_sms() && c * 2 * NW <= dims) c *= 2;
+            a.chunks = c;
+            blocks = (unsigned)(dims * c);
+        }
+        const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk).total;
+        if (sms <= SMEM_LIMIT) {
+            PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
+#define PYL_SEQ(I, A)                                                              \
+    do {                                                                           \
+        static size_t done = 0;                                                    \
+        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms, &done));                \
+        pk_bin_seq_kernel<I, A><<<blocks, 256, sms, st>>>(a, chunk);               \
+    } while (0)
+            if (inter) {
+                if (axis == 0) PYL_SEQ(true, 0); else if (axis == 1) PYL_SEQ(true, 1); else PYL_SEQ(true, 2);
+            } else {
+                if (axis == 0) PYL_SEQ(false, 0); else if (axis == 1) PYL_SEQ(false, 1); else PYL_SEQ(false, 2);
+            }
+#undef PYL_SEQ
+            PYL_LAUNCH_CHECK();
+            return PYL_OK;
+        }
     }
     const size_t smem = sizeof(float) * (size_t)bin_smem(d, a.F, a.C, axis, inter, a.warp_arrays).total;
     if (smem > SMEM_LIMIT) {

@@ -1,0 +1,532 @@
+// SORTED strategy of pyl_ma / pyl_ma_overdensity: a deterministic mass
+// assignment built from a sort by cell key and a per-cell segmented reduction.
+//
+//   1. key kernel: every particle's base cell (the first cell of its support on
+//      each axis, wrapped; MAS_library.pyx:123-545 index arithmetic) as a 32-bit
+//      key (ix*dims + iy)*dims + iz, value = particle index.
+//   2. stable LSD radix sort of (key, index), 8-bit digits: per-tile digit
+//      histograms, one exclusive scan over [digit][tile], and a scatter that
+//      ranks each tile's keys stably (warp match + per-warp digit counts) and
+//      stages them in shared memory so global writes are coalesced.  Equal keys
+//      keep increasing particle index.
+//   3. run table: for every cell the [start, end) range of its particles in the
+//      sorted order (empty cells keep the all-ones marker).
+//   4. the particles' positions (and weights) gathered into sorted order.
+//   5. gather deposit: one thread per output cell walks the S^3 (interlaced
+//      grid: (S+1)^3) neighbouring base cells in a fixed order and, within each
+//      run, the particles in index order, recomputing the weight of its corner.
+//      No atomics: every cell's sum has one fixed order, so the grid is
+//      bit-reproducible whatever the launch configuration; NGP sums each cell's
+//      particles in index order, exactly the serial reference loop.
+// Limits: dims^3 <= 2^32 (dims <= 1625) and fewer than 2^32 particles.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "common.cuh"
+#include "sorted.cuh"
+
+namespace pyl {
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;       // 4096 keys per tile
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;  // 4096 entries per scan block
+constexpr unsigned EMPTY = 0xffffffffu;
+
+template <int MAS>
+__device__ __forceinline__ int sd_first(float p, float inv)
+{
+    const float dist = __fmul_rn(p, inv);
+    if (MAS == PYL_MAS_CIC) return __float2int_rz(dist);
+    const float fl = floorf(dist);
+    const float frac = __fsub_rn(dist, fl);
+    const int fi = __float2int_rz(fl);
+    if (MAS == PYL_MAS_NGP) {
+        int k = fi + (frac >= 0.5f ? 1 : 0);
+        if (dist < -0.5f && frac != 0.5f) k += 1;
+        return k;
+    }
+    if (MAS == PYL_MAS_TSC) return fi - 1 + (frac >= 0.5f ? 1 : 0);
+    return fi - 1;
+}
+
+// Weight of support cell j (0 <= j < S) of one coordinate and the first cell;
+// the same float arithmetic as the scatter kernels (mas.cu axis_weights).
+template <int MAS>
+__device__ __forceinline__ float sd_weight(float p, float inv, int j, int *first)
+{
+    const float dist = __fmul_rn(p, inv);
+    if (MAS == PYL_MAS_NGP) {
+        *first = sd_first<MAS>(p, inv);
+        return 1.0f;
+    } else if (MAS == PYL_MAS_CIC) {
+        const float t = truncf(dist);
+        const float u = __fsub_rn(dist, t);
+        *first = __float2int_rz(t);
+        return j == 0 ? __fsub_rn(1.0f, u) : u;
+    } else if (MAS == PYL_MAS_TSC) {
+        const float fl = floorf(dist);
+        const float frac = __fsub_rn(dist, fl);
+        *first = __float2int_rz(fl) - 1 + (frac >= 0.5f ? 1 : 0);
+        const float fmn = __fsub_rn(__fadd_rn(fl, frac >= 0.5f ? 1.0f : 0.0f), 2.0f);
+        const float diff = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
+        if (diff < 0.5f) return __fsub_rn(0.75f, __fmul_rn(diff, diff));
+        if (diff < 1.5f) {
+            const float t = __fsub_rn(1.5f, diff);
+            return __fmul_rn(__fmul_rn(0.5f, t), t);
+        }
+        return 0.0f;
+    } else {
+        const float fl = floorf(dist);
+        *first = __float2int_rz(fl) - 1;
+        const float fmn = __fsub_rn(fl, 2.0f);
+        const float d = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
+        if (d < 1.0f) {
+            const float a = __fmul_rn(__fmul_rn(6.0f, d), d);
+            const float b = __fmul_rn(__fmul_rn(__fmul_rn(3.0f, d), d), d);
+            return __fdiv_rn(__fadd_rn(__fsub_rn(4.0f, a), b), 6.0f);
+        }
+        if (d < 2.0f) {
+            const float t = __fsub_rn(2.0f, d);
+            return __fdiv_rn(__fmul_rn(__fmul_rn(t, t), t), 6.0f);
+        }
+        return 0.0f;
+    }
+}
+
+// ---- 1. keys --------------------------------------------------------------
+template <int MAS>
+__global__ void __launch_bounds__(256) sd_key_kernel(const float *__restrict__ pos, long long n, float inv,
+                                                     int dims, unsigned *__restrict__ keys,
+                                                     unsigned *__restrict__ vals)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const unsigned d = (unsigned)dims;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned cx = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i), inv), dims);
+        const unsigned cy = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i + 1), inv), dims);
+        const unsigned cz = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i + 2), inv), dims);
+        keys[i] = (cx * d + cy) * d + cz;
+        vals[i] = (unsigned)i;
+    }
+}
+
+// ---- 2. radix sort ----------------------------------------------------------
+// Per-tile histogram of one digit, stored digit-major: hist[digit * tiles + tile].
+__global__ void __launch_bounds__(RS_THREADS) rs_hist_kernel(const unsigned *__restrict__ keys, long long n,
+                                                             int shift, unsigned tiles,
+                                                             unsigned *__restrict__ hist)
+{
+    __shared__ unsigned h[256];
+    h[threadIdx.x] = 0u;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * RS_TILE;
+#pragma unroll 4
+    for (int r = 0; r < RS_ITEMS; r++) {
+        const long long i = base + r * RS_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(long long)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of a block of SCAN_THREADS values (one per thread); returns the
+// block total through *total.
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *warp_sums, unsigned *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned s = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const unsigned prefix = (warp ? warp_sums[warp - 1] : 0u) + x - v;
+    if (total) *total = warp_sums[nw - 1];
+    __syncthreads();
+    return prefix;
+}
+
+// Scan phase 1: sum of each SCAN_BLOCK slice.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const unsigned *__restrict__ a, long long n,
+                                                                   unsigned *__restrict__ partial)
+{
+    __shared__ unsigned ws[32];
+    const long long base = (long long)blockIdx.x * SCAN_BLOCK;
+    unsigned s = 0u;
+#pragma unroll
+    for (int r = 0; r < SCAN_ITEMS; r++) {
+        const long long i = base + r * SCAN_THREADS + threadIdx.x;
+        if (i < n) s += a[i];
+    }
+    unsigned tot;
+    block_excl_scan(s, ws, &tot);
+    if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+// Scan phase 2: exclusive scan of the partial sums by one block.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_partials_kernel(unsigned *__restrict__ partial, long long m)
+{
+    __shared__ unsigned ws[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0u;
+    __syncthreads();
+    for (long long b = 0; b < m; b += SCAN_THREADS) {
+        const long long i = b + threadIdx.x;
+        const unsigned v = i < m ? partial[i] : 0u;
+        unsigned tot;
+        const unsigned ex = block_excl_scan(v, ws, &tot);
+        if (i < m) partial[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+}
+
+// Scan phase 3: exclusive scan of each slice in place, offset by its partial.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(unsigned *__restrict__ a, long long n,
+                                                                  const unsigned *__restrict__ partial)
+{
+    __shared__ unsigned ws[32];
+    const long long base = (long long)blockIdx.x * SCAN_BLOCK + (long long)threadIdx.x * SCAN_ITEMS;
+    unsigned v[SCAN_ITEMS];
+    unsigned s = 0u;
+#pragma unroll
+    for (int r = 0; r < SCAN_ITEMS; r++) {
+        v[r] = base + r < n ? a[base + r] : 0u;
+        s += v[r];
+    }
+    unsigned run = partial[blockIdx.x] + block_excl_scan(s, ws, nullptr);
+#pragma unroll
+    for (int r = 0; r < SCAN_ITEMS; r++) {
+        if (base + r < n) a[base + r] = run;
+        run += v[r];
+    }
+}
+
+// Stable scatter of one tile by one digit.  Element e = r*RS_THREADS + t of the
+// tile (round r, thread t) ranks after every element of the tile with the same
+// digit and a smaller e.  Per round, each warp's count of a digit is published
+// in wc[warp][digit] tagged with the round number (no clearing between rounds).
+__global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(
+    const unsigned *__restrict__ kin, const unsigned *__restrict__ vin, long long n, int shift, unsigned tiles,
+    const unsigned *__restrict__ goff, unsigned *__restrict__ kout, unsigned *__restrict__ vout)
+{
+    __shared__ unsigned sk[RS_TILE], sv[RS_TILE];
+    __shared__ unsigned wc[RS_WARPS][256];
+    __shared__ unsigned run[256];      // elements of each digit ranked so far
+    __shared__ unsigned start[256];    // first staging slot of each digit
+    __shared__ unsigned gbase[256];    // global position of the digit's first element
+    __shared__ unsigned h[256];
+    __shared__ unsigned ws[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const long long base = (long long)blockIdx.x * RS_TILE;
+    for (int i = t; i < RS_WARPS * 256; i += RS_THREADS) (&wc[0][0])[i] = 0xffffffffu;
+    run[t] = 0u;
+    h[t] = 0u;
+    unsigned dg[RS_ITEMS], key[RS_ITEMS], val[RS_ITEMS];
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; r++) {
+        const long long i = base + r * RS_THREADS + t;
+        key[r] = i < n ? kin[i] : 0u;
+        val[r] = i < n ? vin[i] : 0u;
+        dg[r] = i < n ? ((key[r] >> shift) & 255u) : 256u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; r++)
+        if (dg[r] < 256u) atomicAdd(&h[dg[r]], 1u);
+    __syncthreads();
+    start[t] = block_excl_scan(h[t], ws, nullptr);
+    gbase[t] = goff[(long long)t * tiles + blockIdx.x];
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; r++) {
+        const unsigned d = dg[r];
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned lrank = __popc(peers & lt);
+        if (lrank == 0u && d < 256u) wc[warp][d] = ((unsigned)r << 8) | (unsigned)__popc(peers);
+        __syncthreads();
+        if (d < 256u) {
+            unsigned before = run[d];
+            for (int w = 0; w < warp; w++) {
+                const unsigned v = wc[w][d];
+                before += (v >> 8) == (unsigned)r ? (v & 255u) : 0u;
+            }
+            const unsigned slot = start[d] + before + lrank;
+            sk[slot] = key[r];
+            sv[slot] = val[r];
+        }
+        __syncthreads();
+        unsigned add = 0u;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            const unsigned v = wc[w][t];
+            add += (v >> 8) == (unsigned)r ? (v & 255u) : 0u;
+        }
+        run[t] += add;
+        __syncthreads();
+    }
+    const unsigned cnt = (unsigned)min((long long)RS_TILE, n - base);
+    for (unsigned p = t; p < cnt; p += RS_THREADS) {
+        const unsigned k = sk[p];
+        const unsigned d = (k >> shift) & 255u;
+        const unsigned g = gbase[d] + (p - start[d]);
+        kout[g] = k;
+        vout[g] = sv[p];
+    }
+}
+
+// ---- 3. run table -------------------------------------------------------------
+__global__ void __launch_bounds__(256) sd_runs_kernel(const unsigned *__restrict__ keys, long long n,
+                                                      uint2 *__restrict__ runs)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const unsigned k = keys[j];
+        if (j == 0 || keys[j - 1] != k) runs[k].x = (unsigned)j;
+        if (j == n - 1 || keys[j + 1] != k) runs[k].y = (unsigned)(j + 1);
+    }
+}
+
+__global__ void __launch_bounds__(256) sd_fill2_kernel(uint2 *__restrict__ p, long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        p[i] = make_uint2(EMPTY, EMPTY);
+}
+
+// ---- 4. positions in sorted order -------------------------------------------
+__global__ void __launch_bounds__(256) sd_gather_kernel(const float *__restrict__ pos, const float *__restrict__ w,
+                                                        const unsigned *__restrict__ vals, long long n,
+                                                        float4 *__restrict__ spos)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const long long i = vals[j];
+        spos[j] = make_float4(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2),
+                              w ? __ldg(w + i) : 1.0f);
+    }
+}
+
+// ---- 5. gather deposit ----------------------------------------------------------
+// Thread (x, y, z): threadIdx.x + 32*blockIdx.x = z, threadIdx.y + 8*blockIdx.y = y,
+// blockIdx.z = x.  G = 0: plain grid, offsets 0..S-1 per axis.  G = 1: the
+// half-cell-shifted grid; a particle whose shifted first cell is f0 + delta
+// (delta 0 or 1) reaches cell c from base cell c - l with corner l - delta, so
+// offsets 0..S are visited and the corner is checked.
+// scale/base: out = (fold ? out : 0) + sum in fixed order, then
+//   (fold ? sum : out_old + sum * scale).
+template <int MAS, int G, bool WEIGHTED>
+__global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restrict__ spos,
+                                                         const uint2 *__restrict__ runs, int dims, float inv,
+                                                         float halfcell, float *__restrict__ out, float scale_h,
+                                                         const float *__restrict__ scale_d, int fold)
+{
+    constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS;
+    constexpr int R = S + G;                          // offsets visited per axis
+    const int z = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int x = blockIdx.z;
+    if (z >= dims || y >= dims) return;
+    const long long d = dims;
+    const long long cell = ((long long)x * d + y) * d + z;
+    float acc = fold ? out[cell] : 0.0f;
+#pragma unroll 1
+    for (int l = 0; l < R; l++)
+#pragma unroll 1
+        for (int m = 0; m < R; m++) {
+            const long long row = ((long long)wrap_index(x - l, dims) * d + wrap_index(y - m, dims)) * d;
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                const uint2 rr = runs[row + wrap_index(z - q, dims)];
+                if (rr.x == EMPTY) continue;
+                for (unsigned j = rr.x; j < rr.y; j++) {
+                    const float4 p = spos[j];
+                    if (G == 0) {
+                        int f;
+                        const float c0 = sd_weight<MAS>(p.x, inv, l, &f);
+                        const float c1 = sd_weight<MAS>(p.y, inv, m, &f);
+                        const float c2 = sd_weight<MAS>(p.z, inv, q, &f);
+                        float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c0, c1), c2);
+                        if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
+                        acc = __fadd_rn(acc, v);
+                    } else {
+                        // corner of the shifted support: offset minus the shift of the first cell
+                        const float pp[3] = {p.x, p.y, p.z};
+                        const int off[3] = {l, m, q};
+                        float c[3];
+                        bool ok = true;
+#pragma unroll
+                        for (int a = 0; a < 3; a++) {
+                            const int f0 = sd_first<MAS>(pp[a], inv);
+                            const float ps = __fadd_rn(pp[a], halfcell);
+                            const int f1 = sd_first<MAS>(ps, inv);
+                            const int corner = off[a] - (f1 > f0 ? 1 : 0);
+                            if (corner < 0 || corner >= S) { ok = false; c[a] = 0.0f; }
+                            else { int f; c[a] = sd_weight<MAS>(ps, inv, corner, &f); }
+                        }
+                        if (!ok) continue;
+                        float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c[0], c[1]), c[2]);
+                        if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
+                        acc = __fadd_rn(acc, v);
+                    }
+                }
+            }
+        }
+    if (fold) {
+        out[cell] = acc;
+    } else if (acc != 0.0f) {
+        const float s = scale_d ? *scale_d : scale_h;
+        out[cell] = __fadd_rn(out[cell], __fmul_rn(acc, s));
+    }
+}
+
+inline size_t al(size_t v) { return (v + 255) / 256 * 256; }
+
+struct SortedWs {
+    unsigned *k0, *v0, *k1, *v1, *hist, *partial;
+    uint2 *runs;
+    float4 *spos;
+    unsigned tiles;
+    long long hist_len, parts;
+    size_t bytes;
+};
+
+SortedWs sorted_layout(void *base, long long n, int dims)
+{
+    SortedWs w;
+    const long long cells = (long long)dims * dims * dims;
+    w.tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
+    w.hist_len = 256LL * w.tiles;
+    w.parts = (w.hist_len + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    char *b = (char *)base;
+    size_t o = 0;
+    w.k0 = (unsigned *)(b + o); o = al(o + 4 * (size_t)n);
+    w.v0 = (unsigned *)(b + o); o = al(o + 4 * (size_t)n);
+    w.k1 = (unsigned *)(b + o); o = al(o + 4 * (size_t)n);
+    w.v1 = (unsigned *)(b + o); o = al(o + 4 * (size_t)n);
+    w.hist = (unsigned *)(b + o); o = al(o + 4 * (size_t)w.hist_len);
+    w.partial = (unsigned *)(b + o); o = al(o + 4 * (size_t)w.parts);
+    w.runs = (uint2 *)(b + o); o = al(o + 8 * (size_t)cells);
+    w.spos = (float4 *)(b + o); o = al(o + 16 * (size_t)n);
+    w.bytes = o;
+    return w;
+}
+
+inline unsigned blocks_for(long long n, int threads, int per_sm)
+{
+    long long b = (n + threads - 1) / threads;
+    const long long cap = (long long)num_sms() * per_sm;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+template <int MAS>
+int sorted_run(const float *pos, const float *w, long long n, float *grid, float *grid2, int dims, float inv,
+               float halfcell, void *workspace, float scale_h, const float *scale_d, bool fold, cudaStream_t st)
+{
+    SortedWs ws = sorted_layout(workspace, n, dims);
+    const long long cells = (long long)dims * dims * dims;
+    sd_key_kernel<MAS><<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, n, inv, dims, ws.k0, ws.v0);
+    PYL_LAUNCH_CHECK();
+    int bits = 1;
+    while (bits < 32 && (1ull << bits) < (unsigned long long)cells) bits++;
+    unsigned *kin = ws.k0, *vin = ws.v0, *kout = ws.k1, *vout = ws.v1;
+    for (int shift = 0; shift < bits; shift += 8) {
+        rs_hist_kernel<<<ws.tiles, RS_THREADS, 0, st>>>(kin, n, shift, ws.tiles, ws.hist);
+        PYL_LAUNCH_CHECK();
+        scan_reduce_kernel<<<(unsigned)ws.parts, SCAN_THREADS, 0, st>>>(ws.hist, ws.hist_len, ws.partial);
+        PYL_LAUNCH_CHECK();
+        scan_partials_kernel<<<1, SCAN_THREADS, 0, st>>>(ws.partial, ws.parts);
+        PYL_LAUNCH_CHECK();
+        scan_apply_kernel<<<(unsigned)ws.parts, SCAN_THREADS, 0, st>>>(ws.hist, ws.hist_len, ws.partial);
+        PYL_LAUNCH_CHECK();
+        rs_scatter_kernel<<<ws.tiles, RS_THREADS, 0, st>>>(kin, vin, n, shift, ws.tiles, ws.hist, kout, vout);
+        PYL_LAUNCH_CHECK();
+        unsigned *t = kin; kin = kout; kout = t;
+        t = vin; vin = vout; vout = t;
+    }
+    sd_fill2_kernel<<<blocks_for(cells, 256, 16), 256, 0, st>>>(ws.runs, cells);
+    PYL_LAUNCH_CHECK();
+    sd_runs_kernel<<<blocks_for(n, 256, 16), 256, 0, st>>>(kin, n, ws.runs);
+    PYL_LAUNCH_CHECK();
+    sd_gather_kernel<<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, w, vin, n, ws.spos);
+    PYL_LAUNCH_CHECK();
+    const dim3 blk(32, 8), grd((unsigned)((dims + 31) / 32), (unsigned)((dims + 7) / 8), (unsigned)dims);
+    const int f = fold ? 1 : 0;
+    if (w) {
+        sd_deposit_kernel<MAS, 0, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid,
+                                                            scale_h, scale_d, f);
+        PYL_LAUNCH_CHECK();
+        if (grid2) {
+            sd_deposit_kernel<MAS, 1, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid2,
+                                                                scale_h, scale_d, f);
+            PYL_LAUNCH_CHECK();
+        }
+    } else {
+        sd_deposit_kernel<MAS, 0, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid,
+                                                             scale_h, scale_d, f);
+        PYL_LAUNCH_CHECK();
+        if (grid2) {
+            sd_deposit_kernel<MAS, 1, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid2,
+                                                                 scale_h, scale_d, f);
+            PYL_LAUNCH_CHECK();
+        }
+    }
+    return PYL_OK;
+}
+
+}  // namespace
+
+bool sorted_supported(long long n, int dims)
+{
+    return n >= 0 && n < 0xFFFFFFFFLL && dims >= 1 && (long long)dims * dims * dims <= 0xFFFFFFFFLL;
+}
+
+size_t sorted_workspace_bytes(long long n, int dims)
+{
+    return sorted_layout(nullptr, n, dims).bytes;
+}
+
+int launch_sorted(int mas, const float *pos, const float *w, long long n, float *grid, float *grid2, int dims,
+                  float inv, float halfcell, void *workspace, float scale_h, const float *scale_d, bool fold,
+                  cudaStream_t st)
+{
+    if (!sorted_supported(n, dims)) {
+        set_error("sorted strategy: needs dims^3 <= 2^32 and fewer than 2^32 particles");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    if (n == 0) return PYL_OK;
+    switch (mas) {
+        case PYL_MAS_NGP: return sorted_run<PYL_MAS_NGP>(pos, w, n, grid, grid2, dims, inv, halfcell, workspace,
+                                                         scale_h, scale_d, fold, st);
+        case PYL_MAS_CIC: return sorted_run<PYL_MAS_CIC>(pos, w, n, grid, grid2, dims, inv, halfcell, workspace,
+                                                         scale_h, scale_d, fold, st);
+        case PYL_MAS_TSC: return sorted_run<PYL_MAS_TSC>(pos, w, n, grid, grid2, dims, inv, halfcell, workspace,
+                                                         scale_h, scale_d, fold, st);
+        case PYL_MAS_PCS: return sorted_run<PYL_MAS_PCS>(pos, w, n, grid, grid2, dims, inv, halfcell, workspace,
+                                                         scale_h, scale_d, fold, st);
+    }
+    set_error("sorted strategy: bad MAS");
+    return PYL_ERR_INVALID;
+}
+
+}  // namespace pyl

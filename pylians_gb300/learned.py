@@ -8,8 +8,9 @@ from four features of a monopole bin:
     x1 = MAS exponent - 3 (CIC -1, TSC 0, PCS +1),
     x2 = power-law slope n + 1.5,
     x3 = log10(P_shot / P(k_Nyq)) / 3,  P_shot = 1 / nbar,
-so that P_coarse(k) * exp(MLP(x)) stands in for the interlaced estimate on a
-grid four times finer.  Training pairs come from this library itself: Gaussian
+so that P_coarse(k) * exp(x0^2 MLP(x)) stands in for the interlaced estimate on a
+grid four times finer (the x0^2 envelope makes the correction vanish as k -> 0,
+where the coarse estimate is already exact).  Training pairs come from this library itself: Gaussian
 power-law fields (P ~ k^n) Poisson-sampled into particles at number density
 nbar, deposited on a coarse grid without interlacing and on a 4x finer grid
 with interlacing (pipeline.ParticlePk).  The plain interlaced fine-grid
@@ -17,6 +18,7 @@ estimate is both the training target and the fallback.
 """
 import math
 import os
+import time
 
 import numpy as np
 import torch
@@ -58,10 +60,13 @@ class MLP(object):
 
     @staticmethod
     def init_params(seed):
+        """Hidden layers N(0, 1/fan_in); the output layer starts at zero, so an untrained
+        network predicts no correction (the plain coarse estimate)."""
         rng = np.random.default_rng(seed)
         parts = []
         for fan_out, fan_in in ((64, 4), (64, 64), (64, 64), (1, 64)):
-            parts.append(rng.normal(0.0, math.sqrt(1.0 / fan_in), fan_out * fan_in))
+            std = 0.0 if fan_out == 1 else math.sqrt(1.0 / fan_in)
+            parts.append(rng.normal(0.0, 1.0, fan_out * fan_in) * std)
             parts.append(np.zeros(fan_out))
         return np.concatenate(parts).astype(np.float32)
 
@@ -144,84 +149,207 @@ def poisson_particles(delta, L, nbar, seed):
     return pos.contiguous()
 
 
-def make_pair(N, slope, nbar, MAS='CIC', seed=0, n_target=2_000_000, axis=0):
-    """One (coarse plain, 4x fine interlaced) pair: features, log-ratio target and both P(k)."""
+def make_pair(N, slope, nbar, MAS='CIC', seed=0, n_target=2_000_000, axis=0, sigma=0.3, kmax=0.85):
+    """One (coarse plain, 4x fine interlaced) pair: features, log-ratio target and both P(k).
+    The slope and shot-level features are the ones estimate_features measures on the coarse
+    spectrum (as at inference); the true values are kept beside them."""
     L = (n_target / nbar) ** (1.0 / 3.0)
-    delta, A = gaussian_field(2 * N, L, slope, seed)
+    delta, A = gaussian_field(2 * N, L, slope, seed, sigma=sigma)
     pos = poisson_particles(delta, L, nbar, seed)
     del delta
     n = pos.shape[0]
     c = ParticlePk(N, L, MAS, axis=axis, interlaced=False, max_particles=n)
     c.step(pos)
     rc = c.result()
+    del c
     f = ParticlePk(4 * N, L, MAS, axis=axis, interlaced=True, max_particles=n)
     f.step(pos)
     rf = f.result()
+    del f, pos
+    torch.cuda.empty_cache()
     kN = math.pi * N / L
     nb = len(rc.k3D)
     Pc, Pf = rc.Pk[:, 0], rf.Pk[:nb, 0]
-    sel = (rc.k3D <= 0.8 * kN) & (Pc > 0) & (Pf > 0)
-    shot = math.log10((1.0 / nbar) / A)
-    x = features(rc.k3D[sel] / kN, MAS, slope, shot)
+    sel = (rc.k3D > 0) & (rc.k3D <= kmax * kN) & (Pc > 0) & (Pf > 0)
+    s_est, shot_est = estimate_features(rc.k3D, Pc, kN, nbar)
+    x = features(rc.k3D[sel] / kN, MAS, s_est, shot_est)
     t = np.log(Pf[sel] / Pc[sel]).astype(np.float32)
     return dict(x=x, t=t, k=rc.k3D[sel], Pc=Pc[sel], Pf=Pf[sel], N=N, L=L, slope=slope, nbar=nbar,
-                MAS=MAS, shot=shot, n=n, Nmodes=rc.Nmodes3D[sel])
+                MAS=MAS, shot=math.log10((1.0 / nbar) / A), slope_est=s_est, shot_est=shot_est, n=n,
+                Nmodes=rc.Nmodes3D[sel])
 
 
-def training_set(count, seed=0, coarse=(32, 64), mas=('CIC', 'TSC', 'PCS'), n_target=1_000_000):
-    """Pairs with slope n in [-2.5, -0.5] and nbar log-uniform in [1e-4, 1] (h/Mpc)^3."""
+def training_set(count, seed=0, coarse=(128, 256), mas=('CIC', 'TSC', 'PCS'), density=(0.25, 4.0),
+                 sigma=(0.1, 0.6)):
+    """Pairs with slope n in [-2.5, -0.5], nbar log-uniform in [1e-4, 1] (h/Mpc)^3, particle
+    count (2N)^3 times a log-uniform factor in `density`, field rms log-uniform in `sigma`."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
-        out.append(make_pair(int(rng.choice(coarse)), float(rng.uniform(-2.5, -0.5)),
-                             float(10 ** rng.uniform(-4, 0)), str(rng.choice(mas)),
-                             seed=seed * 100003 + i, n_target=n_target))
+        N = int(rng.choice(coarse))
+        n_target = int((2 * N) ** 3 * math.exp(rng.uniform(math.log(density[0]), math.log(density[1]))))
+        out.append(make_pair(N, float(rng.uniform(-2.5, -0.5)), float(10 ** rng.uniform(-4, 0)),
+                             str(rng.choice(mas)), seed=seed * 100003 + i, n_target=n_target,
+                             sigma=float(math.exp(rng.uniform(math.log(sigma[0]), math.log(sigma[1]))))))
     return out
 
 
 def train(pairs, steps=2000, lr=2e-3, seed=0, model=None):
+    """Adam with a cosine learning-rate decay on all bins at once.  The network output y
+    enters as log ratio = x0^2 y, so it is fitted to t / x0^2 with weights x0^4: the same
+    squared error in the log ratio."""
     x = np.concatenate([p['x'] for p in pairs])
-    t = np.concatenate([p['t'] for p in pairs])
+    t = np.concatenate([p['t'] for p in pairs]).astype(np.float64)
+    x0 = x[:, 0].astype(np.float64)
     net = model or MLP(seed=seed)
     xd = torch.as_tensor(x, device=net.device)
-    td = torch.as_tensor(t, device=net.device)
+    td = torch.as_tensor((t / x0 ** 2).astype(np.float32), device=net.device)
+    wd = torch.as_tensor((x0 ** 4 / np.mean(x0 ** 4)).astype(np.float32), device=net.device)
     losses = []
     for s in range(steps):
         rate = lr * (0.5 * (1 + math.cos(math.pi * s / steps)) * 0.95 + 0.05)
-        losses.append(net.gradient(xd, td))
+        losses.append(net.gradient(xd, td, wd))
         net.adam(rate)
     return net, losses
 
 
 class Correction(object):
-    """P_coarse(k) * exp(MLP(features)) on monopole bins below 0.8 k_Nyq."""
+    """P_coarse(k) * exp((k/k_Nyq)^2 MLP(features)) on monopole bins below 0.8 k_Nyq."""
 
     def __init__(self, net=None, path=DEFAULT_WEIGHTS):
         self.net = net or MLP.load(path)
 
     def factor(self, k, kN, MAS, slope, shot_level):
         x = features(np.asarray(k) / kN, MAS, slope, shot_level)
-        return np.exp(self.net.forward(x).cpu().numpy().astype(np.float64))
+        y = self.net.forward(x).cpu().numpy().astype(np.float64)
+        return np.exp(x[:, 0].astype(np.float64) ** 2 * y)
 
     def apply(self, k, Pk0, kN, MAS, slope, shot_level):
         return np.asarray(Pk0) * self.factor(k, kN, MAS, slope, shot_level)
 
 
-def estimate_slope(k, Pk0, kN, lo=0.1, hi=0.4):
-    """Power-law slope from a log-log fit of the coarse monopole between lo and hi k_Nyq."""
-    sel = (k > lo * kN) & (k < hi * kN) & (Pk0 > 0)
-    return float(np.polyfit(np.log(k[sel]), np.log(Pk0[sel]), 1)[0])
+def estimate_features(k, Pk0, kN, nbar, lo=0.1, hi=0.4):
+    """(slope, shot level) of a coarse monopole: a power law is fitted to P(k) - 1/nbar
+    between lo and hi k_Nyq and extrapolated to k_Nyq; shot level = log10((1/nbar) / P(k_Nyq))."""
+    shot = 1.0 / nbar
+    sel = (k > lo * kN) & (k < hi * kN) & (Pk0 - shot > 0)
+    if sel.sum() < 3:       # shot noise dominates the fit range: fit what is above it below hi
+        sel = (k < hi * kN) & (Pk0 - shot > 0)
+    if sel.sum() < 2:
+        raise ValueError('no bins with power above shot noise below %.2f k_Nyq' % hi)
+    b, a = np.polyfit(np.log(k[sel]), np.log(Pk0[sel] - shot), 1)
+    lpn = (a + b * math.log(kN)) / math.log(10.0)
+    return float(b), float(math.log10(shot) - lpn)
+
+
+def _timed(fn, reps):
+    """Median host wall time (ms) of fn() with a device synchronize on both sides."""
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        ts.append((time.perf_counter() - w0) * 1e3)
+    return float(np.median(ts)), out
+
+
+def evaluate(N=512, side=1024, slope=-1.5, L=1000.0, MAS='CIC', seed=11, oracle_grid=0, reps=3,
+             net=None):
+    """Learned-corrected N^3 non-interlaced P(k) against the plain interlaced (2N)^3 estimate of
+    the same side^3 (expected) Poisson particles of a power-law field, and optionally against
+    an interlaced oracle_grid^3 estimate.
+
+    Features are estimated from the coarse spectrum itself (estimate_features) and the
+    known number density.  Returns a dict with the maximum and mean |ratio - 1| up to
+    0.8 k_Nyq of the coarse grid and the wall-clock times of both paths (pipeline step,
+    bin sums to host, P(k) finalisation, and for the coarse path the MLP correction)."""
+    require_cuda()
+    corr = Correction(net)
+    nbar = float(side) ** 3 / L ** 3
+    delta, _ = gaussian_field(2 * N, L, slope, seed)
+    pos = poisson_particles(delta, L, nbar, seed)
+    del delta
+    torch.cuda.empty_cache()
+    n = pos.shape[0]
+    kN = math.pi * N / L
+    c = ParticlePk(N, L, MAS, axis=0, interlaced=False, max_particles=n)
+    f = ParticlePk(2 * N, L, MAS, axis=0, interlaced=True, max_particles=n)
+
+    def coarse():
+        c.step(pos)
+        r = c.result()
+        s, shot = estimate_features(r.k3D, r.Pk[:, 0], kN, nbar)
+        return r, corr.apply(r.k3D, r.Pk[:, 0], kN, MAS, s, shot), s, shot
+
+    def fine():
+        f.step(pos)
+        return f.result()
+
+    t_c, (rc, Pcorr, s_est, shot_est) = _timed(coarse, reps)
+    t_f, rf = _timed(fine, reps)
+    nb = len(rc.k3D)
+    sel = (rc.k3D <= 0.8 * kN) & (rc.Nmodes3D > 0)
+    Pf = rf.Pk[:nb, 0]
+    err_c = np.abs(Pcorr[sel] / Pf[sel] - 1.0)
+    err_plain = np.abs(rc.Pk[sel, 0] / Pf[sel] - 1.0)
+    out = dict(N_coarse=N, N_fine=2 * N, particles=int(n), box=L, slope=slope, MAS=MAS,
+               slope_est=s_est, shot_level_est=shot_est, k_max=float(0.8 * kN), bins=int(sel.sum()),
+               max_err_learned=float(err_c.max()), mean_err_learned=float(err_c.mean()),
+               max_err_plain=float(err_plain.max()), mean_err_plain=float(err_plain.mean()),
+               ms_coarse_learned=t_c, ms_fine_interlaced=t_f, speedup=t_f / t_c,
+               k=rc.k3D[sel].tolist(), ratio_learned=(Pcorr[sel] / Pf[sel]).tolist(),
+               ratio_plain=(rc.Pk[sel, 0] / Pf[sel]).tolist())
+    del c, f
+    torch.cuda.empty_cache()
+    if oracle_grid:
+        o = ParticlePk(oracle_grid, L, MAS, axis=0, interlaced=True, max_particles=n)
+        o.step(pos)
+        ro = o.result()
+        del o
+        torch.cuda.empty_cache()
+        Po = ro.Pk[:nb, 0]
+        out.update(oracle_grid=oracle_grid,
+                   max_err_learned_vs_oracle=float(np.abs(Pcorr[sel] / Po[sel] - 1).max()),
+                   max_err_fine_vs_oracle=float(np.abs(Pf[sel] / Po[sel] - 1).max()),
+                   ratio_fine_vs_oracle=(Pf[sel] / Po[sel]).tolist())
+    return out
 
 
 def main():
-    """Train on the device and save DEFAULT_WEIGHTS (python -m pylians_gb300.learned)."""
+    """Train on the device and save DEFAULT_WEIGHTS (python -m pylians_gb300.learned), or
+    with --evaluate write the evaluation of the saved weights as JSON."""
     import argparse
+    import json
     ap = argparse.ArgumentParser()
     ap.add_argument('--pairs', type=int, default=96)
-    ap.add_argument('--steps', type=int, default=6000)
+    ap.add_argument('--steps', type=int, default=20000)
     ap.add_argument('--out', default=DEFAULT_WEIGHTS)
+    ap.add_argument('--evaluate', default=None, help='write the evaluation JSON here')
+    ap.add_argument('--coarse', type=int, default=512)
+    ap.add_argument('--side', type=int, default=1024)
+    ap.add_argument('--oracle-grid', type=int, default=0)
+    ap.add_argument('--slope', type=float, default=-1.5)
+    ap.add_argument('--mas', default='CIC')
+    ap.add_argument('--weights', default=DEFAULT_WEIGHTS)
+    ap.add_argument('--pairs-out', default=None, help='also save the training pairs (npz)')
     a = ap.parse_args()
+    if a.evaluate:
+        res = evaluate(N=a.coarse, side=a.side, slope=a.slope, MAS=a.mas, oracle_grid=a.oracle_grid,
+                       net=MLP.load(a.weights))
+        with open(a.evaluate, 'w') as fh:
+            json.dump(res, fh)
+        print(json.dumps({k: v for k, v in res.items() if not isinstance(v, list)}))
+        return
     pairs = training_set(a.pairs, seed=1)
+    if a.pairs_out:
+        np.savez(a.pairs_out, x=np.concatenate([p['x'] for p in pairs]),
+                 t=np.concatenate([p['t'] for p in pairs]),
+                 pair=np.concatenate([np.full(len(p['t']), i) for i, p in enumerate(pairs)]),
+                 meta=np.array([(p['N'], p['slope'], p['slope_est'], p['shot'], p['shot_est'], p['n'],
+                                 p['nbar'], MAS_P[p['MAS']]) for p in pairs]))
     net, losses = train(pairs, steps=a.steps)
     net.save(a.out)
     print('trained on %d pairs (%d bins): loss %.3e -> %.3e, saved %s'
