@@ -283,8 +283,8 @@ def main():
     torch.cuda.empty_cache()
     secondary = {}
     if rank == 0 and not a.no_secondary:
-        for name, fn in (('bispectrum', bench_bispectrum), ('batch', lambda: bench_batch(a.batch_size)),
-                         ('learned', bench_learned)):
+        for name, fn in (('zeldovich', bench_zeldovich), ('bispectrum', bench_bispectrum),
+                         ('batch', lambda: bench_batch(a.batch_size)), ('learned', bench_learned)):
             try:
                 secondary[name] = fn()
             except Exception as exc:     # a failed side measurement must not hide the headline line
@@ -317,6 +317,55 @@ def main():
 # our kernels per step: 2 fills, histogram, column scan, tile scan, level-A and level-B
 # placement, deposit, P(k) bin
 KERNELS_PER_STEP = 9
+
+
+def bench_zeldovich(reps=3):
+    """512^3 lattice particles displaced by the Zel'dovich field of a 256^3 Gaussian
+    field (P ~ k^-1.5 exp(-(k/0.5)^2), sigma 0.5, 1000 Mpc/h, seed 1) in redshift space
+    along axis 2 (f = 0.5): TSC and PCS onto 512^3 with and without interlacing, P(k)
+    l=0,2,4 + Pk2D along axis 2 (particles/s, device time per chain); then XPk of the
+    TSC field against the NGP field (fields/s)."""
+    import torch
+    from pylians_gb300 import synthetic
+    from pylians_gb300.pipeline import ParticlePk
+    import pylians_gb300.MAS_library as MASL
+    import pylians_gb300.Pk_library as PKL
+    pos = synthetic.zeldovich(N_field=256, N_lattice=512, BoxSize=BOX, sigma=0.5, f=0.5, rsd_axis=2, seed=1)
+    n = pos.shape[0]
+    out = dict(workload="zeldovich 512^3 particles, 512^3 grid, RSD axis 2", particles=n)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for mas in ('TSC', 'PCS'):
+        for inter in (False, True):
+            pp = ParticlePk(512, BOX, mas, axis=2, interlaced=inter, max_particles=n)
+            pp.step(pos)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                pp.step(pos)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out['%s%s' % (mas, '_interlaced' if inter else '')] = dict(ms=ms, particles_per_s=n / (ms / 1e3))
+            del pp
+            torch.cuda.empty_cache()
+    a = torch.empty((512, 512, 512), device='cuda')
+    b = torch.empty((512, 512, 512), device='cuda')
+    MASL.overdensity_device(pos, a, BOX, 'TSC')
+    MASL.overdensity_device(pos, b, BOX, 'NGP')
+    PKL.XPk([a, b], BOX, 2, ['TSC', 'NGP'])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        PKL.XPk([a, b], BOX, 2, ['TSC', 'NGP'])
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / reps
+    out['XPk_TSC_vs_NGP'] = dict(ms=t * 1e3, timing='host wall incl. sync and result copy')
+    out['metric'] = 'particles/s'
+    out['value'] = out['TSC_interlaced']['particles_per_s']
+    del a, b, pos
+    torch.cuda.empty_cache()
+    return out
 
 
 def bench_bispectrum(reps=3):
@@ -392,8 +441,20 @@ def bench_learned():
     return out
 
 
+STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort')
+
+# DRAM bytes per launch of the deposit kernel measured by ncu on the 512^3-particle,
+# 512^3-grid case (dram__bytes_read.sum + dram__bytes_write.sum; the summary and the
+# command are in profiles/bin_deposit_fx_cic_interlaced_512.md); both particles and
+# cells scale the traffic, so it is scaled by the particle count at equal density.
+DEPOSIT_TRAFFIC_512 = (4.117273e9 + 1.112000e9, 512 ** 3)
+
+
 def stage_times(pp, pos, reps):
-    """CUDA-event durations of each C-ABI call of one step, on the launching stream."""
+    """CUDA-event durations of each phase of one step on the launching stream: the
+    library's own phase timing inside pyl_ma_overdensity (pyl_stage_timing), events
+    around pyl_fft_r2c and pyl_pk_bin."""
+    import ctypes
     import torch
     from pylians_gb300 import _lib
     from pylians_gb300._device import ptr, stream_ptr
@@ -402,38 +463,60 @@ def stage_times(pp, pos, reps):
     st = stream_ptr()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     acc = np.zeros(3)
-    for _ in range(reps):
-        ev[0].record()
-        _lib.call('pyl_ma_overdensity', ptr(pos), None, n, ptr(pp.grids[0]), ptr(pp.grids[1]), d,
-                  pp.BoxSize, _lib.MAS_INDEX[pp.MAS], _lib.STRATEGY[pp.strategy], ptr(pp.ws),
-                  pp.ws_bytes, st)
-        ev[1].record()
-        _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, 2, st)
-        ev[2].record()
-        _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]), 1, pp.dk[0].numel(), d, pp.axis,
-                  pp.mas_p, ptr(pp.sums), ptr(pp.pk_ws), pp.pk_ws_bytes, st)
-        ev[3].record()
-        torch.cuda.synchronize()
-        acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+    buf = (ctypes.c_double * 8)()
+    _lib.call('pyl_stage_times', buf, 8)
+    _lib.call('pyl_stage_timing', 1)
+    try:
+        for _ in range(reps):
+            ev[0].record()
+            _lib.call('pyl_ma_overdensity', ptr(pos), None, n, ptr(pp.grids[0]), ptr(pp.grids[1]), d,
+                      pp.BoxSize, _lib.MAS_INDEX[pp.MAS], _lib.STRATEGY[pp.strategy], ptr(pp.ws),
+                      pp.ws_bytes, st)
+            ev[1].record()
+            _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, 2, st)
+            ev[2].record()
+            _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]), 1, pp.dk[0].numel(), d, pp.axis,
+                      pp.mas_p, ptr(pp.sums), ptr(pp.pk_ws), pp.pk_ws_bytes, st)
+            ev[3].record()
+            torch.cuda.synchronize()
+            acc += [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+        _lib.call('pyl_stage_times', buf, 8)
+    finally:
+        _lib.call('pyl_stage_timing', 0)
     acc /= reps
-    return dict(density=acc[0], fft_r2c=acc[1], pk_bin=acc[2])
+    out = dict(density=acc[0], fft_r2c=acc[1], pk_bin=acc[2])
+    out['density_phases'] = {name: buf[i] / reps for i, name in enumerate(STAGES) if buf[i] > 0}
+    return out
 
 
 def roofline(stages, n, dims, hbm, src):
-    """Algorithmic HBM bytes per launch of each stage:
-    density (particles -> two overdensity grids): 12 B/particle read + 2 grids x 4 B/cell written;
-    fft_r2c: 2 x (4 B/cell read + 8 B/mode written); pk_bin: 2 fields x 8 B/mode read."""
+    """Algorithmic HBM bytes per launch of each kernel or phase of the step:
+      fill (two grids of -1): 2 x 4 B/cell written;
+      hist: 12 B/particle read;  place (level A): 12 B read + 16 B written per particle;
+      place_b: 16 B read + 16 B written per particle;
+      deposit: 16 B/particle record read + 2 grids x 4 B/cell written;
+      fft_r2c: 2 x (4 B/cell read + 8 B/mode written);  pk_bin: 2 fields x 8 B/mode read.
+    The dominant single kernel is the one reported."""
     cells = dims ** 3
     modes = dims * dims * (dims // 2 + 1)
-    alg = dict(density=12.0 * n + 2 * 4.0 * cells, fft_r2c=2 * (4.0 * cells + 8.0 * modes),
+    alg = dict(fill=2 * 4.0 * cells, hist=12.0 * n, place=28.0 * n, place_b=32.0 * n,
+               deposit=16.0 * n + 2 * 4.0 * cells, fft_r2c=2 * (4.0 * cells + 8.0 * modes),
                pk_bin=2 * 8.0 * modes)
-    top = max(alg, key=lambda k: stages[k])
-    achieved = alg[top] / (stages[top] / 1e3) / 1e9
+    ms = dict(stages['density_phases'])
+    ms['fft_r2c'] = stages['fft_r2c']
+    ms['pk_bin'] = stages['pk_bin']
+    ms = {k: v for k, v in ms.items() if k in alg}
+    top = max(ms, key=lambda k: ms[k])
+    achieved = alg[top] / (ms[top] / 1e3) / 1e9
+    traffic = None
+    if top == 'deposit':
+        b512, n512 = DEPOSIT_TRAFFIC_512
+        traffic = b512 * (n / n512)
     return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
-                frac=achieved / hbm, traffic=None, peak_source=src,
-                alg_bytes=alg[top], ms=stages[top],
-                all_stages={k: dict(ms=stages[k], gbs=alg[k] / (stages[k] / 1e3) / 1e9)
-                            for k in alg})
+                frac=achieved / hbm, traffic=traffic, peak_source=src,
+                alg_bytes=alg[top], ms=ms[top],
+                all_kernels={k: dict(ms=ms[k], gbs=alg[k] / (ms[k] / 1e3) / 1e9, frac=alg[k] / (ms[k] / 1e3) / 1e9 / hbm)
+                             for k in ms})
 
 
 if __name__ == '__main__':

@@ -41,7 +41,7 @@ extern "C" {
 #define PYL_STRATEGY_AUTO 0   /* library picks by grid size and particle count */
 #define PYL_STRATEGY_ATOMIC 1 /* one thread per particle, atomics into the grid */
 #define PYL_STRATEGY_TILED 2  /* bin particles by tile, deposit tiles in shared memory */
-#define PYL_STRATEGY_SORTED 3 /* stable sort by tile + fixed-order deposit: bit-reproducible */
+#define PYL_STRATEGY_SORTED 3 /* radix sort by cell + fixed-order per-cell gather: bit-reproducible */
 
 const char *pyl_strerror(int status);
 /* Detail of the last failure on the calling host thread ("" if none). */
@@ -233,6 +233,39 @@ int pyl_mlp_backward(const void *params_bf16, const float *x, const float *act, 
                      float *dy, float *grad, void *stream);
 int pyl_mlp_adam(float *master, void *params_bf16, const float *grad, float *m, float *v, int n, float lr,
                  float beta1, float beta2, float eps, int step, void *stream);
+
+/* ---- optional per-phase timing (no counterpart in the reference; off by default) --
+ * pyl_stage_timing(1) makes pyl_ma / pyl_ma_overdensity bracket their internal
+ * phases with CUDA events on the launching stream; pyl_stage_times writes the
+ * milliseconds summed per phase since the last call into ms_out[0..n) (phases
+ * past PYL_STAGE_COUNT read 0).  Phases: */
+#define PYL_STAGE_FILL 0      /* grids filled with -1 (overdensity) */
+#define PYL_STAGE_HIST 1      /* per-chunk tile histograms and scans */
+#define PYL_STAGE_PLACE 2     /* particles to tiles (single level, or level A) */
+#define PYL_STAGE_PLACE_B 3   /* two-level placement, level B */
+#define PYL_STAGE_DEPOSIT 4   /* per-bin shared-memory deposit and write-out */
+#define PYL_STAGE_SORT 5      /* sorted strategy: keys, radix sort, runs, gather */
+#define PYL_STAGE_COUNT 8
+int pyl_stage_timing(int enable);
+int pyl_stage_times(double *ms_out, int n);
+
+/* Device-side error word (no counterpart in the reference): nonzero when a kernel's
+ * bounded wait for its own bulk copies ran out and the kernel left early (its
+ * output is then incomplete).  Synchronous; reset = 1 clears it. */
+int pyl_device_error(int reset, unsigned *out);
+
+/* ---- particle-side neighbours of the mass assignment --------------------------
+ * pyl_cic_interp replaces MAS_library.CIC_interp (library/MAS_library/MAS_library.pyx:558-599):
+ * out[i] = CIC interpolation of grid [dims]^3 at pos[i] (float32 [n][3]), the
+ * eight terms added in the reference's order; indices wrap non-negatively.
+ * pyl_pos_redshift_space replaces redshift_space_library.pos_redshift_space
+ * (library/redshift_space_library.pyx:29-43): pos[:,axis] += vel[:,axis] *
+ * (1+redshift)/Hubble in place, then positions above box_size or below 0 become
+ * fmod(pos + box_size, box_size). */
+int pyl_cic_interp(const float *grid, int dims, float box_size, const float *pos, int64_t n, float *out,
+                   void *stream);
+int pyl_pos_redshift_space(float *pos, const float *vel, int64_t n, float box_size, float hubble,
+                           float redshift, int axis, void *stream);
 
 #ifdef __cplusplus
 }

@@ -9,10 +9,11 @@ What is compiled (read from the reference tree, never copied into the repo):
   library/MAS_library/MAS_library.pyx + MAS_c.c   -> MAS_library*.so
   library/Pk_library/Pk_library.pyx               -> Pk_library*.so
   library/Pk_library/bispectrum_library.pyx       -> bispectrum_library*.so
-with the reference's own compiler flags (library/setup.py:8-21):
+  library/redshift_space_library.pyx              -> redshift_space_library*.so
+with the reference's own compiler flags (library/setup.py:8-23):
   MAS: -O3 -ffast-math -march=native -fopenmp (+ -fopenmp at link, libm)
   Pk : -O3 -ffast-math -march=native -fopenmp
-  Bk : no extra flags
+  Bk, redshift space: no extra flags
 
 The sources are Python 2 Cython.  Three things are needed to run them on
 Python 3 and they are applied to a temporary copy outside the repository
@@ -42,6 +43,7 @@ _SOURCES = {
                     'library/MAS_library/MAS_c.h', 'library/MAS_library/MAS_c.pxd'],
     'Pk_library': ['library/Pk_library/Pk_library.pyx'],
     'bispectrum_library': ['library/Pk_library/bispectrum_library.pyx'],
+    'redshift_space_library': ['library/redshift_space_library.pyx'],
 }
 
 
@@ -89,6 +91,8 @@ def build(reference=DEFAULT_REF, out=OUT, quiet=True):
                       include_dirs=inc, extra_compile_args=native),
             Extension('bispectrum_library', [os.path.join(tmp, 'bispectrum_library.pyx')],
                       include_dirs=inc),
+            Extension('redshift_space_library', [os.path.join(tmp, 'redshift_space_library.pyx')],
+                      include_dirs=inc),
         ]
         exts = cythonize(exts, compiler_directives={'language_level': 2},
                          include_path=[tmp], quiet=quiet, build_dir=os.path.join(tmp, 'c'))
@@ -119,6 +123,13 @@ def load_reference(out=OUT):
     import Pk_library
     import bispectrum_library
     return MAS_library, Pk_library, bispectrum_library
+
+
+def load_redshift_space(out=OUT):
+    """Import the compiled reference redshift_space_library."""
+    load_reference(out)
+    import redshift_space_library
+    return redshift_space_library
 
 
 if __name__ == '__main__':

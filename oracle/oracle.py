@@ -66,6 +66,11 @@ def lib():
         L.oracle_ma.restype = ctypes.c_int
         L.oracle_pk_modes.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int] + [P] * 12
         L.oracle_pk_modes.restype = ctypes.c_int
+        L.oracle_cic_interp.argtypes = [P, ctypes.c_int, ctypes.c_float, P, ctypes.c_int64, P]
+        L.oracle_cic_interp.restype = None
+        L.oracle_rsd.argtypes = [P, P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_int]
+        L.oracle_rsd.restype = None
         _lib = L
     return _lib
 
@@ -101,6 +106,20 @@ def MA(pos, number, BoxSize, MAS='CIC', W=None, renormalize_2D=True, threads=1):
     ma_kernel(pos, number, BoxSize, MAS, W, threads=threads, flavor=0)
     if number.ndim == 2 and renormalize_2D and MAS != 'NGP':
         number /= {'CIC': 2.0, 'TSC': 3.0, 'PCS': 4.0}[MAS]
+
+
+def CIC_interp(density, BoxSize, pos, den):
+    """MAS_library.CIC_interp (MAS_library.pyx:558-599): den[i] <- CIC value at pos[i]."""
+    assert density.dtype == np.float32 and density.flags.c_contiguous and density.ndim == 3
+    assert pos.dtype == np.float32 and pos.flags.c_contiguous and den.dtype == np.float32
+    lib().oracle_cic_interp(_ptr(density), density.shape[0], float(BoxSize), _ptr(pos), pos.shape[0], _ptr(den))
+
+
+def pos_redshift_space(pos, vel, BoxSize, Hubble, redshift, axis):
+    """redshift_space_library.pos_redshift_space (redshift_space_library.pyx:29-43), in place."""
+    assert pos.dtype == np.float32 and pos.flags.c_contiguous and vel.dtype == np.float32
+    assert vel.flags.c_contiguous and vel.shape == pos.shape
+    lib().oracle_rsd(_ptr(pos), _ptr(vel), pos.shape[0], float(BoxSize), float(Hubble), float(redshift), int(axis))
 
 
 # ------------------------------------------------------------------ P(k) pieces

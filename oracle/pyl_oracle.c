@@ -135,6 +135,57 @@ int oracle_ma(const float *pos, int64_t n, int ndim, float *grid, int dims,
     return 0;
 }
 
+/*
+ * MAS_library.CIC_interp (MAS_library.pyx:558-599): den[i] = sum over the 8
+ * cells around pos[i] of density * d/u weights, terms added left to right in
+ * the reference's order (d,d,d), (d,d,u), (d,u,d), (d,u,u), (u,d,d), ...
+ * Indices wrap non-negatively (the reference reads out of bounds for
+ * positions below 0).
+ */
+void oracle_cic_interp(const float *density, int dims, float box, const float *pos, int64_t n, float *den)
+{
+    const float inv = (float)dims / box;
+    for (int64_t i = 0; i < n; i++) {
+        float u[3], d[3];
+        int id[3], iu[3];
+        for (int a = 0; a < 3; a++) {
+            float dist = pos[i * 3 + a] * inv;
+            int k = (int)dist;
+            u[a] = dist - (float)k;
+            d[a] = (float)(1.0 - (double)u[a]);
+            id[a] = wrap(k, dims);
+            iu[a] = wrap(id[a] + 1, dims);
+        }
+        const int64_t D = dims;
+#define G(x, y, z) density[((int64_t)(x) * D + (y)) * D + (z)]
+        float t = G(id[0], id[1], id[2]) * d[0] * d[1] * d[2];
+        t = t + G(id[0], id[1], iu[2]) * d[0] * d[1] * u[2];
+        t = t + G(id[0], iu[1], id[2]) * d[0] * u[1] * d[2];
+        t = t + G(id[0], iu[1], iu[2]) * d[0] * u[1] * u[2];
+        t = t + G(iu[0], id[1], id[2]) * u[0] * d[1] * d[2];
+        t = t + G(iu[0], id[1], iu[2]) * u[0] * d[1] * u[2];
+        t = t + G(iu[0], iu[1], id[2]) * u[0] * u[1] * d[2];
+        t = t + G(iu[0], iu[1], iu[2]) * u[0] * u[1] * u[2];
+#undef G
+        den[i] = t;
+    }
+}
+
+/*
+ * redshift_space_library.pos_redshift_space (redshift_space_library.pyx:29-43):
+ * pos[:,axis] += vel[:,axis] * (1+z)/H, then positions above BoxSize or below 0
+ * become fmod(pos + BoxSize, BoxSize) (C remainder, as cdivision(True)).
+ */
+void oracle_rsd(float *pos, const float *vel, int64_t n, float box, float hubble, float redshift, int axis)
+{
+    const float factor = (float)((1.0 + (double)redshift) / (double)hubble);
+    for (int64_t i = 0; i < n; i++) {
+        float p = pos[i * 3 + axis] + vel[i * 3 + axis] * factor;
+        if (p > box || p < 0.0f) p = fmodf(p + box, box);
+        pos[i * 3 + axis] = p;
+    }
+}
+
 /* (x/sin x)^p with C(0)=1: Pk_library.pyx:86-87 */
 static inline double mas_correction(double x, int p)
 {

@@ -6,6 +6,7 @@ Mirrors library/MAS_library/MAS_library.pyx:
   NGPc3D/CICc3D/... (pos, number, BoxSize, threads), *Wc3D(pos, number, W, BoxSize, threads),
   *c2D                                                                            (:1136-1221)
   FLOAT_type()                                                                     (:11-13)
+  CIC_interp(density, BoxSize, pos, den)                                           (:558-599)
 
 `number` is accumulated in place (+=), as in the reference; numpy arrays are
 copied to the device and the result written back into them, CUDA tensors are
@@ -29,7 +30,7 @@ from ._device import as_device_f32, is_torch, ptr, require_cuda, stream_ptr, wor
 __all__ = ['MA', 'NGP', 'CIC', 'TSC', 'PCS', 'NGPW', 'CICW', 'TSCW', 'PCSW', 'FLOAT_type',
            'NGPc3D', 'CICc3D', 'TSCc3D', 'PCSc3D', 'NGPWc3D', 'CICWc3D', 'TSCWc3D', 'PCSWc3D',
            'NGPc2D', 'CICc2D', 'TSCc2D', 'PCSc2D', 'NGPWc2D', 'CICWc2D', 'TSCWc2D', 'PCSWc2D',
-           'ma_device', 'overdensity_device']
+           'CIC_interp', 'ma_device', 'overdensity_device']
 
 
 def FLOAT_type():
@@ -112,6 +113,27 @@ def MA(pos, number, BoxSize, MAS='CIC', W=None, verbose=False, renormalize_2D=Tr
     if verbose:
         torch.cuda.synchronize()
         print('Time taken = %.3f seconds\n' % (time.time() - start))
+
+
+def CIC_interp(density, BoxSize, pos, den):
+    """MAS_library.CIC_interp: den[i] <- CIC interpolation of the 3D density grid at
+    pos[i] (the eight corner terms added in the reference's order).  numpy arrays are
+    copied to the device and den written back; CUDA tensors are used in place."""
+    require_cuda()
+    dgrid = as_device_f32(density, 'density')
+    dpos = as_device_f32(pos, 'pos')
+    dden = as_device_f32(den, 'den')
+    if dgrid.dim() != 3 or any(s != dgrid.shape[0] for s in dgrid.shape):
+        raise ValueError('density must be a cubic 3D grid')
+    if dpos.dim() != 2 or dpos.shape[1] != 3 or dden.dim() != 1 or dden.shape[0] != dpos.shape[0]:
+        raise ValueError('pos must be (N,3) and den (N,)')
+    _lib.call('pyl_cic_interp', ptr(dgrid), dgrid.shape[0], float(BoxSize), ptr(dpos), dpos.shape[0],
+              ptr(dden), stream_ptr())
+    if is_torch(den):
+        if not den.is_cuda:
+            den.copy_(dden.cpu())
+    else:
+        np.copyto(den, dden.cpu().numpy())
 
 
 def _single(mas, weighted):

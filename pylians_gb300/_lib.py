@@ -49,6 +49,11 @@ SIGNATURES = {
     'pyl_mlp_forward': (_I, [_P, _P, _I, _P, _P, _P]),
     'pyl_mlp_backward': (_I, [_P, _P, _P, _P, _P, _P, _F, _I, _P, _P, _P, _P]),
     'pyl_mlp_adam': (_I, [_P, _P, _P, _P, _P, _I, _F, _F, _F, _F, _I, _P]),
+    'pyl_stage_timing': (_I, [_I]),
+    'pyl_stage_times': (_I, [_P, _I]),
+    'pyl_device_error': (_I, [_I, _P]),
+    'pyl_cic_interp': (_I, [_P, _I, _F, _P, _I64, _P, _P]),
+    'pyl_pos_redshift_space': (_I, [_P, _P, _I64, _F, _F, _F, _I, _P]),
 }
 
 _lib = None

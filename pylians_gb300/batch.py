@@ -29,7 +29,7 @@ ITEM_DT = np.dtype([('first', '<i8'), ('count', '<u4'), ('real', '<u4')])
 class RealizationBatch(object):
     """specs: list of dicts with keys dims, MAS, interlaced, n (particle count)."""
 
-    def __init__(self, specs, BoxSize, axis=0, device=None, tune=True, ctas_per_sm=None):
+    def __init__(self, specs, BoxSize, axis=0, device=None, tune=True, ctas_per_sm=None, order='size'):
         require_cuda()
         self.specs = [dict(s) for s in specs]
         self.BoxSize, self.axis = float(BoxSize), int(axis)
@@ -61,6 +61,9 @@ class RealizationBatch(object):
         self.item_sizes = [autotune.item_size(int(s['dims']), int(s['n']), s['MAS'], bool(s.get('interlaced')),
                                               tune=tune) for s in self.specs]
         self.ctas_per_sm = ctas_per_sm or autotune.ctas_per_sm(tune=tune)
+        if order not in ('size', 'realization'):
+            raise ValueError("order must be 'size' or 'realization'")
+        self.order = order
         self.reals_dev = None
         self.items_dev = None
         self.graph = None
@@ -87,8 +90,10 @@ class RealizationBatch(object):
             step = self.item_sizes[i]
             for first in range(0, n, step):
                 items.append((first, min(step, n - first), i))
-        # longest items first: the persistent CTAs balance the tail with the short ones
-        items.sort(key=lambda t: -t[1])
+        if self.order == 'size':
+            # longest items first: the persistent CTAs balance the tail with the short ones
+            items.sort(key=lambda t: -t[1])
+        # 'realization': realization by realization, so the CTAs in flight share few grids
         it = np.array(items, dtype=ITEM_DT)
         self.reals_dev = torch.from_numpy(reals.view(np.uint8)).to(self.device)
         self.items_dev = torch.from_numpy(it.view(np.uint8)).to(self.device)

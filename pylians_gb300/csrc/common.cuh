@@ -10,6 +10,9 @@ namespace pyl {
 
 // Thread-local detail message behind the status codes returned by the C-ABI.
 void set_error(const std::string &msg);
+// Records a CUDA event opening (begin) or closing a timed phase (PYL_STAGE_*)
+// when pyl_stage_timing is on; a no-op otherwise.
+void stage_mark(int phase, bool begin, cudaStream_t st);
 
 #define PYL_CHECK_ARG(cond, msg)                                 \
     do {                                                         \

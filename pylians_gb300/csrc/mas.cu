@@ -31,6 +31,7 @@
 
 #include "common.cuh"
 #include "sorted.cuh"
+#include "tma.cuh"
 
 namespace pyl {
 namespace {
@@ -334,9 +335,9 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
 // level B splits each (chunk, coarse) segment into its 64 tiles, again through
 // a shared-memory sort, into the final [tile][chunk] layout.  Both levels place
 // exactly where the single-level scatter would (same per-(chunk, tile) ranges).
+// (Level B is the TMA-staged level_b_tma_kernel below.)
 constexpr int TWO_LEVEL_TILES = 4096;
 constexpr int LA_THREADS = 1024, LA_U = 4, LA_BATCH = LA_THREADS * LA_U;
-constexpr int LB_THREADS = 512, LB_U = 8, LB_BATCH = LB_THREADS * LB_U;
 
 // Exclusive scan of n <= blockDim.x values in place; returns nothing, needs a
 // 32-entry scratch.  All threads of the block must call it.
@@ -428,20 +429,207 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_kernel(
     }
 }
 
+
+// ---- TMA-staged variants ---------------------------------------------------
+// The histogram and level-A kernels stream each chunk's positions, and level B
+// each (chunk, coarse block) segment's records, through two shared-memory
+// buffers filled by bulk copies (cp.async.bulk + mbarrier): the copy of batch
+// j+2 runs while batch j is processed, so the loads no longer wait on DRAM
+// latency between the batches' barriers.  Positions need a 16-byte aligned base
+// and chunks that start on multiples of 4 particles (48 bytes); the last
+// partial 16 bytes of a batch are read directly.  A wait that runs out sets
+// g_tma_error (pyl_device_error) and the CTA leaves after a bounded wait for its
+// other copy.
+__device__ unsigned g_tma_error;
+
+constexpr int HT_BATCH = 2048;                  // histogram batch (particles)
+
+// Particles of batch j wholly inside its bulk copy.
+__device__ __forceinline__ int staged_full(int cnt) { return (int)(((long long)cnt * 12 & ~15LL) / 12); }
+
+__device__ __forceinline__ unsigned staged_bytes(long long cnt) { return (unsigned)((cnt * 12) & ~15LL); }
+
+// One CTA per chunk: tile histogram of the chunk's particles (shared-memory counters).
 template <int MAS>
-__global__ void __launch_bounds__(LB_THREADS) level_b_kernel(
+__global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *__restrict__ pos, long long n,
+                                                              long long chunk, float inv, TileGeom g,
+                                                              unsigned *__restrict__ hist)
+{
+    extern __shared__ __align__(16) unsigned char hraw[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int s_ok;
+    const int T = (int)g.ntiles;
+    float *inb = (float *)hraw;                                  // [2][HT_BATCH * 3]
+    unsigned *cnt = (unsigned *)(hraw + 2 * HT_BATCH * 12);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0;
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    const long long nbat = e > b ? (e - b + HT_BATCH - 1) / HT_BATCH : 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (long long j = 0; j < 2 && j < nbat; j++) {
+            const long long s0 = b + j * HT_BATCH;
+            stage_copy(inb + (j & 1) * HT_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)HT_BATCH, e - s0)),
+                       &bar[j & 1]);
+        }
+    for (long long j = 0; j < nbat; j++) {
+        const long long s0 = b + j * HT_BATCH;
+        const int c = (int)min((long long)HT_BATCH, e - s0);
+        const int full = staged_full(c);
+        const float *in = inb + (j & 1) * HT_BATCH * 3;
+        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (unsigned)((j >> 1) & 1), &g_tma_error);
+        __syncthreads();
+        if (!s_ok) {
+            if (threadIdx.x == 0 && j + 1 < nbat)
+                mbar_wait_bounded(&bar[(j + 1) & 1], (unsigned)(((j + 1) >> 1) & 1), &g_tma_error);
+            return;
+        }
+        for (int i = threadIdx.x; i < c; i += blockDim.x) {
+            float p[3];
+            if (i < full) { p[0] = in[3 * i]; p[1] = in[3 * i + 1]; p[2] = in[3 * i + 2]; }
+            else { const long long q = s0 + i; p[0] = __ldg(pos + 3 * q); p[1] = __ldg(pos + 3 * q + 1); p[2] = __ldg(pos + 3 * q + 2); }
+            atomicAdd(cnt + tile_key<MAS>(p, inv, g), 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && j + 2 < nbat) {
+            const long long s2 = b + (j + 2) * HT_BATCH;
+            stage_copy(inb + (j & 1) * HT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)HT_BATCH, e - s2)),
+                       &bar[j & 1]);
+        }
+    }
+    __syncthreads();
+    unsigned *row = hist + (long long)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = cnt[t];
+}
+
+inline size_t hist_tma_smem(long long ntiles) { return (size_t)2 * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
+
+template <int MAS, bool WEIGHTED>
+__global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
+    const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
+    TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
+    float4 *__restrict__ tmp)
+{
+    extern __shared__ __align__(16) unsigned char araw[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int s_ok;
+    const int NCO = g.nc * g.nc * g.nc;
+    const int T = (int)g.ntiles;
+    float *inb = (float *)araw;                                            // [2][LA_BATCH * 3]
+    float4 *stage = (float4 *)(araw + 2 * LA_BATCH * 12);
+    unsigned short *sco = (unsigned short *)(stage + LA_BATCH);
+    unsigned *cur = (unsigned *)(sco + LA_BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
+    const unsigned *row = colpre + (long long)blockIdx.x * T;
+    for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
+        unsigned sacc = 0;
+        for (int l = 0; l < 64; l++) sacc += row[co * 64 + l];
+        cur[co] = offsets[co * 64] + sacc;
+    }
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    const long long nbat = e > b ? (e - b + LA_BATCH - 1) / LA_BATCH : 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (long long j = 0; j < 2 && j < nbat; j++) {
+            const long long s0 = b + j * LA_BATCH;
+            stage_copy(inb + (j & 1) * LA_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)LA_BATCH, e - s0)),
+                       &bar[j & 1]);
+        }
+    for (long long j = 0; j < nbat; j++) {
+        const long long s0 = b + j * LA_BATCH;
+        const int c = (int)min((long long)LA_BATCH, e - s0);
+        const int full = staged_full(c);
+        const float *in = inb + (j & 1) * LA_BATCH * 3;
+        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (unsigned)((j >> 1) & 1), &g_tma_error);
+        for (int co = threadIdx.x; co < NCO; co += blockDim.x) bcnt[co] = 0u;
+        __syncthreads();
+        if (!s_ok) {
+            if (threadIdx.x == 0 && j + 1 < nbat)
+                mbar_wait_bounded(&bar[(j + 1) & 1], (unsigned)(((j + 1) >> 1) & 1), &g_tma_error);
+            return;
+        }
+        float4 r[LA_U];
+        unsigned co_u[LA_U], rank[LA_U];
+#pragma unroll
+        for (int u = 0; u < LA_U; u++) {
+            const int i = threadIdx.x + u * LA_THREADS;
+            co_u[u] = 0xffffffffu;
+            if (i < c) {
+                if (i < full) r[u] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 1.0f);
+                else {
+                    const long long q = s0 + i;
+                    r[u] = make_float4(__ldg(pos + 3 * q), __ldg(pos + 3 * q + 1), __ldg(pos + 3 * q + 2), 1.0f);
+                }
+                if (WEIGHTED) r[u].w = __ldg(w + s0 + i);
+                const float p[3] = {r[u].x, r[u].y, r[u].z};
+                co_u[u] = tile_key<MAS>(p, inv, g) >> 6;
+                rank[u] = atomicAdd(bcnt + co_u[u], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && j + 2 < nbat) {                  // this buffer is consumed
+            const long long s2 = b + (j + 2) * LA_BATCH;
+            stage_copy(inb + (j & 1) * LA_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LA_BATCH, e - s2)),
+                       &bar[j & 1]);
+        }
+        for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
+            gst[co] = cur[co];
+            cur[co] += bcnt[co];
+        }
+        __syncthreads();
+        block_exclusive_scan(bcnt, NCO, wt);
+#pragma unroll
+        for (int u = 0; u < LA_U; u++) {
+            if (co_u[u] != 0xffffffffu) {
+                const unsigned slot = bcnt[co_u[u]] + rank[u];
+                stage[slot] = r[u];
+                sco[slot] = (unsigned short)co_u[u];
+            }
+        }
+        __syncthreads();
+        for (int sidx = threadIdx.x; sidx < c; sidx += blockDim.x) {
+            const unsigned co = sco[sidx];
+            const unsigned long long dst = (unsigned long long)gst[co] + (sidx - bcnt[co]);
+            if (dst < (unsigned long long)n) tmp[dst] = stage[sidx];
+        }
+        __syncthreads();
+    }
+}
+
+inline size_t level_a_tma_smem(int nco)
+{
+    return (size_t)2 * LA_BATCH * 12 + sizeof(float4) * LA_BATCH + sizeof(unsigned short) * LA_BATCH +
+           sizeof(unsigned) * (3 * nco + 32);
+}
+
+constexpr int LBT_THREADS = 512, LBT_U = 4, LBT_BATCH = LBT_THREADS * LBT_U;   // 2048 records
+
+template <int MAS>
+__global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
     const float4 *__restrict__ tmp, int C, float inv, TileGeom g, const unsigned *__restrict__ colpre,
-    const unsigned *__restrict__ total, const unsigned *__restrict__ offsets, float4 *__restrict__ rec)
+    const unsigned *__restrict__ total, const unsigned *__restrict__ offsets, float4 *__restrict__ rec,
+    unsigned n)
 {
     __shared__ unsigned fcur[64], bcnt[64], gst[64], wt[32];
     __shared__ unsigned seg_start, seg_len;
-    extern __shared__ float4 stage[];                       // LB_BATCH records, then slo
-    unsigned char *slo = (unsigned char *)(stage + LB_BATCH);
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int s_ok;
+    extern __shared__ __align__(16) float4 braw[];
+    float4 *inb = braw;                                     // [2][LBT_BATCH]
+    float4 *stage = braw + 2 * LBT_BATCH;
+    unsigned char *slo = (unsigned char *)(stage + LBT_BATCH);
     const int NCO = g.nc * g.nc * g.nc;
     const int T = (int)g.ntiles;
     const int c = blockIdx.x / NCO, co = blockIdx.x % NCO;
     if (threadIdx.x < 32) {
-        // this chunk's segment of the coarse block: starts after the earlier chunks
         unsigned pre = 0, len = 0;
         for (int l = threadIdx.x; l < 64; l += 32) {
             const int t = co * 64 + l;
@@ -459,28 +647,51 @@ __global__ void __launch_bounds__(LB_THREADS) level_b_kernel(
         if (threadIdx.x == 0) {
             seg_start = offsets[co * 64] + pre;
             seg_len = len;
+            mbar_init(&bar[0], 1);
+            mbar_init(&bar[1], 1);
+            mbar_fence_init();
         }
     }
     __syncthreads();
-    const unsigned start = seg_start, len = seg_len;
-    for (unsigned s0 = 0; s0 < len; s0 += LB_BATCH) {
+    const unsigned start = min(seg_start, n), len = min(seg_len, n - start);
+    const unsigned nbat = (len + LBT_BATCH - 1) / LBT_BATCH;
+    if (threadIdx.x == 0)
+        for (unsigned j = 0; j < 2 && j < nbat; j++) {
+            const unsigned s0 = j * LBT_BATCH;
+            stage_copy(inb + (j & 1) * LBT_BATCH, tmp + start + s0, 16u * min((unsigned)LBT_BATCH, len - s0),
+                       &bar[j & 1]);
+        }
+    for (unsigned j = 0; j < nbat; j++) {
+        const unsigned s0 = j * LBT_BATCH;
+        const int cnt = (int)min((unsigned)LBT_BATCH, len - s0);
+        const float4 *in = inb + (j & 1) * LBT_BATCH;
+        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (j >> 1) & 1u, &g_tma_error);
         if (threadIdx.x < 64) bcnt[threadIdx.x] = 0u;
         __syncthreads();
-        float4 r[LB_U];
-        int lo_u[LB_U];
-        unsigned rank[LB_U];
+        if (!s_ok) {
+            if (threadIdx.x == 0 && j + 1 < nbat) mbar_wait_bounded(&bar[(j + 1) & 1], ((j + 1) >> 1) & 1u, &g_tma_error);
+            return;
+        }
+        float4 r[LBT_U];
+        int lo_u[LBT_U];
+        unsigned rank[LBT_U];
 #pragma unroll
-        for (int u = 0; u < LB_U; u++) {
-            const unsigned i = s0 + threadIdx.x + u * LB_THREADS;
+        for (int u = 0; u < LBT_U; u++) {
+            const int i = threadIdx.x + u * LBT_THREADS;
             lo_u[u] = -1;
-            if (i < len) {
-                r[u] = tmp[start + i];
+            if (i < cnt) {
+                r[u] = in[i];
                 const float p[3] = {r[u].x, r[u].y, r[u].z};
                 lo_u[u] = (int)(tile_key<MAS>(p, inv, g) & 63u);
                 rank[u] = atomicAdd(bcnt + lo_u[u], 1u);
             }
         }
         __syncthreads();
+        if (threadIdx.x == 0 && j + 2 < nbat) {
+            const unsigned s2 = (j + 2) * LBT_BATCH;
+            stage_copy(inb + (j & 1) * LBT_BATCH, tmp + start + s2, 16u * min((unsigned)LBT_BATCH, len - s2),
+                       &bar[j & 1]);
+        }
         if (threadIdx.x < 64) {
             gst[threadIdx.x] = fcur[threadIdx.x];
             fcur[threadIdx.x] += bcnt[threadIdx.x];
@@ -488,7 +699,7 @@ __global__ void __launch_bounds__(LB_THREADS) level_b_kernel(
         __syncthreads();
         block_exclusive_scan(bcnt, 64, wt);
 #pragma unroll
-        for (int u = 0; u < LB_U; u++) {
+        for (int u = 0; u < LBT_U; u++) {
             if (lo_u[u] >= 0) {
                 const unsigned slot = bcnt[lo_u[u]] + rank[u];
                 stage[slot] = r[u];
@@ -496,14 +707,16 @@ __global__ void __launch_bounds__(LB_THREADS) level_b_kernel(
             }
         }
         __syncthreads();
-        const int nb = (int)min((unsigned)LB_BATCH, len - s0);
-        for (int sidx = threadIdx.x; sidx < nb; sidx += blockDim.x) {
+        for (int sidx = threadIdx.x; sidx < cnt; sidx += blockDim.x) {
             const int l = slo[sidx];
-            rec[gst[l] + (sidx - bcnt[l])] = stage[sidx];
+            const unsigned long long dst = (unsigned long long)gst[l] + (sidx - bcnt[l]);
+            if (dst < n) rec[dst] = stage[sidx];
         }
         __syncthreads();
     }
 }
+
+inline size_t level_b_tma_smem() { return sizeof(float4) * 3 * LBT_BATCH + LBT_BATCH; }
 
 // Fallback binning for grids with more tiles than one CTA's shared memory can count.
 template <int MAS>
@@ -719,6 +932,7 @@ int launch_atomic(const float *pos, const float *w, long long n, float *grid, fl
 }
 
 struct TiledWs {
+    unsigned n;                  // particles binned
     unsigned *hist, *total, *offsets;
     float4 *rec;                 // binned particles: x, y, z, weight
     float4 *tmp;                 // two-level placement: the coarse-block layout
@@ -733,6 +947,7 @@ TiledWs tiled_layout(void *base, long long n, int dims)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws;
+    ws.n = (unsigned)n;
     ws.smem_hist = g.ntiles <= HIST_MAX_TILES;
     ws.chunks = num_sms() < MAX_CHUNKS ? num_sms() : MAX_CHUNKS;
     const size_t hist_len = ws.smem_hist ? (size_t)MAX_CHUNKS * g.ntiles : (size_t)g.ntiles;
@@ -858,7 +1073,7 @@ __device__ __forceinline__ void float_scatter(float *acc, int base, const float 
 template <int MAS, bool INTER>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc)
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec)
 {
     using FS = FxShape<MAS, INTER>;
     const float scale = out_scale(sc);
@@ -866,7 +1081,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     extern __shared__ __align__(16) unsigned smw[];
     float *facc = (float *)smw;
     const long long tile = blockIdx.x;
-    const unsigned begin = offsets[tile], end = offsets[tile + 1];
+    const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
     if (begin == end) return;
     int tx, ty, tz;
     tile_coords(tile, g, tx, ty, tz);
@@ -931,15 +1146,183 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     }
 }
 
+// ---- TMA-staged full-bin deposit ----------------------------------------------
+// Same arithmetic and results as bin_deposit_fx_kernel, with three changes:
+//   * each pass streams the bin's records through two shared-memory buffers of
+//     R records filled by bulk copies (batch q+2 loads while batch q deposits);
+//   * the overflow test ORs the old values returned by the atomics and checks
+//     bit 31 (512.0) once per pass: a cell can only wrap past 1024 through an
+//     add whose old value is >= 1023, so a clear bit 31 proves no cell wrapped
+//     (a set one, from cells >= 512, conservatively redoes the pass in float32);
+//   * interior bins (halo inside the grid) write out without wrapping and with
+//     32-bit cell offsets.
+// Only CIC can produce negative or NaN weights (positions below 0, non-finite
+// positions); TSC and PCS weights are in [0, 1] for any input.
+template <int MAS, int E>
+__device__ __forceinline__ unsigned fx_scatter_or(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
+{
+    constexpr int S = Support<MAS>::S;
+    if (MAS == PYL_MAS_NGP) {
+        atomicAdd(acc + base, 1u);
+        return 0u;
+    }
+    unsigned seen = 0u;
+#pragma unroll
+    for (int l = 0; l < S; l++)
+#pragma unroll
+        for (int m = 0; m < S; m++) {
+            const float c01 = __fmul_rn(C[0][l], C[1][m]);
+            const int row = base + (l * E + m) * E;
+#pragma unroll
+            for (int q = 0; q < S; q++) {
+                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
+                seen |= atomicAdd(acc + row + q, __float_as_uint(x) - FX_MAGIC_BITS);
+            }
+        }
+    return seen;
+}
+
+template <int MAS, bool INTER, int R>
+__global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
+    const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec)
+{
+    using FS = FxShape<MAS, INTER>;
+    constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
+    constexpr int PER = R / 1024;                       // records per thread and batch
+    extern __shared__ __align__(16) unsigned smw[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int s_ok;
+    float *facc = (float *)smw;
+    float4 *inb = (float4 *)(smw + FS::SMEM / 4);       // [2][R]
+    const long long tile = blockIdx.x;
+    const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
+    if (begin == end) return;
+    const float scale = out_scale(sc);
+    int tx, ty, tz;
+    tile_coords(tile, g, tx, ty, tz);
+    const int o[3] = {tx * TB, ty * TB, tz * TB};
+    const int dims = g.dims;
+    const bool interior = o[0] + E <= dims && o[1] + E <= dims && o[2] + E <= dims &&
+                          (long long)dims * dims * dims < (1LL << 32);
+    const unsigned cnt = end - begin;
+    const unsigned nb = (cnt + R - 1) / R;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned q0 = 0;                                    // batches issued by this CTA so far
+    for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
+        for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
+            uint4 *z4 = (uint4 *)smw;
+            for (int c = threadIdx.x; c < FS::SMEM / 16; c += 1024) z4[c] = make_uint4(0u, 0u, 0u, 0u);
+            if (threadIdx.x == 0)
+                for (unsigned j = 0; j < 2 && j < nb; j++) {
+                    const unsigned q = q0 + j;
+                    stage_copy(inb + (q & 1) * R, rec + begin + j * R, 16u * min((unsigned)R, cnt - j * R),
+                               &bar[q & 1]);
+                }
+            __syncthreads();
+            unsigned bad = 0u, seen = 0u;
+            for (unsigned j = 0; j < nb; j++) {
+                const unsigned q = q0 + j;
+                if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[q & 1], (q >> 1) & 1u, &g_tma_error);
+                __syncthreads();
+                if (!s_ok) {
+                    if (threadIdx.x == 0 && j + 1 < nb)
+                        mbar_wait_bounded(&bar[(q + 1) & 1], ((q + 1) >> 1) & 1u, &g_tma_error);
+                    return;
+                }
+                const float4 *in = inb + (q & 1) * R;
+                const unsigned c = min((unsigned)R, cnt - j * R);
+                float4 r[PER];
+#pragma unroll
+                for (int u = 0; u < PER; u++) r[u] = in[threadIdx.x + u * 1024];
+                __syncthreads();                                    // buffer consumed
+                if (threadIdx.x == 0 && j + 2 < nb)
+                    stage_copy(inb + (q & 1) * R, rec + begin + (j + 2) * R, 16u * min((unsigned)R, cnt - (j + 2) * R),
+                               &bar[q & 1]);
+#pragma unroll
+                for (int u = 0; u < PER; u++) {
+                    if (threadIdx.x + u * 1024 >= c) break;
+                    float C[3][S];
+                    const int b0 = pass ? fx_support<MAS, 1, E>(r[u], inv, halfcell, dims, o, C)
+                                        : fx_support<MAS, 0, E>(r[u], inv, halfcell, dims, o, C);
+                    if (mode == 0) {
+                        if (MAS == PYL_MAS_CIC) bad |= (unsigned)!(C[0][1] >= 0.0f && C[1][1] >= 0.0f && C[2][1] >= 0.0f);
+                        seen |= fx_scatter_or<MAS, E>(smw, b0, C);
+                    } else {
+                        float_scatter<MAS, E>(facc, b0, C);
+                    }
+                }
+            }
+            q0 += nb;
+            if (__syncthreads_or((int)(bad | (seen >> 31))) && mode == 0) {   // redo this pass in float32
+                __syncthreads();
+                continue;
+            }
+            float *out = pass == 0 ? grid : grid2;
+            if (interior) {
+                const unsigned base = ((unsigned)o[0] * dims + o[1]) * dims + o[2];
+                for (int c = threadIdx.x; c < CELLS; c += 1024) {
+                    const unsigned w = smw[c];
+                    if (w == 0u) continue;
+                    const float v = mode == 1 ? __uint_as_float(w)
+                                              : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
+                                                                    : __fmul_rn(__uint2float_rn(w), FX_INV));
+                    const unsigned lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+                    atomicAdd(out + (base + (lx * dims + ly) * dims + lz), __fmul_rn(v, scale));
+                }
+            } else {
+                const long long d = dims;
+                for (int c = threadIdx.x; c < CELLS; c += 1024) {
+                    const unsigned w = smw[c];
+                    if (w == 0u) continue;
+                    const float v = mode == 1 ? __uint_as_float(w)
+                                              : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
+                                                                    : __fmul_rn(__uint2float_rn(w), FX_INV));
+                    const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
+                    const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
+                                    gz = add_wrap(o[2], lz, d);
+                    atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
+                }
+            }
+            __syncthreads();
+            break;
+        }
+    }
+}
+
+// Records per staging buffer that fit beside the bin (0: no staging).
+template <int MAS, bool I>
+constexpr int fx_tma_batch()
+{
+    return FxShape<MAS, I>::SMEM + 2 * 2048 * 16 <= 227 * 1024 ? 2048
+         : FxShape<MAS, I>::SMEM + 2 * 1024 * 16 <= 227 * 1024 ? 1024 : 0;
+}
+
 template <int MAS, bool I>
 int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
                       float *grid2, OutScale sc, cudaStream_t st)
 {
     using FS = FxShape<MAS, I>;
+    constexpr int R = fx_tma_batch<MAS, I>();
+    if (R > 0) {
+        auto kern = bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024)>;
+        const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
+        static size_t done_t = 0;
+        PYL_CUDA(ensure_smem(kern, smem, &done_t));
+        kern<<<(unsigned)g.ntiles, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n);
+        PYL_LAUNCH_CHECK();
+        return PYL_OK;
+    }
     auto kern = bin_deposit_fx_kernel<MAS, I>;
     static size_t done = 0;
     PYL_CUDA(ensure_smem(kern, FS::SMEM, &done));
-    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc);
+    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc,
+                                                     ws.n);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
@@ -966,23 +1349,43 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
     const int T = (int)g.ntiles;
     if (ws.smem_hist) {
         const int C = ws.chunks;
-        const long long chunk = (n + C - 1) / C;
+        // chunks start on multiples of 4 particles (48 bytes) for the bulk copies
+        const long long chunk = ((n + C - 1) / C + 3) / 4 * 4;
+        const bool tma = (((uintptr_t)pos) & 15) == 0;
         const size_t sm = sizeof(unsigned) * T;
-        static size_t d1 = 0, d2 = 0, d3 = 0;
-        PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm, &d1));
-        chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
+        static size_t d1 = 0, d2 = 0, d3 = 0, d4 = 0;
+        stage_mark(PYL_STAGE_HIST, true, st);
+        if (tma && hist_tma_smem(T) <= 227 * 1024) {
+            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS>, hist_tma_smem(T), &d4));
+            chunk_hist_tma_kernel<MAS><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist);
+        } else {
+            PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm, &d1));
+            chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
+        }
         PYL_LAUNCH_CHECK();
         colscan_kernel<<<(T + 255) / 256, 256, 0, st>>>(ws.hist, C, T, ws.total);
         PYL_LAUNCH_CHECK();
         tile_scan_kernel<<<1, 1024, 0, st>>>(ws.total, T, ws.offsets, nullptr);
         PYL_LAUNCH_CHECK();
+        stage_mark(PYL_STAGE_HIST, false, st);
+        stage_mark(PYL_STAGE_PLACE, true, st);
         if (ws.tmp) {
             const int NCO = g.nc * g.nc * g.nc;
             const size_t sa = sizeof(unsigned) * ((3 * NCO + 32 + 3) & ~3) + sizeof(float4) * LA_BATCH +
                               sizeof(unsigned short) * LA_BATCH;
-            const size_t sb = sizeof(float4) * LB_BATCH + LB_BATCH;
-            static size_t da = 0, db = 0, dc = 0;
-            if (w) {
+            static size_t da = 0, db = 0, dta = 0, dtb = 0, dtc = 0;
+            const size_t sat = level_a_tma_smem(NCO);
+            if (tma && sat <= 227 * 1024) {
+                if (w) {
+                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat, &dta));
+                    level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                             ws.offsets, ws.tmp);
+                } else {
+                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat, &dtb));
+                    level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                              ws.offsets, ws.tmp);
+                }
+            } else if (w) {
                 PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa, &da));
                 level_a_kernel<MAS, true><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                     ws.offsets, ws.tmp);
@@ -992,9 +1395,13 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
                                                                      ws.offsets, ws.tmp);
             }
             PYL_LAUNCH_CHECK();
-            PYL_CUDA(ensure_smem(level_b_kernel<MAS>, sb, &dc));
-            level_b_kernel<MAS><<<(unsigned)(C * NCO), LB_THREADS, sb, st>>>(ws.tmp, C, inv, g, ws.hist,
-                                                                           ws.total, ws.offsets, ws.rec);
+            stage_mark(PYL_STAGE_PLACE, false, st);
+            stage_mark(PYL_STAGE_PLACE_B, true, st);
+            PYL_CUDA(ensure_smem(level_b_tma_kernel<MAS>, level_b_tma_smem(), &dtc));
+            level_b_tma_kernel<MAS><<<(unsigned)(C * NCO), LBT_THREADS, level_b_tma_smem(), st>>>(
+                ws.tmp, C, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n);
+            PYL_LAUNCH_CHECK();
+            stage_mark(PYL_STAGE_PLACE_B, false, st);
         } else if (w) {
             PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
             chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
@@ -1005,6 +1412,7 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
                                                                   ws.offsets, ws.rec);
         }
         PYL_LAUNCH_CHECK();
+        stage_mark(PYL_STAGE_PLACE, false, st);
     } else {
         PYL_CUDA(cudaMemsetAsync(ws.hist, 0, sizeof(unsigned) * g.ntiles, st));
         const int blocks = grid_blocks(n, 256, 16);
@@ -1016,23 +1424,27 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         else   tile_scatter_kernel<MAS, false><<<blocks, 256, 0, st>>>(pos, w, n, inv, g, ws.total, ws.rec);
         PYL_LAUNCH_CHECK();
     }
-    if (w) return grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
-                        : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
-    if (grid2) {
-        if (FxShape<MAS, true>::FITS) return launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
-        return launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
-    }
-    if (FxShape<MAS, false>::FITS) return launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
-    return launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    stage_mark(PYL_STAGE_DEPOSIT, true, st);
+    int rc;
+    if (w) rc = grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                      : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    else if (grid2) rc = FxShape<MAS, true>::FITS
+                             ? launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                             : launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    else rc = FxShape<MAS, false>::FITS
+                  ? launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                  : launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    stage_mark(PYL_STAGE_DEPOSIT, false, st);
+    return rc;
 }
 
+// AUTO: binning pays once a deposit has about a million particles and several per
+// bin; below that, red.global into an L2-resident grid wins.
 inline int pick_strategy(int strategy, int ndim, int dims, long long n)
 {
     if (strategy != PYL_STRATEGY_AUTO) return strategy;
     if (ndim != 3) return PYL_STRATEGY_ATOMIC;
-    const double grid_bytes = 4.0 * dims * (double)dims * dims;
-    if (grid_bytes <= 64.0 * 1024 * 1024 || n < 4 * (long long)tile_geom(dims).ntiles)
-        return PYL_STRATEGY_ATOMIC;
+    if (n < (1LL << 20) || n < 4 * (long long)tile_geom(dims).ntiles) return PYL_STRATEGY_ATOMIC;
     return PYL_STRATEGY_TILED;
 }
 
@@ -1180,12 +1592,14 @@ extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_
         sc = OutScale{0.0f, d_scale};
     }
     const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
+    stage_mark(PYL_STAGE_FILL, true, st);
     fill_kernel<<<blocks, 256, 0, st>>>(grid, cells, -1.0f);
     PYL_LAUNCH_CHECK();
     if (grid_interlaced) {
         fill_kernel<<<blocks, 256, 0, st>>>(grid_interlaced, cells, -1.0f);
         PYL_LAUNCH_CHECK();
     }
+    stage_mark(PYL_STAGE_FILL, false, st);
     const float inv = (float)dims / box_size;
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     int s = pick_strategy(strategy, 3, dims, n);
@@ -1282,4 +1696,15 @@ extern "C" int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n,
         case PYL_MAS_TSC: return launch_tiled<PYL_MAS_TSC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
         default:          return launch_tiled<PYL_MAS_PCS>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
     }
+}
+
+extern "C" int pyl_device_error(int reset, unsigned *out)
+{
+    PYL_CHECK_ARG(out != nullptr, "null pointer");
+    PYL_CUDA(cudaMemcpyFromSymbol(out, pyl::g_tma_error, sizeof(unsigned)));
+    if (reset) {
+        const unsigned zero = 0;
+        PYL_CUDA(cudaMemcpyToSymbol(pyl::g_tma_error, &zero, sizeof(unsigned)));
+    }
+    return PYL_OK;
 }

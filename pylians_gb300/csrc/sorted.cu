@@ -445,6 +445,7 @@ int sorted_run(const float *pos, const float *w, long long n, float *grid, float
 {
     SortedWs ws = sorted_layout(workspace, n, dims);
     const long long cells = (long long)dims * dims * dims;
+    stage_mark(PYL_STAGE_SORT, true, st);
     sd_key_kernel<MAS><<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, n, inv, dims, ws.k0, ws.v0);
     PYL_LAUNCH_CHECK();
     int bits = 1;
@@ -470,6 +471,8 @@ int sorted_run(const float *pos, const float *w, long long n, float *grid, float
     PYL_LAUNCH_CHECK();
     sd_gather_kernel<<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, w, vin, n, ws.spos);
     PYL_LAUNCH_CHECK();
+    stage_mark(PYL_STAGE_SORT, false, st);
+    stage_mark(PYL_STAGE_DEPOSIT, true, st);
     const dim3 blk(32, 8), grd((unsigned)((dims + 31) / 32), (unsigned)((dims + 7) / 8), (unsigned)dims);
     const int f = fold ? 1 : 0;
     if (w) {
@@ -491,6 +494,7 @@ int sorted_run(const float *pos, const float *w, long long n, float *grid, float
             PYL_LAUNCH_CHECK();
         }
     }
+    stage_mark(PYL_STAGE_DEPOSIT, false, st);
     return PYL_OK;
 }
 

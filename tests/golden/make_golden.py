@@ -148,17 +148,50 @@ def make_bk(MASL, BKL):
     return out
 
 
-def main():
+def make_interp_rsd(MASL, RSL):
+    """MAS_library.CIC_interp (MAS_library.pyx:558-599) on a random 24^3 field, and
+    redshift_space_library.pos_redshift_space (redshift_space_library.pyx:29-43) with
+    displacements that push particles below 0 and beyond BoxSize along each axis."""
+    out = {}
+    rng = np.random.default_rng(31)
+    N, L = 24, 1000.0
+    field = rng.normal(size=(N, N, N)).astype(np.float32)
+    pos = np.concatenate([(rng.random((4000, 3)) * L).astype(np.float32), edge_positions(L, N)])
+    den = np.zeros(pos.shape[0], np.float32)
+    MASL.CIC_interp(field, L, pos, den)
+    out['interp_field'] = field
+    out['interp_pos'] = pos
+    out['interp_den'] = den
+    out['interp_meta'] = np.array([N, L])
+    vel = (rng.normal(size=(4000, 3)) * 400.0).astype(np.float32)
+    rpos = (rng.random((4000, 3)) * L).astype(np.float32)
+    out['rsd_pos'] = rpos
+    out['rsd_vel'] = vel
+    out['rsd_meta'] = np.array([L, 100.0, 0.5])
+    for axis in (0, 1, 2):
+        p = rpos.copy()
+        RSL.pos_redshift_space(p, vel, L, 100.0, 0.5, axis)
+        out['rsd_out_axis%d' % axis] = p
+    return out
+
+
+def main(which=('ma', 'pk', 'bk', 'interp')):
     if not build_ref.built():
         build_ref.build()
     MASL, PKL, BKL = build_ref.load_reference()
-    np.savez_compressed(os.path.join(HERE, 'ma_golden.npz'), **make_ma(MASL))
-    np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
-    np.savez_compressed(os.path.join(HERE, 'bk_golden.npz'), **make_bk(MASL, BKL))
+    if 'ma' in which:
+        np.savez_compressed(os.path.join(HERE, 'ma_golden.npz'), **make_ma(MASL))
+    if 'pk' in which:
+        np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
+    if 'bk' in which:
+        np.savez_compressed(os.path.join(HERE, 'bk_golden.npz'), **make_bk(MASL, BKL))
+    if 'interp' in which:
+        RSL = build_ref.load_redshift_space()
+        np.savez_compressed(os.path.join(HERE, 'interp_golden.npz'), **make_interp_rsd(MASL, RSL))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
 if __name__ == '__main__':
-    main()
+    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp'))

@@ -271,3 +271,24 @@ def test_sorted_overdensity_matches_tiled(MASL):
         res[s] = (a, b)
     for i in range(2):
         assert (res['tiled'][i] - res['sorted'][i]).abs().max().item() <= 2e-6 * res['tiled'][i].abs().max().item() + 1e-6
+
+
+def test_staged_placement_reports_no_device_error(MASL):
+    """The TMA-staged histogram and placement kernels (bulk copies + bounded mbarrier
+    waits) finish without a failed wait on a two-level grid, and an offset particle
+    array (not 16-byte aligned) takes the direct-load kernels with the same result."""
+    import ctypes
+    from pylians_gb300 import _lib
+    rng = np.random.default_rng(17)
+    N, L, n = 544, 1000.0, 2_000_001
+    pos = torch.from_numpy((rng.random((n + 1, 3)) * L).astype(np.float32)).cuda()
+    word = ctypes.c_uint(0)
+    _lib.call('pyl_device_error', 1, ctypes.byref(word))
+    a = torch.zeros((N, N, N), device='cuda')
+    b = torch.zeros((N, N, N), device='cuda')
+    MASL.MA(pos[1:].contiguous(), a, L, 'CIC', strategy='tiled')
+    MASL.MA(pos[1:], b, L, 'CIC', strategy='tiled')        # 12-byte offset view
+    torch.cuda.synchronize()
+    _lib.call('pyl_device_error', 0, ctypes.byref(word))
+    assert word.value == 0
+    assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()

@@ -62,8 +62,12 @@ def check_pk(r, get, names, cross=False):
         elif n in ('k1D', 'k3D'):
             np.testing.assert_allclose(x, y, rtol=1e-12, err_msg=n)
         elif n in ('Pk', 'XPk'):
+            # floor 1e-8 of the largest monopole: bins whose power sits ~1e-6 below the
+            # peak (a displaced lattice beyond its field's Nyquist frequency) are float32
+            # deposit round-off on both sides
             p0 = np.abs(y[:, 0:1])
-            assert np.all(np.abs(x - y) <= RTOL * p0 + 1e-30), (n, np.max(np.abs(x - y) / (p0 + 1e-30)))
+            atol = 1e-8 * p0.max()
+            assert np.all(np.abs(x - y) <= RTOL * p0 + atol + 1e-30), (n, np.max(np.abs(x - y) / (p0 + atol + 1e-30)))
         else:
             ok = np.isfinite(y)
             assert np.array_equal(ok, np.isfinite(x)), n

@@ -161,3 +161,27 @@ def test_interlace_phase_reduces_aliasing():
     err_plain = np.abs(np.mean(plain.Pk[sel, 0]) / shot - 1)
     err_inter = np.abs(np.mean(inter.Pk[sel, 0]) / shot - 1)
     assert err_inter < err_plain
+
+
+@pytest.fixture(scope='module')
+def ig():
+    return np.load(os.path.join(GOLDEN, 'interp_golden.npz'))
+
+
+def test_oracle_cic_interp_golden(ig):
+    """CIC_interp restatement against the reference's output.  MAS_library.pyx is built with
+    -O3 -ffast-math -march=native (library/setup.py:8-11), which contracts and reorders the
+    eight-term sum, so the two agree to a few ulps: within 1e-6 of the field scale."""
+    pos = ig['interp_pos']
+    den = np.zeros(pos.shape[0], np.float32)
+    O.CIC_interp(ig['interp_field'], float(ig['interp_meta'][1]), pos, den)
+    np.testing.assert_allclose(den, ig['interp_den'], rtol=0, atol=1e-6 * np.abs(ig['interp_field']).max())
+
+
+@pytest.mark.parametrize('axis', [0, 1, 2])
+def test_oracle_rsd_golden(ig, axis):
+    """pos_redshift_space is built without extra flags (library/setup.py:23): bit-exact."""
+    L, H, z = (float(x) for x in ig['rsd_meta'])
+    p = ig['rsd_pos'].copy()
+    O.pos_redshift_space(p, ig['rsd_vel'], L, H, z, axis)
+    np.testing.assert_array_equal(p, ig['rsd_out_axis%d' % axis])
