@@ -130,6 +130,22 @@ int pyl_ma_batch(const pyl_batch_real *reals, int n_reals, const pyl_batch_item 
 
 /* float32 fill of n values (grids to -1 before an overdensity deposit). */
 int pyl_fill(float *p, int64_t n, float value, void *stream);
+/* p[i] *= factor (the 1/N normalisation of inverse transforms, Pk_library.IFFT3Dr_f). */
+int pyl_scale(float *p, int64_t n, float factor, void *stream);
+
+/* Batched realizations through the tiled binning (no counterpart in the
+ * reference): every realization's grid is cut into 32^3-cell bins numbered
+ * tile_base[r] + (tx*nt + ty)*nt + tz (nt = ceil(dims/32), dims <= 512;
+ * realizations with larger grids are skipped), total_tiles bins in all.  Four
+ * stream-ordered launches: per-item bin histograms, a scan, per-item placement,
+ * and one persistent deposit over all bins (10.22 fixed point per bin, the
+ * realization's MAS and interlacing), adding scale * deposit into the grids
+ * (pre-filled by the caller, e.g. with -1 for the overdensity).  reals, items
+ * and tile_base live in device memory; total_particles = sum of item counts. */
+size_t pyl_ma_batch_tiled_workspace_size(uint32_t total_tiles, int64_t total_particles);
+int pyl_ma_batch_tiled(const pyl_batch_real *reals, int n_reals, const pyl_batch_item *items, int n_items,
+                       const uint32_t *tile_base, uint32_t total_tiles, int64_t total_particles, void *workspace,
+                       size_t workspace_bytes, int ctas_per_sm, void *stream);
 
 /* ---- overdensity --------------------------------------------------------------
  * Replaces the callers' normalisation `delta /= mean; delta -= 1.0`
@@ -233,6 +249,23 @@ int pyl_mlp_backward(const void *params_bf16, const float *x, const float *act, 
                      float *dy, float *grad, void *stream);
 int pyl_mlp_adam(float *master, void *params_bf16, const float *grad, float *m, float *v, int n, float lr,
                  float beta1, float beta2, float eps, int step, void *stream);
+
+/* ---- correlation function (Pk_library.Xi, library/Pk_library/Pk_library.pyx:2035-2150) ----
+ * pyl_xi_power: in place over an R2C output, every stored mode becomes
+ * (|delta_k * W^-1|^2, 0) with the MAS factor of exponent mas_p rounded to float
+ * (:2073-2083).  The caller then runs pyl_fft_c2r (unnormalised).  pyl_xi_bin:
+ * sums over all dims^3 separations of that real grid by bin int(|r|): layout
+ * X[nb3][3] (xi, xi L2(mu), xi L4(mu)) | R[nb3] (sum |r|) | N[nb3] (counts),
+ * float64, pyl_xi_sums_len(dims) = 5 nb3 doubles; mu = r_axis / |r|. */
+/* pyl_correct_mas replaces the mode loop of Pk_library.correct_MAS
+ * (Pk_library.pyx:1776-1794) on an R2C output, in place: all stored modes but the
+ * redundant half of the kz = 0 and kz = N/2 planes times the MAS factor, then
+ * those two planes replaced by their Hermitian part, which is what the
+ * reference's C2R makes of them; pyl_fft_c2r and a 1/dims^3 scale follow. */
+int pyl_correct_mas(void *dk, int dims, int mas_p, void *stream);
+int64_t pyl_xi_sums_len(int dims);
+int pyl_xi_power(void *dk, int dims, int mas_p, void *stream);
+int pyl_xi_bin(const float *xi_grid, int dims, int axis, double *sums, void *stream);
 
 /* ---- optional per-phase timing (no counterpart in the reference; off by default) --
  * pyl_stage_timing(1) makes pyl_ma / pyl_ma_overdensity bracket their internal

@@ -378,3 +378,74 @@ def mlp_forward_backward(flat, x, t, w=None):
     g['b1'] = d1.sum(0)
     grad = np.concatenate([g[name].ravel() for name, _ in MLP_SHAPES])
     return loss, grad, y
+
+
+# ------------------------------------------------------------ correct_MAS / Xi
+def _freqs(dims):
+    """Signed frequency of each index, index dims/2 -> +dims/2 (Pk_library.pyx:1780)."""
+    i = np.arange(dims)
+    return np.where(i > dims // 2, i - dims, i)
+
+
+def _mas_factor(dims, p):
+    """float32 MAS factor of every stored half-complex mode: the float64 product of
+    the three axis factors, rounded once (Pk_library.pyx:1779-1794, 2067-2077)."""
+    f = _freqs(dims)
+    fz = np.arange(dims // 2 + 1)
+    def c(k):
+        x = np.pi * k / dims
+        with np.errstate(invalid='ignore', divide='ignore'):
+            r = np.where(k == 0, 1.0, x / np.sin(np.where(k == 0, 1.0, x)))
+        return r ** p if p else np.ones_like(x, dtype=np.float64)
+    return (c(f)[:, None, None] * c(f)[None, :, None] * c(fz)[None, None, :]).astype(np.float32)
+
+
+def correct_MAS(delta, BoxSize, MAS='CIC', threads=1):
+    """Pk_library.correct_MAS (Pk_library.pyx:1749-1806): the mode loop skips the
+    redundant half of the kz = 0 and kz = N/2 planes (:1789-1792), then a normalised
+    C2R."""
+    import scipy.fft
+    dims = delta.shape[0]
+    dk = fft_r2c(delta, threads)
+    f, fz = _freqs(dims), np.arange(dims // 2 + 1)
+    kx, ky, kz = np.meshgrid(f, f, fz, indexing='ij')
+    even = dims % 2 == 0
+    plane = (kz == 0) | ((kz == dims // 2) & even)
+    skip = plane & ((kx < 0) | (((kx == 0) | ((kx == dims // 2) & even)) & (ky < 0)))
+    dk = np.where(skip, dk, dk * _mas_factor(dims, MAS_function(MAS))).astype(np.complex64)
+    return scipy.fft.irfftn(dk, s=delta.shape, workers=max(1, threads)).astype(np.float32)
+
+
+def Xi(delta, BoxSize, MAS='CIC', axis=2, threads=1):
+    """Pk_library.Xi (Pk_library.pyx:2035-2150) restated with numpy."""
+    import scipy.fft
+    dims = delta.shape[0]
+    dk = fft_r2c(delta, threads)
+    dk = (dk * _mas_factor(dims, MAS_function(MAS))).astype(np.complex64)
+    p = (dk.real * dk.real + dk.imag * dk.imag).astype(np.float32)
+    xi = scipy.fft.irfftn(p.astype(np.complex64), s=delta.shape, workers=max(1, threads)).astype(np.float32)
+    f = _freqs(dims)
+    kx, ky, kz = np.meshgrid(f, f, f, indexing='ij')
+    k2 = kx * kx + ky * ky + kz * kz
+    k = np.sqrt(k2.astype(np.float64))
+    idx = np.floor(k + 1e-9).astype(np.int64)
+    idx = np.where((idx + 1) ** 2 <= k2, idx + 1, idx)
+    idx = np.where(idx ** 2 > k2, idx - 1, idx)
+    par = (kx, ky, kz)[axis].astype(np.float64)
+    with np.errstate(invalid='ignore', divide='ignore'):
+        mu = np.where(k == 0, 0.0, par / np.where(k == 0, 1.0, k))
+    mu2 = mu * mu
+    nb = int(np.sqrt(3.0 * (dims // 2) ** 2)) + 1
+    x = xi.astype(np.float64).ravel()
+    i = idx.ravel()
+    r3D = np.bincount(i, k.ravel(), nb)
+    N = np.bincount(i, None, nb).astype(np.float64)
+    X0 = np.bincount(i, x, nb)
+    X2 = np.bincount(i, x * (3.0 * mu2.ravel() - 1.0) / 2.0, nb)
+    X4 = np.bincount(i, x * (35.0 * mu2.ravel() ** 2 - 30.0 * mu2.ravel() + 3.0) / 8.0, nb)
+    r = _Result()
+    N1 = N[1:]
+    r.r3D = r3D[1:] / N1 * (BoxSize * 1.0 / dims)
+    r.Nmodes3D = N1
+    r.xi = np.stack([X0[1:] / N1, X2[1:] * 5.0 / N1, X4[1:] * 9.0 / N1], axis=1) / float(dims) ** 3
+    return r

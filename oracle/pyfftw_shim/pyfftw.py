@@ -8,8 +8,12 @@ reference pins no version of either (Pylians README lists "pyfftw" unpinned).
 The reference uses exactly two things (Pk_library.pyx:120-245):
   * ``pyfftw.empty_aligned(shape, dtype)``
   * ``pyfftw.FFTW(a_in, a_out, axes, flags, direction, threads)`` called as
-    ``plan(a_in, a_out)``; FFTW_FORWARD is an unnormalised R2C, FFTW_BACKWARD
-    an unnormalised C2R.
+    ``plan(a_in, a_out)``, i.e. through ``FFTW.__call__``, whose
+    ``normalise_idft`` defaults to True: FFTW_FORWARD is an unnormalised R2C,
+    FFTW_BACKWARD a C2R divided by the number of grid points.  The reference
+    relies on that: ``Xi`` scales the inverse transform of |delta_k|^2 by
+    1/dims^3 only (Pk_library.pyx:2088,2144-2146), and ``correct_MAS`` returns
+    the corrected field at the input's scale (Pk_library.pyx:1801).
 
 Both are served by ``scipy.fft`` in the input's own precision (float32 stays
 float32, as FFTW's single-precision plans do) with ``workers=threads``.
@@ -35,5 +39,5 @@ class FFTW(object):
         else:
             shape = tuple(a_out.shape[i] for i in self.axes)
             a_out[...] = _sfft.irfftn(a_in, s=shape, axes=self.axes,
-                                      norm='forward', workers=self.threads)
+                                      norm='backward', workers=self.threads)
         return a_out

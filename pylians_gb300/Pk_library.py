@@ -29,7 +29,8 @@ from . import _lib
 from ._device import as_device_c64, as_device_f32, is_torch, ptr, require_cuda, stream_ptr, workspace
 
 __all__ = ['frequencies', 'MAS_function', 'check_number_modes', 'FFT3Dr_f', 'IFFT3Dr_f',
-           'Pk', 'XPk', 'Bk', 'Bk_triangles', 'pk_sums_device', 'finalize_pk', 'geometry']
+           'Pk', 'XPk', 'Bk', 'Bk_triangles', 'Xi', 'correct_MAS', 'pk_sums_device', 'finalize_pk',
+           'geometry']
 
 
 def frequencies(BoxSize, dims):
@@ -70,12 +71,15 @@ def FFT3Dr_f(a, threads=1):
 
 
 def IFFT3Dr_f(a, threads=1):
-    """Unnormalised float32 C2R of a (dims, dims, dims//2+1) complex64 grid."""
+    """float32 C2R of a (dims, dims, dims//2+1) complex64 grid, divided by dims^3: the
+    reference calls pyFFTW plans through FFTW.__call__, whose normalise_idft defaults to
+    True (its Xi scales this transform by 1/dims^3 only, Pk_library.pyx:2144)."""
     require_cuda()
     x = as_device_c64(a, 'a').clone()     # cuFFT C2R overwrites its input
     dims = x.shape[0]
     out = torch.empty((dims,) * 3, dtype=torch.float32, device=x.device)
     _lib.call('pyl_fft_c2r', ptr(x), ptr(out), dims, 1, stream_ptr())
+    _lib.call('pyl_scale', ptr(out), out.numel(), float(np.float32(1.0 / float(dims) ** 3)), stream_ptr())
     return out if is_torch(a) else out.cpu().numpy()
 
 
@@ -222,6 +226,55 @@ class Pk(object):
             self.delta_k = dk[0] if is_torch(delta) else dk[0].cpu().numpy()
         if verbose:
             print('Time taken = %.2f seconds' % (time.time() - start))
+
+
+def correct_MAS(delta, BoxSize, MAS='CIC', threads=1):
+    """Pk_library.correct_MAS (Pk_library.pyx:1749-1806): the field with its Fourier
+    modes divided by the MAS window, back at the input's scale.  As in the reference,
+    the redundant half of the kz = 0 and kz = N/2 planes is left uncorrected
+    (:1789-1792) and those planes enter the inverse transform through their
+    Hermitian part."""
+    require_cuda()
+    x = as_device_f32(delta, 'delta')
+    dims = x.shape[0]
+    dk = torch.empty(_half_shape(dims), dtype=torch.complex64, device=x.device)
+    _lib.call('pyl_fft_r2c', ptr(x), ptr(dk), dims, 1, stream_ptr())
+    _lib.call('pyl_correct_mas', ptr(dk), dims, MAS_function(MAS), stream_ptr())
+    out = torch.empty((dims,) * 3, dtype=torch.float32, device=x.device)
+    _lib.call('pyl_fft_c2r', ptr(dk), ptr(out), dims, 1, stream_ptr())
+    _lib.call('pyl_scale', ptr(out), out.numel(), float(np.float32(1.0 / float(dims) ** 3)), stream_ptr())
+    return out if is_torch(delta) else out.cpu().numpy()
+
+
+class Xi(object):
+    """Pk_library.Xi (Pk_library.pyx:2035-2150): correlation function of a grid from the
+    inverse transform of |delta_k W^-1|^2; attributes r3D, xi ([bins, 3]: l = 0, 2, 4)
+    and Nmodes3D (bin 0 dropped, as the reference)."""
+
+    def __init__(self, delta, BoxSize, MAS='CIC', axis=2, threads=1):
+        require_cuda()
+        if axis not in (0, 1, 2):
+            raise ValueError('axis must be 0, 1 or 2')
+        x = as_device_f32(delta, 'delta')
+        dims = x.shape[0]
+        dk = torch.empty(_half_shape(dims), dtype=torch.complex64, device=x.device)
+        _lib.call('pyl_fft_r2c', ptr(x), ptr(dk), dims, 1, stream_ptr())
+        _lib.call('pyl_xi_power', ptr(dk), dims, MAS_function(MAS), stream_ptr())
+        g = torch.empty((dims,) * 3, dtype=torch.float32, device=x.device)
+        _lib.call('pyl_fft_c2r', ptr(dk), ptr(g), dims, 1, stream_ptr())
+        del dk
+        nb = _lib.load().pyl_xi_sums_len(dims) // 5
+        sums = torch.empty(5 * nb, dtype=torch.float64, device=x.device)
+        _lib.call('pyl_xi_bin', ptr(g), dims, axis, ptr(sums), stream_ptr())
+        s = sums.cpu().numpy()
+        X = s[:3 * nb].reshape(nb, 3)[1:]
+        R, N = s[3 * nb:4 * nb][1:], s[4 * nb:][1:]
+        # the unnormalised C2R carries dims^3; the reference's normalised one leaves the
+        # 1/dims^3 of its finalisation (:2144-2146)
+        norm = 1.0 / float(dims) ** 6
+        self.r3D = R / N * (BoxSize * 1.0 / dims)
+        self.Nmodes3D = N
+        self.xi = np.stack([X[:, 0] / N * norm, X[:, 1] * 5.0 / N * norm, X[:, 2] * 9.0 / N * norm], axis=1)
 
 
 class XPk(object):

@@ -32,6 +32,9 @@ SIGNATURES = {
     'pyl_ma_overdensity': (_I, [_P, _P, _I64, _P, _P, _I, _F, _I, _I, _P, _SZ, _P]),
     'pyl_ma_batch': (_I, [_P, _I, _P, _I, _P, _I, _P]),
     'pyl_fill': (_I, [_P, _I64, _F, _P]),
+    'pyl_scale': (_I, [_P, _I64, _F, _P]),
+    'pyl_ma_batch_tiled_workspace_size': (_SZ, [ctypes.c_uint32, _I64]),
+    'pyl_ma_batch_tiled': (_I, [_P, _I, _P, _I, _P, ctypes.c_uint32, _I64, _P, _SZ, _I, _P]),
     'pyl_grid_sum': (_I, [_P, _I64, _P, _P]),
     'pyl_overdensity': (_I, [_P, _I64, _P, _D, _P]),
     'pyl_fft_r2c': (_I, [_P, _P, _I, _I, _P]),
@@ -49,6 +52,10 @@ SIGNATURES = {
     'pyl_mlp_forward': (_I, [_P, _P, _I, _P, _P, _P]),
     'pyl_mlp_backward': (_I, [_P, _P, _P, _P, _P, _P, _F, _I, _P, _P, _P, _P]),
     'pyl_mlp_adam': (_I, [_P, _P, _P, _P, _P, _I, _F, _F, _F, _F, _I, _P]),
+    'pyl_correct_mas': (_I, [_P, _I, _I, _P]),
+    'pyl_xi_sums_len': (_I64, [_I]),
+    'pyl_xi_power': (_I, [_P, _I, _I, _P]),
+    'pyl_xi_bin': (_I, [_P, _I, _I, _P, _P]),
     'pyl_stage_timing': (_I, [_I]),
     'pyl_stage_times': (_I, [_P, _I]),
     'pyl_device_error': (_I, [_I, _P]),

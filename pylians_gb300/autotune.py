@@ -1,5 +1,6 @@
 """Autotuner for the batched deposit: work-item size per realization class and
-CTAs per SM of the persistent launch.
+CTAs per SM of the persistent launches, for either batch method ('tiled':
+bins + one persistent bin deposit; 'atomic': red.global work queue).
 
 Classes are (grid side, particle-count bucket (power of 2), MAS, interlaced).
 For a class the tuner deposits one synthetic realization of that class through
@@ -59,12 +60,12 @@ def _device_key():
     return torch.cuda.get_device_name(torch.cuda.current_device()).replace(' ', '_')
 
 
-def class_key(dims, n, MAS, interlaced):
+def class_key(dims, n, MAS, interlaced, method='atomic'):
     bucket = 1 << max(10, int(math.ceil(math.log2(max(n, 1)))))
-    return '%s/%d/%d/%s/%d' % (_device_key(), dims, bucket, MAS, int(interlaced))
+    return '%s/%s/%d/%d/%s/%d' % (_device_key(), method, dims, bucket, MAS, int(interlaced))
 
 
-def _time_deposit(dims, n, MAS, interlaced, item, ctas, reps=3):
+def _time_deposit(dims, n, MAS, interlaced, item, ctas, reps=3, method='atomic'):
     from .batch import ITEM_DT, REAL_DT
     dev = torch.device('cuda', torch.cuda.current_device())
     gen = torch.Generator(device=dev)
@@ -85,13 +86,22 @@ def _time_deposit(dims, n, MAS, interlaced, item, ctas, reps=3):
     idv = torch.from_numpy(items.view(np.uint8)).to(dev)
     cnt = torch.zeros(1, dtype=torch.int32, device=dev)
     st = stream_ptr()
+    tiles = (-(-dims // 32)) ** 3
+    tb = torch.zeros(1, dtype=torch.int32, device=dev)
+    L = _lib.load()
+    ws_bytes = L.pyl_ma_batch_tiled_workspace_size(tiles, n) if method == 'tiled' else 1
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev) if method == 'tiled' else None
     times = []
     for r in range(reps + 1):
         g.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        _lib.call('pyl_ma_batch', ptr(rd), 1, ptr(idv), len(items), ptr(cnt), ctas, st)
+        if method == 'tiled':
+            _lib.call('pyl_ma_batch_tiled', ptr(rd), 1, ptr(idv), len(items), ptr(tb), tiles, n, ptr(ws), ws_bytes,
+                      ctas, st)
+        else:
+            _lib.call('pyl_ma_batch', ptr(rd), 1, ptr(idv), len(items), ptr(cnt), ctas, st)
         e1.record()
         torch.cuda.synchronize()
         if r:
@@ -99,8 +109,8 @@ def _time_deposit(dims, n, MAS, interlaced, item, ctas, reps=3):
     return float(np.median(times))
 
 
-def item_size(dims, n, MAS, interlaced, tune=True):
-    key = class_key(dims, n, MAS, interlaced)
+def item_size(dims, n, MAS, interlaced, tune=True, method='atomic'):
+    key = class_key(dims, n, MAS, interlaced, method)
     with _lock:
         c = _load()
         if key in c:
@@ -108,21 +118,23 @@ def item_size(dims, n, MAS, interlaced, tune=True):
         if not tune:
             return DEFAULT_ITEM
         n_probe = min(max(n, 1 << 12), 1 << 22)
-        best = min(ITEM_CANDIDATES, key=lambda it: _time_deposit(dims, n_probe, MAS, interlaced, it, DEFAULT_CTAS))
+        best = min(ITEM_CANDIDATES, key=lambda it: _time_deposit(dims, n_probe, MAS, interlaced, it, DEFAULT_CTAS,
+                                                                 method=method))
         c[key] = int(best)
         _save()
         return int(best)
 
 
-def ctas_per_sm(tune=True):
-    key = '%s/ctas_per_sm' % _device_key()
+def ctas_per_sm(tune=True, method='atomic'):
+    key = '%s/%s/ctas_per_sm' % (_device_key(), method)
     with _lock:
         c = _load()
         if key in c:
             return int(c[key])
         if not tune:
             return DEFAULT_CTAS
-        best = min(CTA_CANDIDATES, key=lambda k: _time_deposit(128, 1 << 22, 'CIC', True, DEFAULT_ITEM, k))
+        cands = CTA_CANDIDATES if method == 'atomic' else (1, 2)     # tiled kernels run 1024 threads per CTA
+        best = min(cands, key=lambda k: _time_deposit(128, 1 << 22, 'CIC', True, DEFAULT_ITEM, k, method=method))
         c[key] = int(best)
         _save()
         return int(best)

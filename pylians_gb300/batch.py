@@ -3,9 +3,12 @@
 A batch holds realizations with uneven particle counts, grid sizes, MAS and
 interlacing.  One step runs:
   * one fill of every grid with -1 per grid-size class (pyl_fill);
-  * ONE persistent deposit launch for all realizations (pyl_ma_batch), fed by a
-    device work list whose item sizes the autotuner picks per
-    (grid, particle count, MAS, interlacing) class;
+  * the deposit of all realizations at once, fed by a device work list whose
+    item sizes the autotuner picks per (grid, particle count, MAS, interlacing)
+    class: method 'tiled' (grids <= 512^3) bins every realization's particles
+    into 32^3-cell bins and deposits all bins in ONE persistent launch
+    (pyl_ma_batch_tiled); method 'atomic' is ONE persistent launch of
+    red.global deposits (pyl_ma_batch);
   * one batched cuFFT R2C per grid-size class;
   * the fused P(k) bin kernel per realization (pyl_pk_bin).
 Everything is stream-ordered, so `capture()` turns a step into one CUDA graph
@@ -29,7 +32,8 @@ ITEM_DT = np.dtype([('first', '<i8'), ('count', '<u4'), ('real', '<u4')])
 class RealizationBatch(object):
     """specs: list of dicts with keys dims, MAS, interlaced, n (particle count)."""
 
-    def __init__(self, specs, BoxSize, axis=0, device=None, tune=True, ctas_per_sm=None, order='size'):
+    def __init__(self, specs, BoxSize, axis=0, device=None, tune=True, ctas_per_sm=None, order='size',
+                 method='auto'):
         require_cuda()
         self.specs = [dict(s) for s in specs]
         self.BoxSize, self.axis = float(BoxSize), int(axis)
@@ -58,12 +62,29 @@ class RealizationBatch(object):
         self.pk_ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.geom = {d: PKL.geometry(d, self.axis, self.device) for d in self.classes}
-        self.item_sizes = [autotune.item_size(int(s['dims']), int(s['n']), s['MAS'], bool(s.get('interlaced')),
-                                              tune=tune) for s in self.specs]
-        self.ctas_per_sm = ctas_per_sm or autotune.ctas_per_sm(tune=tune)
+
         if order not in ('size', 'realization'):
             raise ValueError("order must be 'size' or 'realization'")
         self.order = order
+        if method not in ('auto', 'tiled', 'atomic'):
+            raise ValueError("method must be 'auto', 'tiled' or 'atomic'")
+        fits = all(int(s['dims']) <= 512 for s in self.specs)
+        if method == 'tiled' and not fits:
+            raise ValueError('the tiled batch needs grids of at most 512^3')
+        self.method = 'tiled' if (method == 'auto' and fits) else ('atomic' if method == 'auto' else method)
+        nts = [-(-int(s['dims']) // 32) for s in self.specs]
+        tb = np.concatenate([[0], np.cumsum([t ** 3 for t in nts])]).astype(np.uint32)
+        self.total_tiles = int(tb[-1])
+        self.tile_base = torch.from_numpy(tb[:-1].copy().view(np.int32)).to(self.device)
+        self.total_particles = int(sum(int(s['n']) for s in self.specs))
+        self.bt_ws = None
+        if self.method == 'tiled':
+            nb = L.pyl_ma_batch_tiled_workspace_size(self.total_tiles, self.total_particles)
+            self.bt_ws_bytes = nb
+            self.bt_ws = torch.empty(max(nb, 1), dtype=torch.uint8, device=self.device)
+        self.item_sizes = [autotune.item_size(int(s['dims']), int(s['n']), s['MAS'], bool(s.get('interlaced')),
+                                              tune=tune, method=self.method) for s in self.specs]
+        self.ctas_per_sm = ctas_per_sm or autotune.ctas_per_sm(tune=tune, method=self.method)
         self.reals_dev = None
         self.items_dev = None
         self.graph = None
@@ -106,8 +127,13 @@ class RealizationBatch(object):
         st = stream_ptr(stream)
         for d, g in self.grids.items():
             _lib.call('pyl_fill', ptr(g), g.numel(), -1.0, st)
-        _lib.call('pyl_ma_batch', ptr(self.reals_dev), len(self.specs), ptr(self.items_dev), self.n_items,
-                  ptr(self.counter), self.ctas_per_sm, st)
+        if self.method == 'tiled':
+            _lib.call('pyl_ma_batch_tiled', ptr(self.reals_dev), len(self.specs), ptr(self.items_dev), self.n_items,
+                      ptr(self.tile_base), self.total_tiles, self.total_particles, ptr(self.bt_ws), self.bt_ws_bytes,
+                      self.ctas_per_sm, st)
+        else:
+            _lib.call('pyl_ma_batch', ptr(self.reals_dev), len(self.specs), ptr(self.items_dev), self.n_items,
+                      ptr(self.counter), self.ctas_per_sm, st)
         for d, g in self.grids.items():
             _lib.call('pyl_fft_r2c', ptr(g), ptr(self.dk[d]), d, g.shape[0], st)
         for i, s in enumerate(self.specs):

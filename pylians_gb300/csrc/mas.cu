@@ -30,14 +30,12 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "deposit.cuh"
 #include "sorted.cuh"
 #include "tma.cuh"
 
 namespace pyl {
 namespace {
-
-template <int MAS>
-struct Support { static constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS; };
 
 // Factor applied to every deposited value: 1 for MA(), dims^3 / sum(mass) when
 // the deposit writes the overdensity directly (read from device memory when the
@@ -48,87 +46,6 @@ struct OutScale {
 };
 
 __device__ __forceinline__ float out_scale(const OutScale &s) { return s.dev ? *s.dev : s.host; }
-
-// First cell (unwrapped) of the support of one particle coordinate.  Cell
-// arithmetic is 32-bit (float->int64 conversions run on the slow fp64 pipe):
-// coordinates must satisfy |x * dims / BoxSize| < 2^31; beyond that the
-// conversion saturates and the cell still wraps into the grid.
-template <int MAS>
-__device__ __forceinline__ int axis_first(float p, float inv)
-{
-    const float dist = __fmul_rn(p, inv);
-    if (MAS == PYL_MAS_CIC) return __float2int_rz(dist);
-    const float fl = floorf(dist);
-    const float frac = __fsub_rn(dist, fl);
-    const int fi = __float2int_rz(fl);
-    if (MAS == PYL_MAS_NGP) {
-        int k = fi + (frac >= 0.5f ? 1 : 0);              // floor(dist + 0.5)
-        if (dist < -0.5f && frac != 0.5f) k += 1;         // trunc for negative sums
-        return k;
-    }
-    if (MAS == PYL_MAS_TSC) return fi - 1 + (frac >= 0.5f ? 1 : 0);
-    return fi - 1;                                        // PCS
-}
-
-// Per-axis support of one particle coordinate: first cell f (unwrapped) and the
-// S weights of cells f, f+1, ..., f+S-1.  f equals axis_first<MAS>(p, inv).
-template <int MAS>
-__device__ __forceinline__ int axis_weights(float p, float inv, float *C)
-{
-    const float dist = __fmul_rn(p, inv);
-    if (MAS == PYL_MAS_NGP) {
-        C[0] = 1.0f;
-        return axis_first<MAS>(p, inv);
-    } else if (MAS == PYL_MAS_CIC) {
-        // <int>dist truncates toward zero; u = dist - <int>dist, d = 1 - u
-        const float t = truncf(dist);
-        const float u = __fsub_rn(dist, t);
-        C[0] = __fsub_rn(1.0f, u);
-        C[1] = u;
-        return __float2int_rz(t);
-    } else if (MAS == PYL_MAS_TSC) {
-        const float fl = floorf(dist);
-        const float frac = __fsub_rn(dist, fl);
-        const int mn = __float2int_rz(fl) - 2 + (frac >= 0.5f ? 1 : 0);  // floor(dist - 1.5)
-        const float fmn = __fsub_rn(__fadd_rn(fl, frac >= 0.5f ? 1.0f : 0.0f), 2.0f);
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            const float diff = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
-            float c;
-            if (diff < 0.5f) {
-                c = __fsub_rn(0.75f, __fmul_rn(diff, diff));
-            } else if (diff < 1.5f) {
-                const float t = __fsub_rn(1.5f, diff);
-                c = __fmul_rn(__fmul_rn(0.5f, t), t);
-            } else {
-                c = 0.0f;
-            }
-            C[j] = c;
-        }
-        return mn + 1;
-    } else {  // PCS
-        const float fl = floorf(dist);
-        const int mn = __float2int_rz(fl) - 2;            // floor(dist - 2)
-        const float fmn = __fsub_rn(fl, 2.0f);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const float d = fabsf(__fsub_rn(__fadd_rn(fmn, (float)(j + 1)), dist));
-            float c;
-            if (d < 1.0f) {
-                const float a = __fmul_rn(__fmul_rn(6.0f, d), d);
-                const float b = __fmul_rn(__fmul_rn(__fmul_rn(3.0f, d), d), d);
-                c = __fdiv_rn(__fadd_rn(__fsub_rn(4.0f, a), b), 6.0f);
-            } else if (d < 2.0f) {
-                const float t = __fsub_rn(2.0f, d);
-                c = __fdiv_rn(__fmul_rn(__fmul_rn(t, t), t), 6.0f);
-            } else {
-                c = 0.0f;
-            }
-            C[j] = c;
-        }
-        return mn + 1;
-    }
-}
 
 // ------------------------------------------------------------------ ATOMIC path
 template <int MAS, int NDIM, bool WEIGHTED, bool INTERLACED>
@@ -203,9 +120,8 @@ __global__ void __launch_bounds__(256) ma_atomic_kernel(
 // global atomics instead (the same tile layout).  Then one CTA per tile deposits
 // into a (TB+H)^3 shared-memory block (H = kernel support - 1, +1 for the
 // interlaced shift) and adds it to the grid with coalesced red.global.add.
-constexpr int TB = 32;
 constexpr int HIST_MAX_TILES = 49152;
-constexpr int MAX_CHUNKS = 256;
+constexpr int MAX_CHUNKS = 512;
 
 struct TileGeom {
     int dims, nt, nc;      // grid side, tiles per axis, coarse blocks (4^3 tiles) per axis
@@ -508,8 +424,10 @@ __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *__res
 
 inline size_t hist_tma_smem(long long ntiles) { return (size_t)2 * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
 
+constexpr int LAT_U = 2, LAT_BATCH = LA_THREADS * LAT_U;     // 2048 particles: two CTAs per SM
+
 template <int MAS, bool WEIGHTED>
-__global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
+__global__ void __launch_bounds__(LA_THREADS, 2) level_a_tma_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
     TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
     float4 *__restrict__ tmp)
@@ -519,10 +437,10 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     __shared__ int s_ok;
     const int NCO = g.nc * g.nc * g.nc;
     const int T = (int)g.ntiles;
-    float *inb = (float *)araw;                                            // [2][LA_BATCH * 3]
-    float4 *stage = (float4 *)(araw + 2 * LA_BATCH * 12);
-    unsigned short *sco = (unsigned short *)(stage + LA_BATCH);
-    unsigned *cur = (unsigned *)(sco + LA_BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
+    float *inb = (float *)araw;                                            // [2][LAT_BATCH * 3]
+    float4 *stage = (float4 *)(araw + 2 * LAT_BATCH * 12);
+    unsigned short *sco = (unsigned short *)(stage + LAT_BATCH);
+    unsigned *cur = (unsigned *)(sco + LAT_BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
     const unsigned *row = colpre + (long long)blockIdx.x * T;
     for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
         unsigned sacc = 0;
@@ -530,7 +448,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         cur[co] = offsets[co * 64] + sacc;
     }
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
-    const long long nbat = e > b ? (e - b + LA_BATCH - 1) / LA_BATCH : 0;
+    const long long nbat = e > b ? (e - b + LAT_BATCH - 1) / LAT_BATCH : 0;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -539,15 +457,15 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     __syncthreads();
     if (threadIdx.x == 0)
         for (long long j = 0; j < 2 && j < nbat; j++) {
-            const long long s0 = b + j * LA_BATCH;
-            stage_copy(inb + (j & 1) * LA_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)LA_BATCH, e - s0)),
+            const long long s0 = b + j * LAT_BATCH;
+            stage_copy(inb + (j & 1) * LAT_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)LAT_BATCH, e - s0)),
                        &bar[j & 1]);
         }
     for (long long j = 0; j < nbat; j++) {
-        const long long s0 = b + j * LA_BATCH;
-        const int c = (int)min((long long)LA_BATCH, e - s0);
+        const long long s0 = b + j * LAT_BATCH;
+        const int c = (int)min((long long)LAT_BATCH, e - s0);
         const int full = staged_full(c);
-        const float *in = inb + (j & 1) * LA_BATCH * 3;
+        const float *in = inb + (j & 1) * LAT_BATCH * 3;
         if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (unsigned)((j >> 1) & 1), &g_tma_error);
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) bcnt[co] = 0u;
         __syncthreads();
@@ -556,10 +474,10 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
                 mbar_wait_bounded(&bar[(j + 1) & 1], (unsigned)(((j + 1) >> 1) & 1), &g_tma_error);
             return;
         }
-        float4 r[LA_U];
-        unsigned co_u[LA_U], rank[LA_U];
+        float4 r[LAT_U];
+        unsigned co_u[LAT_U], rank[LAT_U];
 #pragma unroll
-        for (int u = 0; u < LA_U; u++) {
+        for (int u = 0; u < LAT_U; u++) {
             const int i = threadIdx.x + u * LA_THREADS;
             co_u[u] = 0xffffffffu;
             if (i < c) {
@@ -576,8 +494,8 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         }
         __syncthreads();
         if (threadIdx.x == 0 && j + 2 < nbat) {                  // this buffer is consumed
-            const long long s2 = b + (j + 2) * LA_BATCH;
-            stage_copy(inb + (j & 1) * LA_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LA_BATCH, e - s2)),
+            const long long s2 = b + (j + 2) * LAT_BATCH;
+            stage_copy(inb + (j & 1) * LAT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LAT_BATCH, e - s2)),
                        &bar[j & 1]);
         }
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
@@ -587,7 +505,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         __syncthreads();
         block_exclusive_scan(bcnt, NCO, wt);
 #pragma unroll
-        for (int u = 0; u < LA_U; u++) {
+        for (int u = 0; u < LAT_U; u++) {
             if (co_u[u] != 0xffffffffu) {
                 const unsigned slot = bcnt[co_u[u]] + rank[u];
                 stage[slot] = r[u];
@@ -606,7 +524,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
 
 inline size_t level_a_tma_smem(int nco)
 {
-    return (size_t)2 * LA_BATCH * 12 + sizeof(float4) * LA_BATCH + sizeof(unsigned short) * LA_BATCH +
+    return (size_t)2 * LAT_BATCH * 12 + sizeof(float4) * LAT_BATCH + sizeof(unsigned short) * LAT_BATCH +
            sizeof(unsigned) * (3 * nco + 32);
 }
 
@@ -949,8 +867,9 @@ TiledWs tiled_layout(void *base, long long n, int dims)
     TiledWs ws;
     ws.n = (unsigned)n;
     ws.smem_hist = g.ntiles <= HIST_MAX_TILES;
-    ws.chunks = num_sms() < MAX_CHUNKS ? num_sms() : MAX_CHUNKS;
-    const size_t hist_len = ws.smem_hist ? (size_t)MAX_CHUNKS * g.ntiles : (size_t)g.ntiles;
+    // two chunks per SM: the staged level-A kernel runs two CTAs per SM
+    ws.chunks = 2 * num_sms() < MAX_CHUNKS ? 2 * num_sms() : MAX_CHUNKS;
+    const size_t hist_len = ws.smem_hist ? (size_t)ws.chunks * g.ntiles : (size_t)g.ntiles;
     size_t off = 0;
     char *b = (char *)base;
     ws.hist = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * hist_len, 256);
@@ -978,98 +897,6 @@ TiledWs tiled_layout(void *base, long long n, int dims)
 // flag, and the pass is redone with float32 shared atomics.  The grids (plain,
 // then interlaced) are deposited one after the other; the second pass reads the
 // bin's particles again from L2.
-template <int MAS, bool INTER>
-struct FxShape {
-    static constexpr int H = Support<MAS>::S - 1 + (INTER ? 1 : 0);
-    static constexpr int E = TB + H;
-    static constexpr int CELLS = E * E * E;
-    static constexpr size_t SMEM = sizeof(unsigned) * ((CELLS + 3) / 4 * 4);
-    static constexpr bool FITS = SMEM <= 227 * 1024;
-};
-
-constexpr float FX_MAGIC = 12582912.0f;        // 1.5 * 2^23
-constexpr unsigned FX_MAGIC_BITS = 0x4B400000u;
-constexpr float FX_SCALE = 4194304.0f;         // 2^22
-constexpr float FX_INV = 2.384185791015625e-07f;
-
-// Weights and bin-local first cell (base, row-major over E^3) of one particle
-// for the plain (G=0) or the half-cell-shifted (G=1) grid.
-template <int MAS, int G, int E>
-__device__ __forceinline__ int fx_support(const float4 &r, float inv, float halfcell, int dims, const int *o,
-                                          float (*C)[Support<MAS>::S])
-{
-    const float p[3] = {r.x, r.y, r.z};
-    int base = 0;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        int loc;
-        if (G == 1) {
-            const int f0 = axis_first<MAS>(p[a], inv);
-            const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
-            loc = wrap_index(f0, dims) - o[a] + (f > f0 ? 1 : 0);
-        } else {
-            loc = wrap_index(axis_weights<MAS>(p[a], inv, C[a]), dims) - o[a];
-        }
-        base = base * E + loc;
-    }
-    return base;
-}
-
-// All weights non-negative and not NaN (CIC: u >= 0; TSC/PCS weights are >= 0
-// for finite positions by construction).
-template <int MAS>
-__device__ __forceinline__ bool fx_weights_ok(const float (*C)[Support<MAS>::S])
-{
-    if (MAS == PYL_MAS_NGP) return true;
-    bool ok = true;
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int j = 0; j < Support<MAS>::S; j++) ok = ok && C[a][j] >= 0.0f;
-    return ok;
-}
-
-template <int MAS, int E>
-__device__ __forceinline__ unsigned fx_scatter(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
-{
-    constexpr int S = Support<MAS>::S;
-    if (MAS == PYL_MAS_NGP) {
-        atomicAdd(acc + base, 1u);       // a bin holds < 2^32 particles: no wrap
-        return 0u;
-    }
-    unsigned wrapped = 0u;
-#pragma unroll
-    for (int l = 0; l < S; l++)
-#pragma unroll
-        for (int m = 0; m < S; m++) {
-            const float c01 = __fmul_rn(C[0][l], C[1][m]);
-            const int row = base + (l * E + m) * E;
-#pragma unroll
-            for (int q = 0; q < S; q++) {
-                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
-                const unsigned qv = __float_as_uint(x) - FX_MAGIC_BITS;
-                const unsigned old = atomicAdd(acc + row + q, qv);
-                wrapped |= (unsigned)(old + qv < old);
-            }
-        }
-    return wrapped;
-}
-
-template <int MAS, int E>
-__device__ __forceinline__ void float_scatter(float *acc, int base, const float (*C)[Support<MAS>::S])
-{
-    constexpr int S = Support<MAS>::S;
-#pragma unroll
-    for (int l = 0; l < S; l++)
-#pragma unroll
-        for (int m = 0; m < S; m++) {
-            const float c01 = __fmul_rn(C[0][l], C[1][m]);
-            const int row = base + (l * E + m) * E;
-#pragma unroll
-            for (int q = 0; q < S; q++) atomicAdd(acc + row + q, __fmul_rn(c01, C[2][q]));
-        }
-}
-
 template <int MAS, bool INTER>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
@@ -1158,30 +985,6 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
 //     32-bit cell offsets.
 // Only CIC can produce negative or NaN weights (positions below 0, non-finite
 // positions); TSC and PCS weights are in [0, 1] for any input.
-template <int MAS, int E>
-__device__ __forceinline__ unsigned fx_scatter_or(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
-{
-    constexpr int S = Support<MAS>::S;
-    if (MAS == PYL_MAS_NGP) {
-        atomicAdd(acc + base, 1u);
-        return 0u;
-    }
-    unsigned seen = 0u;
-#pragma unroll
-    for (int l = 0; l < S; l++)
-#pragma unroll
-        for (int m = 0; m < S; m++) {
-            const float c01 = __fmul_rn(C[0][l], C[1][m]);
-            const int row = base + (l * E + m) * E;
-#pragma unroll
-            for (int q = 0; q < S; q++) {
-                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
-                seen |= atomicAdd(acc + row + q, __float_as_uint(x) - FX_MAGIC_BITS);
-            }
-        }
-    return seen;
-}
-
 template <int MAS, bool INTER, int R>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,

@@ -175,7 +175,28 @@ def make_interp_rsd(MASL, RSL):
     return out
 
 
-def main(which=('ma', 'pk', 'bk', 'interp')):
+def make_xi(MASL, PKL):
+    """Pk_library.Xi and correct_MAS (Pk_library.pyx:1749-1806, 2035-2150) on a 32^3
+    CIC overdensity of 1000 Mpc/h, and on a 15^3 one (odd grid)."""
+    out = {}
+    rng = np.random.default_rng(41)
+    L = 1000.0
+    for N in (32, 15):
+        pos = (rng.random((N ** 3 * 2, 3)) * L).astype(np.float32)
+        d = cic_overdensity(MASL, pos, N, L)
+        out['delta_%d' % N] = d
+        for axis in (0, 2):
+            with quiet():
+                X = PKL.Xi(d, L, 'CIC', axis, 1)
+            out['Xi_%d_axis%d_r3D' % (N, axis)] = np.asarray(X.r3D)
+            out['Xi_%d_axis%d_xi' % (N, axis)] = np.asarray(X.xi)
+            out['Xi_%d_axis%d_Nmodes3D' % (N, axis)] = np.asarray(X.Nmodes3D)
+        with quiet():
+            out['correct_MAS_%d' % N] = np.asarray(PKL.correct_MAS(d, L, 'CIC', 1))
+    return out
+
+
+def main(which=('ma', 'pk', 'bk', 'interp', 'xi')):
     if not build_ref.built():
         build_ref.build()
     MASL, PKL, BKL = build_ref.load_reference()
@@ -185,6 +206,8 @@ def main(which=('ma', 'pk', 'bk', 'interp')):
         np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
     if 'bk' in which:
         np.savez_compressed(os.path.join(HERE, 'bk_golden.npz'), **make_bk(MASL, BKL))
+    if 'xi' in which:
+        np.savez_compressed(os.path.join(HERE, 'xi_golden.npz'), **make_xi(MASL, PKL))
     if 'interp' in which:
         RSL = build_ref.load_redshift_space()
         np.savez_compressed(os.path.join(HERE, 'interp_golden.npz'), **make_interp_rsd(MASL, RSL))
@@ -194,4 +217,4 @@ def main(which=('ma', 'pk', 'bk', 'interp')):
 
 
 if __name__ == '__main__':
-    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp'))
+    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi'))

