@@ -250,6 +250,18 @@ int pyl_mlp_backward(const void *params_bf16, const float *x, const float *act, 
 int pyl_mlp_adam(float *master, void *params_bf16, const float *grad, float *m, float *v, int n, float lr,
                  float beta1, float beta2, float eps, int step, void *stream);
 
+/* ---- 2D fields (Pk_library.Pk_plane / XPk_plane, Pk_library.pyx:440-516, 814-941) ----
+ * pyl_fft2_r2c: unnormalised R2C of `batch` contiguous dims^2 float32 maps into
+ * [dims][dims/2+1] complex64 each (FFT2Dr_f).  pyl_pk_plane_bin: float64 sums
+ * over the independent modes of one or two transformed maps (dk2 NULL for one):
+ * K[nb] (sum |k|) | N[nb] | P1[nb] | P2[nb] | PX[nb] (Re d1 d2*), each field
+ * multiplied by its MAS factor (exponent mas_p1 / mas_p2), nb =
+ * pyl_pk_plane_bins(dims) = int(sqrt(2) dims/2) + 1. */
+int pyl_fft2_r2c(const float *in, void *out_c64, int dims, int batch, void *stream);
+int pyl_pk_plane_bins(int dims);
+int pyl_pk_plane_bin(const void *dk1, const void *dk2, int dims, int mas_p1, int mas_p2, double *sums,
+                     void *stream);
+
 /* ---- correlation function (Pk_library.Xi, library/Pk_library/Pk_library.pyx:2035-2150) ----
  * pyl_xi_power: in place over an R2C output, every stored mode becomes
  * (|delta_k * W^-1|^2, 0) with the MAS factor of exponent mas_p rounded to float

@@ -449,3 +449,63 @@ def Xi(delta, BoxSize, MAS='CIC', axis=2, threads=1):
     r.Nmodes3D = N1
     r.xi = np.stack([X0[1:] / N1, X2[1:] * 5.0 / N1, X4[1:] * 9.0 / N1], axis=1) / float(dims) ** 3
     return r
+
+
+# ------------------------------------------------------------------- 2D maps
+def _plane(maps, BoxSize, mas_list):
+    """Sums of Pk_plane / XPk_plane (Pk_library.pyx:440-516, 814-941) with numpy."""
+    import scipy.fft
+    dims = maps[0].shape[0]
+    middle = dims // 2
+    f, fy = _freqs(dims), np.arange(dims // 2 + 1)
+    kx, ky = np.meshgrid(f, fy, indexing='ij')
+    even = dims % 2 == 0
+    keep = ~(((ky == 0) | ((ky == middle) & even)) & (kx < 0))
+    n2 = kx * kx + ky * ky
+    k = np.sqrt(n2.astype(np.float64))
+    idx = np.floor(k + 1e-9).astype(np.int64)
+    idx = np.where(idx * idx > n2, idx - 1, idx)
+    nb = int(np.sqrt(middle ** 2 + middle ** 2)) + 1
+    dks = []
+    for m, mas in zip(maps, mas_list):
+        dk = scipy.fft.rfftn(np.asarray(m, np.float32))
+        p = MAS_function(mas)
+        def c(q):
+            x = np.pi * q / dims
+            with np.errstate(invalid='ignore', divide='ignore'):
+                r = np.where(q == 0, 1.0, x / np.sin(np.where(q == 0, 1.0, x)))
+            return r ** p if p else np.ones_like(x, dtype=np.float64)
+        fac = (c(f)[:, None] * c(fy)[None, :]).astype(np.float32)
+        dks.append((dk * fac).astype(np.complex64))
+    i = idx[keep]
+    K = np.bincount(i, k[keep], nb)
+    N = np.bincount(i, None, nb).astype(np.float64)
+    P = [np.bincount(i, (d.real.astype(np.float64) ** 2 + d.imag.astype(np.float64) ** 2)[keep], nb) for d in dks]
+    X = None
+    if len(dks) > 1:
+        a, b = dks
+        X = np.bincount(i, (a.real.astype(np.float64) * b.real + a.imag.astype(np.float64) * b.imag)[keep], nb)
+    return dims, K, N, P, X
+
+
+def Pk_plane(delta, BoxSize, MAS='CIC', threads=1):
+    dims, K, N, P, _ = _plane([delta], BoxSize, [MAS])
+    kF = 2.0 * np.pi / BoxSize
+    r = _Result()
+    r.k = K[1:] / N[1:] * kF
+    r.Nmodes = N[1:]
+    r.Pk = P[0][1:] / N[1:] * (BoxSize / dims ** 2) ** 2
+    return r
+
+
+def XPk_plane(delta1, delta2, BoxSize, MAS1=None, MAS2=None, threads=1):
+    dims, K, N, P, X = _plane([delta1, delta2], BoxSize, [MAS1, MAS2])
+    kF = 2.0 * np.pi / BoxSize
+    fact = (BoxSize / dims ** 2) ** 3
+    r = _Result()
+    r.k = K[1:] / N[1:] * kF
+    r.Nmodes = N[1:]
+    r.Pk = np.stack([P[0][1:] / N[1:] * fact, P[1][1:] / N[1:] * fact], axis=1)
+    r.XPk = X[1:] / N[1:] * fact
+    r.r = r.XPk / np.sqrt(r.Pk[:, 0] * r.Pk[:, 1])
+    return r

@@ -29,8 +29,8 @@ from . import _lib
 from ._device import as_device_c64, as_device_f32, is_torch, ptr, require_cuda, stream_ptr, workspace
 
 __all__ = ['frequencies', 'MAS_function', 'check_number_modes', 'FFT3Dr_f', 'IFFT3Dr_f',
-           'Pk', 'XPk', 'Bk', 'Bk_triangles', 'Xi', 'correct_MAS', 'pk_sums_device', 'finalize_pk',
-           'geometry']
+           'Pk', 'XPk', 'Bk', 'Bk_triangles', 'Xi', 'correct_MAS', 'Pk_plane', 'XPk_plane',
+           'frequencies_2D', 'check_number_modes_2D', 'FFT2Dr_f', 'pk_sums_device', 'finalize_pk', 'geometry']
 
 
 def frequencies(BoxSize, dims):
@@ -226,6 +226,89 @@ class Pk(object):
             self.delta_k = dk[0] if is_torch(delta) else dk[0].cpu().numpy()
         if verbose:
             print('Time taken = %.2f seconds' % (time.time() - start))
+
+
+# ------------------------------------------------------------------- 2D fields
+def frequencies_2D(BoxSize, dims):
+    """Pk_library.frequencies_2D (Pk_library.pyx:67-72)."""
+    kF = 2.0 * np.pi / BoxSize
+    middle = dims // 2
+    kN = middle * kF
+    return kF, kN, middle, middle, int(np.sqrt(middle ** 2 + middle ** 2))
+
+
+def check_number_modes_2D(Nmodes, dims):
+    """Pk_library.check_number_modes_2D (:105-117); raises instead of exiting."""
+    own = 1 if dims % 2 == 1 else 4
+    indep = (dims ** 2 - own) // 2 + own
+    if int(np.sum(Nmodes)) != indep:
+        raise ValueError('Not all modes counted: counted %d independent modes, expected %d'
+                         % (int(np.sum(Nmodes)), indep))
+
+
+def FFT2Dr_f(a, threads=1):
+    """Unnormalised float32 R2C of a (dims, dims) map (Pk_library FFT2Dr_f)."""
+    require_cuda()
+    x = as_device_f32(a, 'a')
+    dims = x.shape[0]
+    out = torch.empty((dims, dims // 2 + 1), dtype=torch.complex64, device=x.device)
+    _lib.call('pyl_fft2_r2c', ptr(x), ptr(out), dims, 1, stream_ptr())
+    return out if is_torch(a) else out.cpu().numpy()
+
+
+def _plane_sums(maps, mas):
+    xs = [as_device_f32(m, 'delta') for m in maps]
+    dims = xs[0].shape[0]
+    for x in xs:
+        if x.dim() != 2 or tuple(x.shape) != (dims, dims):
+            raise ValueError('maps must be square (dims, dims) float32 arrays of one size')
+    dks = []
+    for x in xs:
+        dk = torch.empty((dims, dims // 2 + 1), dtype=torch.complex64, device=x.device)
+        _lib.call('pyl_fft2_r2c', ptr(x), ptr(dk), dims, 1, stream_ptr())
+        dks.append(dk)
+    nb = _lib.load().pyl_pk_plane_bins(dims)
+    sums = torch.empty(5 * nb, dtype=torch.float64, device=xs[0].device)
+    _lib.call('pyl_pk_plane_bin', ptr(dks[0]), ptr(dks[1]) if len(dks) > 1 else None, dims,
+              MAS_function(mas[0]), MAS_function(mas[1]) if len(mas) > 1 else 0, ptr(sums), stream_ptr())
+    s = sums.cpu().numpy().reshape(5, nb)
+    return dims, s
+
+
+class Pk_plane(object):
+    """Pk_library.Pk_plane (Pk_library.pyx:440-516): P(k) of a 2D map; attributes k,
+    Nmodes, Pk (DC bin dropped)."""
+
+    def __init__(self, delta, BoxSize, MAS='CIC', threads=1):
+        require_cuda()
+        dims, s = _plane_sums([delta], [MAS])
+        kF = frequencies_2D(BoxSize, dims)[0]
+        check_number_modes_2D(s[1], dims)
+        N = s[1][1:]
+        self.k = s[0][1:] / N * kF
+        self.Nmodes = N
+        self.Pk = s[2][1:] / N * (BoxSize / dims ** 2) ** 2
+
+
+class XPk_plane(object):
+    """Pk_library.XPk_plane (Pk_library.pyx:814-941): auto and cross P(k) of two 2D
+    maps; attributes k, Nmodes, Pk [bins, 2], XPk, r = XPk / sqrt(Pk1 Pk2).  As in the
+    reference, spectra are scaled by (BoxSize/dims^2)^3 and the size check compares
+    delta1.shape[0] with delta2.shape[1]."""
+
+    def __init__(self, delta1, delta2, BoxSize, MAS1=None, MAS2=None, threads=1):
+        require_cuda()
+        if delta1.shape[0] != delta2.shape[1]:
+            raise ValueError('Images have different grid sizes!!!')
+        dims, s = _plane_sums([delta1, delta2], [MAS1, MAS2])
+        kF = frequencies_2D(BoxSize, dims)[0]
+        fact = (BoxSize / dims ** 2) ** 3
+        N = s[1][1:]
+        self.k = s[0][1:] / N * kF
+        self.Nmodes = N
+        self.Pk = np.stack([s[2][1:] / N * fact, s[3][1:] / N * fact], axis=1)
+        self.XPk = s[4][1:] / N * fact
+        self.r = self.XPk / np.sqrt(self.Pk[:, 0] * self.Pk[:, 1])
 
 
 def correct_MAS(delta, BoxSize, MAS='CIC', threads=1):

@@ -52,6 +52,9 @@ SIGNATURES = {
     'pyl_mlp_forward': (_I, [_P, _P, _I, _P, _P, _P]),
     'pyl_mlp_backward': (_I, [_P, _P, _P, _P, _P, _P, _F, _I, _P, _P, _P, _P]),
     'pyl_mlp_adam': (_I, [_P, _P, _P, _P, _P, _I, _F, _F, _F, _F, _I, _P]),
+    'pyl_fft2_r2c': (_I, [_P, _P, _I, _I, _P]),
+    'pyl_pk_plane_bins': (_I, [_I]),
+    'pyl_pk_plane_bin': (_I, [_P, _P, _I, _I, _I, _P, _P]),
     'pyl_correct_mas': (_I, [_P, _I, _I, _P]),
     'pyl_xi_sums_len': (_I64, [_I]),
     'pyl_xi_power': (_I, [_P, _I, _I, _P]),

@@ -15,10 +15,10 @@ namespace pyl {
 namespace {
 
 struct PlanKey {
-    int device, dims, batch, dir;
+    int device, dims, batch, dir, rank;
     bool operator<(const PlanKey &o) const
     {
-        return std::tie(device, dims, batch, dir) < std::tie(o.device, o.dims, o.batch, o.dir);
+        return std::tie(device, dims, batch, dir, rank) < std::tie(o.device, o.dims, o.batch, o.dir, o.rank);
     }
 };
 
@@ -49,25 +49,26 @@ const char *cufft_name(cufftResult r)
         }                                                                               \
     } while (0)
 
-// Returns a plan for `batch` contiguous dims^3 transforms (caller holds g_mu).
-int get_plan(int dims, int batch, int dir, cufftHandle *out)
+// Returns a plan for `batch` contiguous dims^rank transforms, rank 2 or 3
+// (caller holds g_mu).
+int get_plan(int dims, int batch, int dir, cufftHandle *out, int rank = 3)
 {
     int dev = 0;
     PYL_CUDA(cudaGetDevice(&dev));
-    PlanKey k{dev, dims, batch, dir};
+    PlanKey k{dev, dims, batch, dir, rank};
     auto it = g_plans.find(k);
     if (it != g_plans.end()) { *out = it->second; return PYL_OK; }
     cufftHandle h;
     PYL_CUFFT(cufftCreate(&h));
     long long n[3] = {dims, dims, dims};
-    const long long real_dist = (long long)dims * dims * dims;
-    const long long cplx_dist = (long long)dims * dims * (dims / 2 + 1);
+    const long long real_dist = rank == 3 ? (long long)dims * dims * dims : (long long)dims * dims;
+    const long long cplx_dist = (rank == 3 ? (long long)dims * dims : (long long)dims) * (dims / 2 + 1);
     size_t ws = 0;
     cufftResult r;
     if (dir == CUFFT_R2C)
-        r = cufftMakePlanMany64(h, 3, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, CUFFT_R2C, batch, &ws);
+        r = cufftMakePlanMany64(h, rank, n, nullptr, 1, real_dist, nullptr, 1, cplx_dist, CUFFT_R2C, batch, &ws);
     else
-        r = cufftMakePlanMany64(h, 3, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, CUFFT_C2R, batch, &ws);
+        r = cufftMakePlanMany64(h, rank, n, nullptr, 1, cplx_dist, nullptr, 1, real_dist, CUFFT_C2R, batch, &ws);
     if (r != CUFFT_SUCCESS) {
         cufftDestroy(h);
         set_error(std::string("cufftMakePlanMany64 -> ") + cufft_name(r));
@@ -83,16 +84,29 @@ int get_plan(int dims, int batch, int dir, cufftHandle *out)
 
 using namespace pyl;
 
+// At 1024^3 and above, cuFFT runs a batch of R2C transforms as one batch-1
+// transform after another faster than as one batched plan (10.8 ms vs 13.3 ms for
+// two 1024^3 grids on GB300), so large batches are split.
+constexpr int SPLIT_BATCH_DIMS = 1024;
+
 extern "C" int pyl_fft_r2c(const float *in, void *out_c64, int dims, int batch, void *stream)
 {
     PYL_CHECK_ARG(in != nullptr && out_c64 != nullptr, "null pointer");
     PYL_CHECK_ARG(dims >= 2 && batch >= 1, "bad size");
     std::lock_guard<std::mutex> lk(g_mu);
     cufftHandle h;
-    int rc = get_plan(dims, batch, CUFFT_R2C, &h);
+    const bool split = batch > 1 && dims >= SPLIT_BATCH_DIMS;
+    int rc = get_plan(dims, split ? 1 : batch, CUFFT_R2C, &h);
     if (rc) return rc;
     PYL_CUFFT(cufftSetStream(h, (cudaStream_t)stream));
-    PYL_CUFFT(cufftExecR2C(h, (cufftReal *)in, (cufftComplex *)out_c64));
+    if (!split) {
+        PYL_CUFFT(cufftExecR2C(h, (cufftReal *)in, (cufftComplex *)out_c64));
+        return PYL_OK;
+    }
+    const long long real_dist = (long long)dims * dims * dims;
+    const long long cplx_dist = (long long)dims * dims * (dims / 2 + 1);
+    for (int b = 0; b < batch; b++)
+        PYL_CUFFT(cufftExecR2C(h, (cufftReal *)(in + b * real_dist), (cufftComplex *)out_c64 + b * cplx_dist));
     return PYL_OK;
 }
 
@@ -106,6 +120,19 @@ extern "C" int pyl_fft_c2r(void *in_c64, float *out, int dims, int batch, void *
     if (rc) return rc;
     PYL_CUFFT(cufftSetStream(h, (cudaStream_t)stream));
     PYL_CUFFT(cufftExecC2R(h, (cufftComplex *)in_c64, (cufftReal *)out));
+    return PYL_OK;
+}
+
+extern "C" int pyl_fft2_r2c(const float *in, void *out_c64, int dims, int batch, void *stream)
+{
+    PYL_CHECK_ARG(in != nullptr && out_c64 != nullptr, "null pointer");
+    PYL_CHECK_ARG(dims >= 2 && batch >= 1, "bad size");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cufftHandle h;
+    int rc = get_plan(dims, batch, CUFFT_R2C, &h, 2);
+    if (rc) return rc;
+    PYL_CUFFT(cufftSetStream(h, (cudaStream_t)stream));
+    PYL_CUFFT(cufftExecR2C(h, (cufftReal *)in, (cufftComplex *)out_c64));
     return PYL_OK;
 }
 

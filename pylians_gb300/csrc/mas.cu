@@ -424,10 +424,10 @@ __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *__res
 
 inline size_t hist_tma_smem(long long ntiles) { return (size_t)2 * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
 
-constexpr int LAT_U = 2, LAT_BATCH = LA_THREADS * LAT_U;     // 2048 particles: two CTAs per SM
+constexpr int LAT_U = 4, LAT_BATCH = LA_THREADS * LAT_U;     // 4096 particles per batch
 
 template <int MAS, bool WEIGHTED>
-__global__ void __launch_bounds__(LA_THREADS, 2) level_a_tma_kernel(
+__global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
     TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
     float4 *__restrict__ tmp)
@@ -867,8 +867,7 @@ TiledWs tiled_layout(void *base, long long n, int dims)
     TiledWs ws;
     ws.n = (unsigned)n;
     ws.smem_hist = g.ntiles <= HIST_MAX_TILES;
-    // two chunks per SM: the staged level-A kernel runs two CTAs per SM
-    ws.chunks = 2 * num_sms() < MAX_CHUNKS ? 2 * num_sms() : MAX_CHUNKS;
+    ws.chunks = num_sms() < MAX_CHUNKS ? num_sms() : MAX_CHUNKS;
     const size_t hist_len = ws.smem_hist ? (size_t)ws.chunks * g.ntiles : (size_t)g.ntiles;
     size_t off = 0;
     char *b = (char *)base;

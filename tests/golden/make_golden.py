@@ -196,7 +196,30 @@ def make_xi(MASL, PKL):
     return out
 
 
-def main(which=('ma', 'pk', 'bk', 'interp', 'xi')):
+def make_plane(MASL, PKL):
+    """Pk_library.Pk_plane / XPk_plane (Pk_library.pyx:440-516, 814-941) on 2D CIC
+    maps of 64^2 and 45^2 cells (1000 Mpc/h)."""
+    out = {}
+    rng = np.random.default_rng(51)
+    L = 1000.0
+    for N in (64, 45):
+        pos = (rng.random((N * N * 4, 2)) * L).astype(np.float32)
+        a = np.zeros((N, N), np.float32)
+        MASL.MA(pos, a, L, 'CIC')
+        a /= np.mean(a, dtype=np.float64); a -= 1.0
+        b = (0.7 * a + 0.3 * np.roll(a, 2, axis=0)).astype(np.float32)
+        out['map1_%d' % N], out['map2_%d' % N] = a, b
+        with quiet():
+            P = PKL.Pk_plane(a, L, 'CIC', 1)
+            X = PKL.XPk_plane(a, b, L, 'CIC', 'TSC', 1)
+        for n in ('k', 'Nmodes', 'Pk'):
+            out['Pkplane_%d_%s' % (N, n)] = np.asarray(getattr(P, n))
+        for n in ('k', 'Nmodes', 'Pk', 'XPk', 'r'):
+            out['XPkplane_%d_%s' % (N, n)] = np.asarray(getattr(X, n))
+    return out
+
+
+def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane')):
     if not build_ref.built():
         build_ref.build()
     MASL, PKL, BKL = build_ref.load_reference()
@@ -206,6 +229,8 @@ def main(which=('ma', 'pk', 'bk', 'interp', 'xi')):
         np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
     if 'bk' in which:
         np.savez_compressed(os.path.join(HERE, 'bk_golden.npz'), **make_bk(MASL, BKL))
+    if 'plane' in which:
+        np.savez_compressed(os.path.join(HERE, 'plane_golden.npz'), **make_plane(MASL, PKL))
     if 'xi' in which:
         np.savez_compressed(os.path.join(HERE, 'xi_golden.npz'), **make_xi(MASL, PKL))
     if 'interp' in which:
@@ -217,4 +242,4 @@ def main(which=('ma', 'pk', 'bk', 'interp', 'xi')):
 
 
 if __name__ == '__main__':
-    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi'))
+    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi', 'plane'))

@@ -207,3 +207,19 @@ def test_oracle_correct_mas_golden(xg, N):
     """The same float operations and the same (scipy) inverse transform as the
     reference run under the pyFFTW stand-in: bit-exact."""
     np.testing.assert_array_equal(O.correct_MAS(xg['delta_%d' % N], 1000.0, 'CIC'), xg['correct_MAS_%d' % N])
+
+
+@pytest.fixture(scope='module')
+def pg():
+    return np.load(os.path.join(GOLDEN, 'plane_golden.npz'))
+
+
+@pytest.mark.parametrize('N', [64, 45])
+def test_oracle_plane_golden(pg, N):
+    a, b = pg['map1_%d' % N], pg['map2_%d' % N]
+    r = O.Pk_plane(a, 1000.0, 'CIC')
+    np.testing.assert_array_equal(r.Nmodes, pg['Pkplane_%d_Nmodes' % N])
+    np.testing.assert_allclose(r.Pk, pg['Pkplane_%d_Pk' % N], rtol=1e-12)
+    x = O.XPk_plane(a, b, 1000.0, 'CIC', 'TSC')
+    for n in ('k', 'Pk', 'XPk', 'r'):
+        np.testing.assert_allclose(getattr(x, n), pg['XPkplane_%d_%s' % (N, n)], rtol=1e-12)
