@@ -262,6 +262,15 @@ int pyl_pk_plane_bins(int dims);
 int pyl_pk_plane_bin(const void *dk1, const void *dk2, int dims, int mas_p1, int mas_p2, double *sums,
                      void *stream);
 
+/* ---- smoothing (smoothing_library.pyx:20-123) ---------------------------------
+ * pyl_filter_grid replaces the real-space part of FT_filter: field [dims]^3 gets
+ * the Top-Hat (gaussian = 0: 1 where d^2 <= (R dims/BoxSize)^2) or Gaussian
+ * (exp(-d^2 / (2 R_grid^2))) filter divided by its float64 sum (written to *norm);
+ * pyl_fft_r2c follows.  pyl_cmul: a[i] *= b[i] for n complex64 values (the
+ * Fourier-space product of field_smoothing). */
+int pyl_filter_grid(float *field, int dims, float box_size, float R, int gaussian, double *norm, void *stream);
+int pyl_cmul(void *a, const void *b, int64_t n, void *stream);
+
 /* ---- correlation function (Pk_library.Xi, library/Pk_library/Pk_library.pyx:2035-2150) ----
  * pyl_xi_power: in place over an R2C output, every stored mode becomes
  * (|delta_k * W^-1|^2, 0) with the MAS factor of exponent mas_p rounded to float

@@ -10,10 +10,12 @@ What is compiled (read from the reference tree, never copied into the repo):
   library/Pk_library/Pk_library.pyx               -> Pk_library*.so
   library/Pk_library/bispectrum_library.pyx       -> bispectrum_library*.so
   library/redshift_space_library.pyx              -> redshift_space_library*.so
-with the reference's own compiler flags (library/setup.py:8-23):
+  library/smoothing_library/smoothing_library.pyx -> smoothing_library*.so
+with the reference's own compiler flags (library/setup.py:8-46):
   MAS: -O3 -ffast-math -march=native -fopenmp (+ -fopenmp at link, libm)
   Pk : -O3 -ffast-math -march=native -fopenmp
   Bk, redshift space: no extra flags
+  smoothing: -O3 -ffast-math -march=native -fopenmp (+ -fopenmp at link, libm)
 
 The sources are Python 2 Cython.  Three things are needed to run them on
 Python 3 and they are applied to a temporary copy outside the repository
@@ -44,6 +46,7 @@ _SOURCES = {
     'Pk_library': ['library/Pk_library/Pk_library.pyx'],
     'bispectrum_library': ['library/Pk_library/bispectrum_library.pyx'],
     'redshift_space_library': ['library/redshift_space_library.pyx'],
+    'smoothing_library': ['library/smoothing_library/smoothing_library.pyx'],
 }
 
 
@@ -93,6 +96,9 @@ def build(reference=DEFAULT_REF, out=OUT, quiet=True):
                       include_dirs=inc),
             Extension('redshift_space_library', [os.path.join(tmp, 'redshift_space_library.pyx')],
                       include_dirs=inc),
+            Extension('smoothing_library', [os.path.join(tmp, 'smoothing_library.pyx')],
+                      include_dirs=inc, extra_compile_args=native, extra_link_args=['-fopenmp'],
+                      libraries=['m']),
         ]
         exts = cythonize(exts, compiler_directives={'language_level': 2},
                          include_path=[tmp], quiet=quiet, build_dir=os.path.join(tmp, 'c'))
@@ -123,6 +129,13 @@ def load_reference(out=OUT):
     import Pk_library
     import bispectrum_library
     return MAS_library, Pk_library, bispectrum_library
+
+
+def load_smoothing(out=OUT):
+    """Import the compiled reference smoothing_library (it imports Pk_library itself)."""
+    load_reference(out)
+    import smoothing_library
+    return smoothing_library
 
 
 def load_redshift_space(out=OUT):

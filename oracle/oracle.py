@@ -509,3 +509,30 @@ def XPk_plane(delta1, delta2, BoxSize, MAS1=None, MAS2=None, threads=1):
     r.XPk = X[1:] / N[1:] * fact
     r.r = r.XPk / np.sqrt(r.Pk[:, 0] * r.Pk[:, 1])
     return r
+
+
+# ------------------------------------------------------------------ smoothing
+def FT_filter(BoxSize, R, dims, Filter, threads=1):
+    """smoothing_library.FT_filter (smoothing_library.pyx:20-87): the filter on the
+    grid (Top-Hat: 1 where d^2 <= (R dims/BoxSize)^2; Gaussian: exp(-d^2/(2 R_grid^2))),
+    divided by its float64 sum, then R2C."""
+    if Filter not in ('Top-Hat', 'Gaussian'):
+        raise ValueError('Filter %s not implemented!' % Filter)
+    R_grid = np.float32(np.float32(R) * dims / np.float32(BoxSize))
+    R2 = np.float32(R_grid * R_grid)
+    f = _freqs(dims)
+    d2 = (f[:, None, None] ** 2 + f[None, :, None] ** 2 + f[None, None, :] ** 2)
+    if Filter == 'Top-Hat':
+        field = (d2 <= R2).astype(np.float32)
+    else:
+        field = np.exp(-d2 / (2.0 * np.float64(R2))).astype(np.float32)
+    norm = np.sum(field, dtype=np.float64)
+    field = (field.astype(np.float64) / norm).astype(np.float32)
+    return fft_r2c(field, threads).astype(np.complex64)
+
+
+def field_smoothing(field, filter_k, threads=1):
+    """smoothing_library.field_smoothing (:94-123): normalised C2R of FFT(field) * filter_k."""
+    import scipy.fft
+    fk = (fft_r2c(field, threads) * filter_k).astype(np.complex64)
+    return scipy.fft.irfftn(fk, s=field.shape, workers=max(1, threads)).astype(np.float32)

@@ -55,6 +55,8 @@ SIGNATURES = {
     'pyl_fft2_r2c': (_I, [_P, _P, _I, _I, _P]),
     'pyl_pk_plane_bins': (_I, [_I]),
     'pyl_pk_plane_bin': (_I, [_P, _P, _I, _I, _I, _P, _P]),
+    'pyl_filter_grid': (_I, [_P, _I, _F, _F, _I, _P, _P]),
+    'pyl_cmul': (_I, [_P, _P, _I64, _P]),
     'pyl_correct_mas': (_I, [_P, _I, _I, _P]),
     'pyl_xi_sums_len': (_I64, [_I]),
     'pyl_xi_power': (_I, [_P, _I, _I, _P]),

@@ -219,7 +219,28 @@ def make_plane(MASL, PKL):
     return out
 
 
-def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane')):
+def make_smoothing(MASL):
+    """smoothing_library.FT_filter and field_smoothing (smoothing_library.pyx:20-123):
+    Top-Hat and Gaussian filters on 32^3 and 15^3 grids, applied to a CIC field."""
+    SL = build_ref.load_smoothing()
+    out = {}
+    rng = np.random.default_rng(61)
+    L = 1000.0
+    for N in (32, 15):
+        pos = (rng.random((N ** 3 * 2, 3)) * L).astype(np.float32)
+        d = cic_overdensity(MASL, pos, N, L)
+        out['field_%d' % N] = d
+        for filt, R in (('Top-Hat', 100.0), ('Gaussian', 60.0)):
+            with quiet():
+                fk = np.asarray(SL.FT_filter(L, R, N, filt, 1))
+                sm = np.asarray(SL.field_smoothing(d, fk, 1))
+            tag = filt.replace('-', '')
+            out['filter_%s_%d' % (tag, N)] = fk
+            out['smoothed_%s_%d' % (tag, N)] = sm
+    return out
+
+
+def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing')):
     if not build_ref.built():
         build_ref.build()
     MASL, PKL, BKL = build_ref.load_reference()
@@ -229,6 +250,8 @@ def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane')):
         np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
     if 'bk' in which:
         np.savez_compressed(os.path.join(HERE, 'bk_golden.npz'), **make_bk(MASL, BKL))
+    if 'smoothing' in which:
+        np.savez_compressed(os.path.join(HERE, 'smoothing_golden.npz'), **make_smoothing(MASL))
     if 'plane' in which:
         np.savez_compressed(os.path.join(HERE, 'plane_golden.npz'), **make_plane(MASL, PKL))
     if 'xi' in which:
@@ -242,4 +265,4 @@ def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane')):
 
 
 if __name__ == '__main__':
-    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi', 'plane'))
+    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing'))

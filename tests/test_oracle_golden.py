@@ -223,3 +223,19 @@ def test_oracle_plane_golden(pg, N):
     x = O.XPk_plane(a, b, 1000.0, 'CIC', 'TSC')
     for n in ('k', 'Pk', 'XPk', 'r'):
         np.testing.assert_allclose(getattr(x, n), pg['XPkplane_%d_%s' % (N, n)], rtol=1e-12)
+
+
+@pytest.fixture(scope='module')
+def sg():
+    return np.load(os.path.join(GOLDEN, 'smoothing_golden.npz'))
+
+
+@pytest.mark.parametrize('N', [32, 15])
+@pytest.mark.parametrize('filt,R', [('Top-Hat', 100.0), ('Gaussian', 60.0)])
+def test_oracle_smoothing_golden(sg, N, filt, R):
+    t = filt.replace('-', '')
+    gf = sg['filter_%s_%d' % (t, N)]
+    np.testing.assert_array_equal(O.FT_filter(1000.0, R, N, filt), gf)
+    sm = O.field_smoothing(sg['field_%d' % N], gf)
+    ref = sg['smoothed_%s_%d' % (t, N)]
+    assert np.abs(sm - ref).max() <= 1e-6 * np.abs(ref).max()
