@@ -324,7 +324,8 @@ def bench_zeldovich(reps=3):
     field (P ~ k^-1.5 exp(-(k/0.5)^2), sigma 0.5, 1000 Mpc/h, seed 1) in redshift space
     along axis 2 (f = 0.5): TSC and PCS onto 512^3 with and without interlacing, P(k)
     l=0,2,4 + Pk2D along axis 2 (particles/s, device time per chain); then XPk of the
-    TSC field against the NGP field (fields/s)."""
+    TSC field against the NGP field; the interlaced TSC chain again through the
+    deterministic sorted strategy."""
     import torch
     from pylians_gb300 import synthetic
     from pylians_gb300.pipeline import ParticlePk
@@ -349,6 +350,19 @@ def bench_zeldovich(reps=3):
             out['%s%s' % (mas, '_interlaced' if inter else '')] = dict(ms=ms, particles_per_s=n / (ms / 1e3))
             del pp
             torch.cuda.empty_cache()
+    # the deterministic sorted strategy on the same chain (TSC, interlaced)
+    pp = ParticlePk(512, BOX, 'TSC', axis=2, interlaced=True, max_particles=n, strategy='sorted')
+    pp.step(pos)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        pp.step(pos)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out['TSC_interlaced_sorted'] = dict(ms=ms, particles_per_s=n / (ms / 1e3))
+    del pp
+    torch.cuda.empty_cache()
     a = torch.empty((512, 512, 512), device='cuda')
     b = torch.empty((512, 512, 512), device='cuda')
     MASL.overdensity_device(pos, a, BOX, 'TSC')

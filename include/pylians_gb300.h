@@ -82,6 +82,16 @@ int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n_particl
                        float *grid_interlaced, int dims, float box_size, int mas, int strategy,
                        void *workspace, size_t workspace_bytes, void *stream);
 
+/* pyl_ma_overdensity with redshift_space_library.pos_redshift_space
+ * (library/redshift_space_library.pyx:29-43) in front: pos[:,axis] becomes
+ * pos + vel (1+redshift)/hubble, wrapped into the box, IN PLACE (as the reference
+ * mutates pos), then the overdensity deposit runs on the shifted positions.  On
+ * the tiled path with a 16-byte aligned pos the shift is fused into the
+ * histogram pass; otherwise it runs as its own pass first. */
+int pyl_ma_overdensity_rsd(float *pos, const float *vel, const float *weights, int64_t n, float *grid,
+                           float *grid_interlaced, int dims, float box_size, int mas, int strategy, float hubble,
+                           float redshift, int axis, void *workspace, size_t workspace_bytes, void *stream);
+
 /* Allocation-free mass assignment.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory around the call (code running
  * during CUDA-graph capture, plugins inside a host framework that owns the

@@ -30,6 +30,7 @@ SIGNATURES = {
     'pyl_ma': (_I, [_P, _P, _I64, _I, _P, _P, _I, _F, _I, _I, _I, _P, _SZ, _P]),
     'pyl_ma_noalloc': (_I, [_P, _P, _I64, _P, _P, _I, _F, _I, _P]),
     'pyl_ma_overdensity': (_I, [_P, _P, _I64, _P, _P, _I, _F, _I, _I, _P, _SZ, _P]),
+    'pyl_ma_overdensity_rsd': (_I, [_P, _P, _P, _I64, _P, _P, _I, _F, _I, _I, _F, _F, _I, _P, _SZ, _P]),
     'pyl_ma_batch': (_I, [_P, _I, _P, _I, _P, _I, _P]),
     'pyl_fill': (_I, [_P, _I64, _F, _P]),
     'pyl_scale': (_I, [_P, _I64, _F, _P]),

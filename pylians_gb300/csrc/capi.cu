@@ -79,6 +79,30 @@ void stage_mark(int phase, bool begin, cudaStream_t st)
 }
 }  // namespace pyl
 
+#include <map>
+#include <utility>
+
+namespace pyl {
+namespace {
+std::mutex g_smem_mu;
+std::map<std::pair<int, const void *>, size_t> g_smem_limits;
+}  // namespace
+
+size_t smem_limit_raise(const void *kernel, size_t bytes, cudaError_t *err)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    size_t &cur = g_smem_limits[std::make_pair(dev, kernel)];
+    if (bytes > cur) {
+        *err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (*err != cudaSuccess) return cur;
+        cur = bytes;
+    }
+    return cur;
+}
+}  // namespace pyl
+
 extern "C" int pyl_stage_timing(int enable)
 {
     std::lock_guard<std::mutex> lk(pyl::g_stage_mu);

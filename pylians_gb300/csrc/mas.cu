@@ -207,13 +207,33 @@ __global__ void __launch_bounds__(256) colscan_kernel(unsigned *__restrict__ his
     total[t] = run;
 }
 
+// Placement chosen on the device from the input's coherence.  The histogram pass
+// counts particles that fall in the same bin as the particle before them; input in
+// spatial order (lattices, cell-ordered catalogues) scores near 1, random order
+// near 1/bins.  Coherent input is placed in one pass straight into the final
+// layout (its writes already form long runs), the rest through the two-level
+// shared-memory sorts.  Every candidate launch sits in the stream (and a captured
+// graph); a launch whose gate does not match the count returns at once.
+struct Gate {
+    const unsigned long long *same;    // null: the launch always runs
+    unsigned long long thresh;         // coherent when *same >= thresh
+    int want;                          // 1: run on coherent input only, 0: on incoherent only
+};
+
+__device__ __forceinline__ bool gate_closed(const Gate &gt)
+{
+    if (!gt.same) return false;
+    return (*gt.same >= gt.thresh ? 1 : 0) != gt.want;
+}
+
 template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk,
     float inv, TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
-    float4 *__restrict__ rec)
+    float4 *__restrict__ rec, Gate gate = Gate{nullptr, 0ull, 0})
 {
     extern __shared__ unsigned cur[];
+    if (gate_closed(gate)) return;
     const int T = (int)g.ntiles;
     const unsigned *row = colpre + (long long)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) cur[t] = offsets[t] + row[t];
@@ -221,7 +241,8 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
     constexpr int U = 4;            // particles in flight per thread
     const long long step = (long long)blockDim.x * U;
-    for (long long i0 = b + threadIdx.x; i0 < e; i0 += step) {
+    for (long long base = b; base < e; base += step) {     // uniform over the block
+        const long long i0 = base + threadIdx.x;
         float4 r[U];
         unsigned key[U];
 #pragma unroll
@@ -234,10 +255,22 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
                 key[u] = tile_key<MAS>(p, inv, g);
             }
         }
+        // lanes hold consecutive particles: lanes with equal bins take one
+        // reservation of consecutive slots (spatially ordered input has whole
+        // warps in one bin)
+        const unsigned lane = threadIdx.x & 31u;
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const long long i = i0 + (long long)u * blockDim.x;
-            if (i < e) rec[atomicAdd(cur + key[u], 1u)] = r[u];
+            const unsigned act = __ballot_sync(0xffffffffu, i < e);
+            if (i < e) {
+                const unsigned peers = __match_any_sync(act, key[u]);
+                const unsigned leader = (unsigned)__ffs(peers) - 1u;
+                unsigned slot = 0u;
+                if (lane == leader) slot = atomicAdd(cur + key[u], (unsigned)__popc(peers));
+                slot = __shfl_sync(peers, slot, leader) + (unsigned)__popc(peers & ((1u << lane) - 1u));
+                if (slot < (unsigned long long)n) rec[slot] = r[u];
+            }
         }
     }
 }
@@ -252,7 +285,7 @@ __global__ void __launch_bounds__(1024) chunk_scatter_kernel(
 // a shared-memory sort, into the final [tile][chunk] layout.  Both levels place
 // exactly where the single-level scatter would (same per-(chunk, tile) ranges).
 // (Level B is the TMA-staged level_b_tma_kernel below.)
-constexpr int TWO_LEVEL_TILES = 4096;
+constexpr int TWO_LEVEL_TILES = 1024;   // up to here level A sorts by bin in one pass, whatever the input order
 constexpr int LA_THREADS = 1024, LA_U = 4, LA_BATCH = LA_THREADS * LA_U;
 
 // Exclusive scan of n <= blockDim.x values in place; returns nothing, needs a
@@ -359,6 +392,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_kernel(
 __device__ unsigned g_tma_error;
 
 constexpr int HT_BATCH = 2048;                  // histogram batch (particles)
+constexpr int HT_NBUF = 4;                      // batches in flight
 
 // Particles of batch j wholly inside its bulk copy.
 __device__ __forceinline__ int staged_full(int cnt) { return (int)(((long long)cnt * 12 & ~15LL) / 12); }
@@ -366,112 +400,159 @@ __device__ __forceinline__ int staged_full(int cnt) { return (int)(((long long)c
 __device__ __forceinline__ unsigned staged_bytes(long long cnt) { return (unsigned)((cnt * 12) & ~15LL); }
 
 // One CTA per chunk: tile histogram of the chunk's particles (shared-memory counters).
-template <int MAS>
-__global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *__restrict__ pos, long long n,
-                                                              long long chunk, float inv, TileGeom g,
-                                                              unsigned *__restrict__ hist)
+// Redshift-space shift fused into the histogram pass (pyl_ma_overdensity_rsd):
+// the line-of-sight coordinate becomes x + v (1+z)/H, wrapped like
+// redshift_space_library.pyx:38-42, and is written back before it is binned.
+struct RsdArgs {
+    float *pos;          // the same array as the kernel's input, written in place
+    const float *vel;
+    float factor, box;   // factor = (1 + redshift) / hubble, rounded to float
+    float hubble, redshift;
+    int axis;
+};
+
+__device__ __forceinline__ float rsd_shift(float p, float v, float factor, float box)
 {
+    float s = __fadd_rn(p, __fmul_rn(v, factor));
+    if (s > box || s < 0.0f) s = fmodf(__fadd_rn(s, box), box);
+    return s;
+}
+
+template <int MAS, bool RSD = false>
+__global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *pos, long long n,
+                                                              long long chunk, float inv, TileGeom g,
+                                                              unsigned *__restrict__ hist, RsdArgs rsd = RsdArgs{},
+                                                              unsigned long long *coh = nullptr)
+{
+    __shared__ unsigned s_same;             // particles in the same bin as their predecessor
     extern __shared__ __align__(16) unsigned char hraw[];
-    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ __align__(8) unsigned long long bar[HT_NBUF];
     __shared__ int s_ok;
     const int T = (int)g.ntiles;
-    float *inb = (float *)hraw;                                  // [2][HT_BATCH * 3]
-    unsigned *cnt = (unsigned *)(hraw + 2 * HT_BATCH * 12);
+    float *inb = (float *)hraw;                                  // [HT_NBUF][HT_BATCH * 3]
+    unsigned *cnt = (unsigned *)(hraw + HT_NBUF * HT_BATCH * 12);
     for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0;
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
     const long long nbat = e > b ? (e - b + HT_BATCH - 1) / HT_BATCH : 0;
+    unsigned my_same = 0u;                  // lane 0 of each warp: its warp's count
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        s_same = 0u;
+        for (int k = 0; k < HT_NBUF; k++) mbar_init(&bar[k], 1);
         mbar_fence_init();
     }
     __syncthreads();
     if (threadIdx.x == 0)
-        for (long long j = 0; j < 2 && j < nbat; j++) {
+        for (long long j = 0; j < HT_NBUF && j < nbat; j++) {
             const long long s0 = b + j * HT_BATCH;
-            stage_copy(inb + (j & 1) * HT_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)HT_BATCH, e - s0)),
-                       &bar[j & 1]);
+            stage_copy(inb + (j % HT_NBUF) * HT_BATCH * 3, pos + 3 * s0,
+                       staged_bytes(min((long long)HT_BATCH, e - s0)), &bar[j % HT_NBUF]);
         }
     for (long long j = 0; j < nbat; j++) {
         const long long s0 = b + j * HT_BATCH;
         const int c = (int)min((long long)HT_BATCH, e - s0);
         const int full = staged_full(c);
-        const float *in = inb + (j & 1) * HT_BATCH * 3;
-        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (unsigned)((j >> 1) & 1), &g_tma_error);
+        const int buf = (int)(j % HT_NBUF);
+        const float *in = inb + buf * HT_BATCH * 3;
+        if (threadIdx.x == 0)
+            s_ok = mbar_wait_bounded(&bar[buf], (unsigned)((j / HT_NBUF) & 1), &g_tma_error);
         __syncthreads();
         if (!s_ok) {
-            if (threadIdx.x == 0 && j + 1 < nbat)
-                mbar_wait_bounded(&bar[(j + 1) & 1], (unsigned)(((j + 1) >> 1) & 1), &g_tma_error);
+            if (threadIdx.x == 0)
+                for (long long k = j + 1; k < nbat && k < j + HT_NBUF; k++)
+                    mbar_wait_bounded(&bar[k % HT_NBUF], (unsigned)((k / HT_NBUF) & 1), &g_tma_error);
             return;
         }
         for (int i = threadIdx.x; i < c; i += blockDim.x) {
             float p[3];
+            const long long q = s0 + i;
             if (i < full) { p[0] = in[3 * i]; p[1] = in[3 * i + 1]; p[2] = in[3 * i + 2]; }
-            else { const long long q = s0 + i; p[0] = __ldg(pos + 3 * q); p[1] = __ldg(pos + 3 * q + 1); p[2] = __ldg(pos + 3 * q + 2); }
-            atomicAdd(cnt + tile_key<MAS>(p, inv, g), 1u);
+            else { p[0] = pos[3 * q]; p[1] = pos[3 * q + 1]; p[2] = pos[3 * q + 2]; }
+            if (RSD) {
+                const float sh = rsd_shift(p[rsd.axis], __ldg(rsd.vel + 3 * q + rsd.axis), rsd.factor, rsd.box);
+                p[rsd.axis] = sh;
+                rsd.pos[3 * q + rsd.axis] = sh;
+            }
+            const unsigned key = tile_key<MAS>(p, inv, g);
+            atomicAdd(cnt + key, 1u);
+            if (coh) {                              // the warp's lanes hold consecutive particles
+                const unsigned prev = __shfl_up_sync(__activemask(), key, 1);
+                const unsigned same = __ballot_sync(__activemask(), (threadIdx.x & 31) && prev == key);
+                my_same += (unsigned)__popc(same);
+            }
         }
         __syncthreads();
-        if (threadIdx.x == 0 && j + 2 < nbat) {
-            const long long s2 = b + (j + 2) * HT_BATCH;
-            stage_copy(inb + (j & 1) * HT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)HT_BATCH, e - s2)),
-                       &bar[j & 1]);
+        if (threadIdx.x == 0 && j + HT_NBUF < nbat) {
+            const long long s2 = b + (j + HT_NBUF) * HT_BATCH;
+            stage_copy(inb + buf * HT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)HT_BATCH, e - s2)),
+                       &bar[buf]);
         }
     }
+    if (coh && (threadIdx.x & 31) == 0 && my_same) atomicAdd(&s_same, my_same);
     __syncthreads();
     unsigned *row = hist + (long long)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = cnt[t];
+    if (coh && threadIdx.x == 0 && s_same) atomicAdd(coh, (unsigned long long)s_same);
 }
 
-inline size_t hist_tma_smem(long long ntiles) { return (size_t)2 * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
+inline size_t hist_tma_smem(long long ntiles) { return (size_t)HT_NBUF * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
 
 constexpr int LAT_U = 4, LAT_BATCH = LA_THREADS * LAT_U;     // 4096 particles per batch
+constexpr int LA_NBUF = 2;                                  // batches in flight
 
 template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
     TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
-    float4 *__restrict__ tmp)
+    float4 *__restrict__ tmp, int by_tile, Gate gate = Gate{nullptr, 0ull, 0})
 {
     extern __shared__ __align__(16) unsigned char araw[];
-    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ __align__(8) unsigned long long bar[LA_NBUF];
     __shared__ int s_ok;
-    const int NCO = g.nc * g.nc * g.nc;
+    if (gate_closed(gate)) return;
+    // buckets: coarse blocks of 4^3 bins (level A of two), or the bins themselves
+    // (one pass into the final layout, for grids of at most TWO_LEVEL_TILES bins)
     const int T = (int)g.ntiles;
-    float *inb = (float *)araw;                                            // [2][LAT_BATCH * 3]
-    float4 *stage = (float4 *)(araw + 2 * LAT_BATCH * 12);
+    const int NCO = by_tile ? T : g.nc * g.nc * g.nc;
+    float *inb = (float *)araw;                                            // [LA_NBUF][LAT_BATCH * 3]
+    float4 *stage = (float4 *)(araw + LA_NBUF * LAT_BATCH * 12);
     unsigned short *sco = (unsigned short *)(stage + LAT_BATCH);
     unsigned *cur = (unsigned *)(sco + LAT_BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
     const unsigned *row = colpre + (long long)blockIdx.x * T;
     for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
-        unsigned sacc = 0;
-        for (int l = 0; l < 64; l++) sacc += row[co * 64 + l];
-        cur[co] = offsets[co * 64] + sacc;
+        if (by_tile) {
+            cur[co] = offsets[co] + row[co];
+        } else {
+            unsigned sacc = 0;
+            for (int l = 0; l < 64; l++) sacc += row[co * 64 + l];
+            cur[co] = offsets[co * 64] + sacc;
+        }
     }
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
     const long long nbat = e > b ? (e - b + LAT_BATCH - 1) / LAT_BATCH : 0;
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int q = 0; q < LA_NBUF; q++) mbar_init(&bar[q], 1);
         mbar_fence_init();
     }
     __syncthreads();
     if (threadIdx.x == 0)
-        for (long long j = 0; j < 2 && j < nbat; j++) {
+        for (long long j = 0; j < LA_NBUF && j < nbat; j++) {
             const long long s0 = b + j * LAT_BATCH;
-            stage_copy(inb + (j & 1) * LAT_BATCH * 3, pos + 3 * s0, staged_bytes(min((long long)LAT_BATCH, e - s0)),
-                       &bar[j & 1]);
+            stage_copy(inb + (j % LA_NBUF) * LAT_BATCH * 3, pos + 3 * s0,
+                       staged_bytes(min((long long)LAT_BATCH, e - s0)), &bar[j % LA_NBUF]);
         }
     for (long long j = 0; j < nbat; j++) {
         const long long s0 = b + j * LAT_BATCH;
         const int c = (int)min((long long)LAT_BATCH, e - s0);
         const int full = staged_full(c);
-        const float *in = inb + (j & 1) * LAT_BATCH * 3;
-        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[j & 1], (unsigned)((j >> 1) & 1), &g_tma_error);
+        const int buf = (int)(j % LA_NBUF);
+        const float *in = inb + buf * LAT_BATCH * 3;
+        if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[buf], (unsigned)((j / LA_NBUF) & 1), &g_tma_error);
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) bcnt[co] = 0u;
         __syncthreads();
         if (!s_ok) {
-            if (threadIdx.x == 0 && j + 1 < nbat)
-                mbar_wait_bounded(&bar[(j + 1) & 1], (unsigned)(((j + 1) >> 1) & 1), &g_tma_error);
+            if (threadIdx.x == 0)
+                for (long long q = j + 1; q < nbat && q < j + LA_NBUF; q++)
+                    mbar_wait_bounded(&bar[q % LA_NBUF], (unsigned)((q / LA_NBUF) & 1), &g_tma_error);
             return;
         }
         float4 r[LAT_U];
@@ -488,15 +569,16 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
                 }
                 if (WEIGHTED) r[u].w = __ldg(w + s0 + i);
                 const float p[3] = {r[u].x, r[u].y, r[u].z};
-                co_u[u] = tile_key<MAS>(p, inv, g) >> 6;
+                const unsigned key = tile_key<MAS>(p, inv, g);
+                co_u[u] = by_tile ? key : key >> 6;
                 rank[u] = atomicAdd(bcnt + co_u[u], 1u);
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0 && j + 2 < nbat) {                  // this buffer is consumed
-            const long long s2 = b + (j + 2) * LAT_BATCH;
-            stage_copy(inb + (j & 1) * LAT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LAT_BATCH, e - s2)),
-                       &bar[j & 1]);
+        if (threadIdx.x == 0 && j + LA_NBUF < nbat) {            // this buffer is consumed
+            const long long s2 = b + (j + LA_NBUF) * LAT_BATCH;
+            stage_copy(inb + buf * LAT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LAT_BATCH, e - s2)),
+                       &bar[buf]);
         }
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
             gst[co] = cur[co];
@@ -524,7 +606,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
 
 inline size_t level_a_tma_smem(int nco)
 {
-    return (size_t)2 * LAT_BATCH * 12 + sizeof(float4) * LAT_BATCH + sizeof(unsigned short) * LAT_BATCH +
+    return (size_t)LA_NBUF * LAT_BATCH * 12 + sizeof(float4) * LAT_BATCH + sizeof(unsigned short) * LAT_BATCH +
            sizeof(unsigned) * (3 * nco + 32);
 }
 
@@ -534,12 +616,13 @@ template <int MAS>
 __global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
     const float4 *__restrict__ tmp, int C, float inv, TileGeom g, const unsigned *__restrict__ colpre,
     const unsigned *__restrict__ total, const unsigned *__restrict__ offsets, float4 *__restrict__ rec,
-    unsigned n)
+    unsigned n, Gate gate = Gate{nullptr, 0ull, 0})
 {
     __shared__ unsigned fcur[64], bcnt[64], gst[64], wt[32];
     __shared__ unsigned seg_start, seg_len;
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ int s_ok;
+    if (gate_closed(gate)) return;
     extern __shared__ __align__(16) float4 braw[];
     float4 *inb = braw;                                     // [2][LBT_BATCH]
     float4 *stage = braw + 2 * LBT_BATCH;
@@ -854,6 +937,7 @@ struct TiledWs {
     unsigned *hist, *total, *offsets;
     float4 *rec;                 // binned particles: x, y, z, weight
     float4 *tmp;                 // two-level placement: the coarse-block layout
+    unsigned long long *same;    // coherence count of the histogram pass
     int chunks;
     bool smem_hist;
     size_t bytes;
@@ -874,6 +958,7 @@ TiledWs tiled_layout(void *base, long long n, int dims)
     ws.hist = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * hist_len, 256);
     ws.total = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.offsets = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * (g.ntiles + 1), 256);
+    ws.same = (unsigned long long *)(b + off); off = align_up(off + sizeof(unsigned long long), 256);
     ws.rec = (float4 *)(b + off); off = align_up(off + sizeof(float4) * (size_t)n, 256);
     ws.tmp = nullptr;
     if (ws.smem_hist && g.ntiles > TWO_LEVEL_TILES) {
@@ -1067,7 +1152,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
             }
             float *out = pass == 0 ? grid : grid2;
             if (interior) {
-                const unsigned base = ((unsigned)o[0] * dims + o[1]) * dims + o[2];
+                const unsigned gbase = ((unsigned)o[0] * dims + o[1]) * dims + o[2];
                 for (int c = threadIdx.x; c < CELLS; c += 1024) {
                     const unsigned w = smw[c];
                     if (w == 0u) continue;
@@ -1075,7 +1160,7 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
                                               : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
                                                                     : __fmul_rn(__uint2float_rn(w), FX_INV));
                     const unsigned lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                    atomicAdd(out + (base + (lx * dims + ly) * dims + lz), __fmul_rn(v, scale));
+                    atomicAdd(out + (gbase + (lx * dims + ly) * dims + lz), __fmul_rn(v, scale));
                 }
             } else {
                 const long long d = dims;
@@ -1144,7 +1229,8 @@ int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, flo
 
 template <int MAS>
 int launch_tiled(const float *pos, const float *w, long long n, float *grid, float *grid2,
-                 int dims, float inv, float halfcell, void *workspace, OutScale sc, cudaStream_t st)
+                 int dims, float inv, float halfcell, void *workspace, OutScale sc, cudaStream_t st,
+                 const RsdArgs *rsd = nullptr)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws = tiled_layout(workspace, n, dims);
@@ -1156,10 +1242,21 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         const bool tma = (((uintptr_t)pos) & 15) == 0;
         const size_t sm = sizeof(unsigned) * T;
         static size_t d1 = 0, d2 = 0, d3 = 0, d4 = 0;
+        // grids past TWO_LEVEL_TILES bins choose their placement by input coherence
+        const bool counted = rsd || (tma && hist_tma_smem(T) <= 227 * 1024);
+        const bool gated = counted && tma && ws.tmp;
+        unsigned long long *same = gated ? ws.same : nullptr;
         stage_mark(PYL_STAGE_HIST, true, st);
-        if (tma && hist_tma_smem(T) <= 227 * 1024) {
+        if (gated) PYL_CUDA(cudaMemsetAsync(ws.same, 0, sizeof(unsigned long long), st));
+        if (rsd) {                                 // callers check tiled_rsd_fusable first
+            static size_t d5 = 0;
+            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS, true>, hist_tma_smem(T), &d5));
+            chunk_hist_tma_kernel<MAS, true><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist, *rsd,
+                                                                                 same);
+        } else if (counted) {
             PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS>, hist_tma_smem(T), &d4));
-            chunk_hist_tma_kernel<MAS><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist);
+            chunk_hist_tma_kernel<MAS><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist,
+                                                                          RsdArgs{}, same);
         } else {
             PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm, &d1));
             chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
@@ -1171,21 +1268,50 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         PYL_LAUNCH_CHECK();
         stage_mark(PYL_STAGE_HIST, false, st);
         stage_mark(PYL_STAGE_PLACE, true, st);
-        if (ws.tmp) {
+        if (!ws.tmp && tma && level_a_tma_smem(T) <= 227 * 1024) {
+            // at most TWO_LEVEL_TILES bins: level A with one bucket per bin writes the
+            // final [bin][chunk] layout in one pass
+            static size_t dw = 0, du = 0;
+            const size_t sat = level_a_tma_smem(T);
+            if (w) {
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat, &dw));
+                level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                         ws.offsets, ws.rec, 1);
+            } else {
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat, &du));
+                level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                          ws.offsets, ws.rec, 1);
+            }
+        } else if (ws.tmp) {
             const int NCO = g.nc * g.nc * g.nc;
             const size_t sa = sizeof(unsigned) * ((3 * NCO + 32 + 3) & ~3) + sizeof(float4) * LA_BATCH +
                               sizeof(unsigned short) * LA_BATCH;
             static size_t da = 0, db = 0, dta = 0, dtb = 0, dtc = 0;
             const size_t sat = level_a_tma_smem(NCO);
+            // coherent when at least 3/4 of the particles share their predecessor's bin
+            const unsigned long long thresh = (unsigned long long)n - (unsigned long long)n / 4;
+            const Gate coherent{same, thresh, 1}, incoherent{same, thresh, 0};
+            if (gated) {
+                if (w) {
+                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
+                    chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                         ws.offsets, ws.rec, coherent);
+                } else {
+                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm, &d3));
+                    chunk_scatter_kernel<MAS, false><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                                                                          ws.offsets, ws.rec, coherent);
+                }
+                PYL_LAUNCH_CHECK();
+            }
             if (tma && sat <= 227 * 1024) {
                 if (w) {
                     PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat, &dta));
                     level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                             ws.offsets, ws.tmp);
+                                                                             ws.offsets, ws.tmp, 0, incoherent);
                 } else {
                     PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat, &dtb));
                     level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                              ws.offsets, ws.tmp);
+                                                                              ws.offsets, ws.tmp, 0, incoherent);
                 }
             } else if (w) {
                 PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa, &da));
@@ -1201,7 +1327,7 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
             stage_mark(PYL_STAGE_PLACE_B, true, st);
             PYL_CUDA(ensure_smem(level_b_tma_kernel<MAS>, level_b_tma_smem(), &dtc));
             level_b_tma_kernel<MAS><<<(unsigned)(C * NCO), LBT_THREADS, level_b_tma_smem(), st>>>(
-                ws.tmp, C, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n);
+                ws.tmp, C, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n, incoherent);
             PYL_LAUNCH_CHECK();
             stage_mark(PYL_STAGE_PLACE_B, false, st);
         } else if (w) {
@@ -1365,9 +1491,20 @@ __global__ void mass_scale_kernel(const double *sum, double cells, float *scale)
 
 extern "C" int pyl_grid_sum(const float *grid, int64_t n, double *d_sum, void *stream);
 
-extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n, float *grid,
-                                  float *grid_interlaced, int dims, float box_size, int mas,
-                                  int strategy, void *workspace, size_t workspace_bytes, void *stream)
+extern "C" int pyl_pos_redshift_space(float *pos, const float *vel, int64_t n, float box_size, float hubble,
+                                      float redshift, int axis, void *stream);
+
+namespace {
+// The redshift shift can ride on the staged histogram pass of the tiled deposit.
+bool tiled_rsd_fusable(const float *pos, int dims)
+{
+    const TileGeom g = tile_geom(dims);
+    return (((uintptr_t)pos) & 15) == 0 && g.ntiles <= HIST_MAX_TILES && hist_tma_smem(g.ntiles) <= 227 * 1024;
+}
+
+int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float *grid, float *grid_interlaced,
+                        int dims, float box_size, int mas, int strategy, void *workspace, size_t workspace_bytes,
+                        void *stream, const RsdArgs *rsd)
 {
     PYL_CHECK_ARG(mas >= PYL_MAS_NGP && mas <= PYL_MAS_PCS, "MAS must be NGP, CIC, TSC or PCS");
     PYL_CHECK_ARG(dims > 0 && dims <= 65536, "dims out of range");
@@ -1393,6 +1530,10 @@ extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_
         PYL_LAUNCH_CHECK();
         sc = OutScale{0.0f, d_scale};
     }
+    const float inv = (float)dims / box_size;
+    const float halfcell = (float)(0.5 * (double)box_size / dims);
+    int s = pick_strategy(strategy, 3, dims, n);
+    if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
     const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
     stage_mark(PYL_STAGE_FILL, true, st);
     fill_kernel<<<blocks, 256, 0, st>>>(grid, cells, -1.0f);
@@ -1402,19 +1543,25 @@ extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_
         PYL_LAUNCH_CHECK();
     }
     stage_mark(PYL_STAGE_FILL, false, st);
-    const float inv = (float)dims / box_size;
-    const float halfcell = (float)(0.5 * (double)box_size / dims);
-    int s = pick_strategy(strategy, 3, dims, n);
+    const RsdArgs *fused = nullptr;
+    if (rsd) {
+        if (s == PYL_STRATEGY_TILED && tiled_rsd_fusable(pos, dims)) {
+            fused = rsd;
+        } else {
+            const int rc = pyl_pos_redshift_space(rsd->pos, rsd->vel, n, rsd->box, rsd->hubble, rsd->redshift,
+                                                  rsd->axis, stream);
+            if (rc) return rc;
+        }
+    }
     if (s == PYL_STRATEGY_SORTED)
         return launch_sorted(mas, pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, workspace, sc.host,
                              sc.dev, false, st);
-    if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
     switch (mas) {
 #define PYL_OD(M)                                                                                    \
     case M:                                                                                          \
         return s == PYL_STRATEGY_TILED                                                               \
                    ? launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,   \
-                                     workspace, sc, st)                                              \
+                                     workspace, sc, st, fused)                                       \
                    : launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
         PYL_OD(PYL_MAS_NGP)
         PYL_OD(PYL_MAS_CIC)
@@ -1423,6 +1570,36 @@ extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_
 #undef PYL_OD
     }
     return PYL_ERR_INVALID;
+}
+
+}  // namespace
+
+extern "C" int pyl_ma_overdensity(const float *pos, const float *weights, int64_t n, float *grid,
+                                  float *grid_interlaced, int dims, float box_size, int mas,
+                                  int strategy, void *workspace, size_t workspace_bytes, void *stream)
+{
+    return ma_overdensity_impl(pos, weights, n, grid, grid_interlaced, dims, box_size, mas, strategy, workspace,
+                               workspace_bytes, stream, nullptr);
+}
+
+extern "C" int pyl_ma_overdensity_rsd(float *pos, const float *vel, const float *weights, int64_t n, float *grid,
+                                      float *grid_interlaced, int dims, float box_size, int mas, int strategy,
+                                      float hubble, float redshift, int axis, void *workspace,
+                                      size_t workspace_bytes, void *stream)
+{
+    PYL_CHECK_ARG(pos != nullptr && vel != nullptr, "null pointer");
+    PYL_CHECK_ARG(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+    PYL_CHECK_ARG(hubble != 0.0f, "Hubble must be non-zero");
+    RsdArgs r;
+    r.pos = pos;
+    r.vel = vel;
+    r.factor = (float)((1.0 + (double)redshift) / (double)hubble);   // redshift_space_library.pyx:36
+    r.box = box_size;
+    r.hubble = hubble;
+    r.redshift = redshift;
+    r.axis = axis;
+    return ma_overdensity_impl(pos, weights, n, grid, grid_interlaced, dims, box_size, mas, strategy, workspace,
+                               workspace_bytes, stream, &r);
 }
 
 // ------------------------------------------------------- allocation-free variant

@@ -56,16 +56,28 @@ class ParticlePk(object):
             self.ws = torch.empty(need, dtype=torch.uint8, device=self.device)
             self.ws_bytes = need
 
-    def step(self, pos, W=None, stream=None):
-        """Enqueue one pass: overdensity deposit (grids overwritten), FFT, bin -> self.sums."""
+    def step(self, pos, W=None, stream=None, rsd=None):
+        """Enqueue one pass: overdensity deposit (grids overwritten), FFT, bin -> self.sums.
+
+        rsd=(vel, Hubble, redshift, axis) first moves the particles to redshift space
+        IN PLACE (redshift_space_library.pos_redshift_space), fused into the deposit's
+        histogram pass on the tiled path."""
         n = pos.shape[0]
         d = self.dims
         st = stream_ptr(stream)
         self.reserve(n, W is not None)
         g2 = self.grids[1] if self.interlaced else None
-        _lib.call('pyl_ma_overdensity', ptr(pos), ptr(W), n, ptr(self.grids[0]), ptr(g2), d,
-                  self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy],
-                  ptr(self.ws), self.ws_bytes, st)
+        if rsd is not None:
+            vel, hubble, redshift, axis = rsd
+            if tuple(vel.shape) != tuple(pos.shape) or vel.dtype != torch.float32 or not vel.is_cuda:
+                raise ValueError('vel must be a float32 CUDA tensor shaped like pos')
+            _lib.call('pyl_ma_overdensity_rsd', ptr(pos), ptr(vel.contiguous()), ptr(W), n, ptr(self.grids[0]),
+                      ptr(g2), d, self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy],
+                      float(hubble), float(redshift), int(axis), ptr(self.ws), self.ws_bytes, st)
+        else:
+            _lib.call('pyl_ma_overdensity', ptr(pos), ptr(W), n, ptr(self.grids[0]), ptr(g2), d,
+                      self.BoxSize, _lib.MAS_INDEX[self.MAS], _lib.STRATEGY[self.strategy],
+                      ptr(self.ws), self.ws_bytes, st)
         ng = self.grids.shape[0]
         _lib.call('pyl_fft_r2c', ptr(self.grids), ptr(self.dk), d, ng, st)
         dk2 = self.dk[1] if self.interlaced else None

@@ -185,8 +185,8 @@ def test_bad_input_raises(MASL):
 
 @pytest.mark.parametrize('mas', ['NGP', 'CIC'])
 def test_two_level_placement_matches_atomic(MASL, mas):
-    """Grids with more than 4096 tiles place particles in two levels (coarse blocks,
-    then tiles); 544^3 has 17^3 tiles in ragged 4^3 coarse blocks.  Weighted and
+    """Grids with more than 1024 tiles place randomly ordered particles in two levels
+    (coarse blocks, then tiles); 544^3 has 17^3 tiles in ragged 4^3 coarse blocks.  Weighted and
     unweighted, plain and interlaced grids must equal the atomic strategy's."""
     rng = np.random.default_rng(11)
     N, L, n = 544, 1000.0, 3_000_000
@@ -203,6 +203,38 @@ def test_two_level_placement_matches_atomic(MASL, mas):
             else:
                 assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
         del a1, a2, b1, b2
+
+
+@pytest.mark.parametrize('N', [384, 544])
+def test_coherent_placement_matches_atomic(MASL, N):
+    """Particles in spatial order (a jittered lattice, z fastest) share their
+    predecessor's bin, so the tiled strategy places them in one pass: by bin in shared
+    memory up to 4096 bins (384^3: 12^3 bins), straight to the bin otherwise (544^3).
+    Half-shuffled input (coherence near 1/2) takes the two-level sorts.  All must
+    equal the atomic strategy."""
+    rng = np.random.default_rng(13)
+    L, M = 1000.0, 160
+    g = (np.arange(M, dtype=np.float32) + 0.5) * np.float32(L / M)
+    q = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    q = (q + (rng.random(q.shape) - 0.5).astype(np.float32) * np.float32(L / M)) % np.float32(L)
+    q = q.astype(np.float32)
+    half = q.copy()
+    idx = rng.permutation(len(q))[: len(q) // 2]
+    half[np.sort(idx)] = half[idx]
+    w = torch.from_numpy((rng.random(len(q)) * 2).astype(np.float32)).cuda()
+    for arr in (q, half):
+        pos = torch.from_numpy(arr).cuda()
+        for mas, W in (('NGP', None), ('CIC', None), ('TSC', w)):
+            a1 = torch.zeros((N, N, N), device='cuda'); a2 = torch.zeros((N, N, N), device='cuda')
+            b1 = torch.zeros((N, N, N), device='cuda'); b2 = torch.zeros((N, N, N), device='cuda')
+            MASL.MA(pos, a1, L, mas, W, interlaced=a2, strategy='atomic')
+            MASL.MA(pos, b1, L, mas, W, interlaced=b2, strategy='tiled')
+            for a, b in ((a1, b1), (a2, b2)):
+                if mas == 'NGP':
+                    assert torch.equal(a, b)
+                else:
+                    assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
+            del a1, a2, b1, b2
 
 
 @pytest.mark.parametrize('mas', ['CIC', 'TSC', 'PCS'])

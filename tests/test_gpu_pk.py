@@ -199,3 +199,24 @@ def test_overdensity_deposit_matches_two_pass(weighted):
         for d, g in ((d1, g1), (d2, g2)):
             ref = g.double() / mean - 1.0
             assert (d.double() - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
+
+
+@pytest.mark.parametrize('mas', ['NGP', 'CIC', 'TSC', 'PCS'])
+def test_overdensity_owned_cells_with_empty_bins(mas):
+    """The staged tiled deposit stores its bins' own cells itself (only the halo shells
+    are pre-filled with -1): particles packed into one corner of a ragged 200^3 grid
+    leave most bins empty, which must still read -1, and every cell must equal the
+    two-pass MA + delta = n/mean - 1, plain and interlaced."""
+    import pylians_gb300.MAS_library as MASL
+    rng = np.random.default_rng(23)
+    N, L, n = 200, 1000.0, 1_500_000
+    pos = torch.from_numpy((rng.random((n, 3)) * 260.0 + 30.0).astype(np.float32)).cuda()
+    d1 = torch.full((N, N, N), 7.0, device='cuda'); d2 = torch.full((N, N, N), 7.0, device='cuda')
+    MASL.overdensity_device(pos, d1, L, mas, grid_interlaced=d2, strategy='tiled')
+    g1 = torch.zeros((N, N, N), device='cuda'); g2 = torch.zeros((N, N, N), device='cuda')
+    MASL.MA(pos, g1, L, mas, interlaced=g2, strategy='atomic')
+    mean = float(n) / N ** 3
+    for d, g in ((d1, g1), (d2, g2)):
+        ref = g.double() / mean - 1.0
+        assert (d.double() - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
+        assert torch.equal(d[g == 0], torch.full_like(d[g == 0], -1.0))

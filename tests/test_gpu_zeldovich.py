@@ -72,3 +72,26 @@ def test_zeldovich_xpk_against_ngp(parts):
     r = PKL.XPk([torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()], L, 2, ['TSC', 'NGP'])
     o = O.XPk([a, b], L, 2, ['TSC', 'NGP'], 1)
     check_pk(r, lambda n: getattr(o, n), XPK_NAMES, cross=True, floor=1e-6)
+
+
+@pytest.mark.parametrize('strategy', ['auto', 'atomic'])
+def test_rsd_fused_into_deposit(strategy):
+    """ParticlePk.step(pos, rsd=...) shifts the positions in place exactly like
+    pos_redshift_space (fused into the histogram pass on the tiled path, a pass of
+    its own otherwise) and deposits the shifted particles."""
+    from pylians_gb300.pipeline import ParticlePk
+    import pylians_gb300.redshift_space_library as RSL
+    rng = np.random.default_rng(33)
+    n, N, Lb = 1_200_000, 96, 500.0
+    pos = torch.from_numpy((rng.random((n, 3)) * Lb).astype(np.float32)).cuda()
+    vel = torch.from_numpy((rng.normal(size=(n, 3)) * 500.0).astype(np.float32)).cuda()
+    a, b = pos.clone(), pos.clone()
+    p1 = ParticlePk(N, Lb, 'CIC', axis=2, interlaced=True, strategy=strategy, max_particles=n)
+    p1.step(a, rsd=(vel, 100.0, 0.5, 2))
+    RSL.pos_redshift_space(b, vel, Lb, 100.0, 0.5, 2)
+    p2 = ParticlePk(N, Lb, 'CIC', axis=2, interlaced=True, strategy=strategy, max_particles=n)
+    p2.step(b)
+    assert torch.equal(a, b)
+    r1, r2 = p1.result(), p2.result()
+    np.testing.assert_array_equal(r1.Nmodes3D, r2.Nmodes3D)
+    np.testing.assert_allclose(r1.Pk, r2.Pk, rtol=1e-5, atol=1e-6 * np.abs(r2.Pk[:, 0]).max())
