@@ -455,7 +455,7 @@ def bench_learned():
     return out
 
 
-STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort')
+STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort', 'halo')
 
 # DRAM bytes per launch of the deposit kernel measured by ncu on the 512^3-particle,
 # 512^3-grid case (dram__bytes_read.sum + dram__bytes_write.sum; the summary and the

@@ -309,6 +309,7 @@ int pyl_xi_bin(const float *xi_grid, int dims, int axis, double *sums, void *str
 #define PYL_STAGE_PLACE_B 3   /* two-level placement, level B */
 #define PYL_STAGE_DEPOSIT 4   /* per-bin shared-memory deposit and write-out */
 #define PYL_STAGE_SORT 5      /* sorted strategy: keys, radix sort, runs, gather */
+#define PYL_STAGE_HALO 6      /* owned-cell write-out: halo blocks added into the next bins */
 #define PYL_STAGE_COUNT 8
 int pyl_stage_timing(int enable);
 int pyl_stage_times(double *ms_out, int n);

@@ -140,10 +140,10 @@ __host__ __device__ inline TileGeom tile_geom(int dims)
 
 // Tile keys are coarse-major: key = coarse * 64 + local, coarse = (tx/4, ty/4, tz/4),
 // local = (tx%4, ty%4, tz%4), so the 64 tiles of a coarse block are contiguous.
-__host__ __device__ inline unsigned tile_key_of(int tx, int ty, int tz, const TileGeom &g)
+__host__ __device__ inline unsigned tile_key_of(unsigned tx, unsigned ty, unsigned tz, const TileGeom &g)
 {
-    const unsigned coarse = ((unsigned)(tx >> 2) * g.nc + (ty >> 2)) * g.nc + (tz >> 2);
-    return coarse * 64u + (unsigned)(((tx & 3) << 4) | ((ty & 3) << 2) | (tz & 3));
+    const unsigned coarse = ((tx >> 2) * (unsigned)g.nc + (ty >> 2)) * (unsigned)g.nc + (tz >> 2);
+    return coarse * 64u + (((tx & 3u) << 4) | ((ty & 3u) << 2) | (tz & 3u));
 }
 
 __device__ __forceinline__ void tile_coords(long long key, const TileGeom &g, int &tx, int &ty, int &tz)
@@ -159,10 +159,13 @@ __device__ __forceinline__ void tile_coords(long long key, const TileGeom &g, in
 template <int MAS>
 __device__ __forceinline__ unsigned tile_key(const float *p, float inv, const TileGeom &g)
 {
-    const int cx = wrap_index(axis_first<MAS>(p[0], inv), g.dims);
-    const int cy = wrap_index(axis_first<MAS>(p[1], inv), g.dims);
-    const int cz = wrap_index(axis_first<MAS>(p[2], inv), g.dims);
-    return tile_key_of(cx / TB, cy / TB, cz / TB, g);
+    unsigned c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int f = axis_first<MAS>(p[a], inv);
+        c[a] = (unsigned)f < (unsigned)g.dims ? (unsigned)f : (unsigned)wrap_index(f, g.dims);   // rare: past the edge
+    }
+    return tile_key_of(c[0] / TB, c[1] / TB, c[2] / TB, g);
 }
 
 template <int MAS>
@@ -595,10 +598,10 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
             }
         }
         __syncthreads();
-        for (int sidx = threadIdx.x; sidx < c; sidx += blockDim.x) {
+        for (int sidx = threadIdx.x; sidx < c; sidx += LA_THREADS) {
             const unsigned co = sco[sidx];
-            const unsigned long long dst = (unsigned long long)gst[co] + (sidx - bcnt[co]);
-            if (dst < (unsigned long long)n) tmp[dst] = stage[sidx];
+            const unsigned dst = gst[co] + ((unsigned)sidx - bcnt[co]);      // n < 2^32
+            if (dst < (unsigned)n) tmp[dst] = stage[sidx];
         }
         __syncthreads();
     }
@@ -708,9 +711,9 @@ __global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
             }
         }
         __syncthreads();
-        for (int sidx = threadIdx.x; sidx < cnt; sidx += blockDim.x) {
+        for (int sidx = threadIdx.x; sidx < cnt; sidx += LBT_THREADS) {
             const int l = slo[sidx];
-            const unsigned long long dst = (unsigned long long)gst[l] + (sidx - bcnt[l]);
+            const unsigned dst = gst[l] + ((unsigned)sidx - bcnt[l]);
             if (dst < n) rec[dst] = stage[sidx];
         }
         __syncthreads();
@@ -932,11 +935,27 @@ int launch_atomic(const float *pos, const float *w, long long n, float *grid, fl
     return PYL_OK;
 }
 
+// Halo blocks of the owned-cell write-out (see Owned below): block h = 1..7, bits
+// (x, y, z) = (4, 2, 1), spans H layers along the axes whose bit is set and TB
+// cells along the others.
+__host__ __device__ constexpr int halo_ext(int H, int bit) { return bit ? H : TB; }
+__host__ __device__ constexpr int halo_block_size(int H, int h)
+{
+    return halo_ext(H, h & 4) * halo_ext(H, h & 2) * halo_ext(H, h & 1);
+}
+__host__ __device__ constexpr int halo_block_off(int H, int h)
+{
+    return h <= 1 ? 0 : halo_block_off(H, h - 1) + halo_block_size(H, h - 1);
+}
+__host__ __device__ constexpr int halo_cells(int H) { return halo_block_off(H, 8); }   // (TB + H)^3 - TB^3
+static_assert(halo_cells(2) == 34 * 34 * 34 - TB * TB * TB, "halo blocks cover the + side layers");
+
 struct TiledWs {
     unsigned n;                  // particles binned
     unsigned *hist, *total, *offsets;
     float4 *rec;                 // binned particles: x, y, z, weight
     float4 *tmp;                 // two-level placement: the coarse-block layout
+    float *halo;                 // owned-cell write-out: per-bin halo blocks
     unsigned long long *same;    // coherence count of the histogram pass
     int chunks;
     bool smem_hist;
@@ -945,7 +964,7 @@ struct TiledWs {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-TiledWs tiled_layout(void *base, long long n, int dims)
+TiledWs tiled_layout(void *base, long long n, int dims, size_t halo_floats = 0)
 {
     TileGeom g = tile_geom(dims);
     TiledWs ws;
@@ -965,8 +984,23 @@ TiledWs tiled_layout(void *base, long long n, int dims)
         ws.tmp = (float4 *)(b + off);
         off = align_up(off + sizeof(float4) * (size_t)n, 256);
     }
+    ws.halo = (float *)(b + off);
+    off = align_up(off + sizeof(float) * halo_floats, 256);
     ws.bytes = off;
     return ws;
+}
+
+// Grids whose bins tile them exactly take the owned-cell write-out.
+inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= 2 * TB; }
+
+// Floats of the owned-cell halo buffers of both grids (0 when the grid does not
+// take the owned-cell write-out, or a non-interlaced NGP deposit has no halo).
+inline size_t owned_halo_floats(int mas, int dims, bool inter)
+{
+    if (!owned_applies(dims)) return 0;
+    const int S = mas == PYL_MAS_NGP ? 1 : mas;
+    const int H = S - 1 + (inter ? 1 : 0);
+    return (size_t)(inter ? 2 : 1) * (size_t)tile_geom(dims).ntiles * (size_t)halo_cells(H);
 }
 
 // ---- full-bin fixed-point deposit (unweighted) ------------------------------
@@ -1058,128 +1092,334 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
 }
 
 // ---- TMA-staged full-bin deposit ----------------------------------------------
-// Same arithmetic and results as bin_deposit_fx_kernel, with three changes:
+// Same arithmetic and results as bin_deposit_fx_kernel, with these changes:
 //   * each pass streams the bin's records through two shared-memory buffers of
 //     R records filled by bulk copies (batch q+2 loads while batch q deposits);
 //   * the overflow test ORs the old values returned by the atomics and checks
 //     bit 31 (512.0) once per pass: a cell can only wrap past 1024 through an
 //     add whose old value is >= 1023, so a clear bit 31 proves no cell wrapped
 //     (a set one, from cells >= 512, conservatively redoes the pass in float32);
-//   * interior bins (halo inside the grid) write out without wrapping and with
-//     32-bit cell offsets.
+//   * the grid (plain or shifted) and the arithmetic (fixed point or float) of a
+//     pass are compile-time, and bin-local cells come from tile_key's first cell
+//     without the general wrap (taken only by cells past the grid edge);
+//   * the write-out walks the cells with incremental (x, y, z) indices, and
+//     interior bins (halo inside the grid) use 32-bit cell offsets.
 // Only CIC can produce negative or NaN weights (positions below 0, non-finite
 // positions); TSC and PCS weights are in [0, 1] for any input.
+
+// Bin-local cell of a particle along one axis (0 <= loc < TB for the first cell
+// of the plain grid, loc <= TB for the shifted one) and the axis weights.
+template <int MAS, int G>
+__device__ __forceinline__ int axis_local(float p, float inv, float halfcell, int dims, int o, float *C)
+{
+    if (G == 0) {
+        const int f = axis_weights<MAS>(p, inv, C);
+        const int loc = f - o;
+        return (unsigned)loc < (unsigned)TB ? loc : wrap_index(f, dims) - o;
+    }
+    const int f0 = axis_first<MAS>(p, inv);
+    const int f = axis_weights<MAS>(__fadd_rn(p, halfcell), inv, C);
+    const int loc0 = f0 - o;
+    return ((unsigned)loc0 < (unsigned)TB ? loc0 : wrap_index(f0, dims) - o) + (f > f0 ? 1 : 0);
+}
+
+struct FxStage {
+    const float4 *rec;
+    unsigned begin, cnt, nb;           // the bin's records and their batches
+    float4 *inb;                       // [2][R] staging buffers
+    unsigned long long *bar;           // one mbarrier per buffer
+    int *ok;
+};
+
+// One pass over the bin's records into shared memory.  Returns 1 when the pass
+// must be redone in float32, 0 when done, -1 after a failed staging wait.
+// q0: batches staged on the two barriers before this pass.
+template <int MAS, bool INTER, int R, int G, bool FLOAT>
+__device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, float inv, float halfcell, int dims,
+                                             const int *o, unsigned *smw)
+{
+    using FS = FxShape<MAS, INTER>;
+    constexpr int S = Support<MAS>::S, E = FS::E;
+    constexpr int PER = R / 1024;                       // records per thread and batch
+    uint4 *z4 = (uint4 *)smw;
+    for (int c = threadIdx.x; c < FS::SMEM / 16; c += 1024) z4[c] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0)
+        for (unsigned j = 0; j < 2 && j < sg.nb; j++) {
+            const unsigned q = q0 + j;
+            stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + j * R, 16u * min((unsigned)R, sg.cnt - j * R),
+                       &sg.bar[q & 1]);
+        }
+    __syncthreads();
+    unsigned bad = 0u, seen = 0u;
+    for (unsigned j = 0; j < sg.nb; j++) {
+        const unsigned q = q0 + j;
+        if (threadIdx.x == 0) *sg.ok = mbar_wait_bounded(&sg.bar[q & 1], (q >> 1) & 1u, &g_tma_error);
+        __syncthreads();
+        if (!*sg.ok) {
+            if (threadIdx.x == 0 && j + 1 < sg.nb)
+                mbar_wait_bounded(&sg.bar[(q + 1) & 1], ((q + 1) >> 1) & 1u, &g_tma_error);
+            return -1;
+        }
+        const float4 *in = sg.inb + (q & 1) * R;
+        const unsigned c = min((unsigned)R, sg.cnt - j * R);
+        float4 r[PER];
+#pragma unroll
+        for (int u = 0; u < PER; u++) r[u] = in[threadIdx.x + u * 1024];
+        __syncthreads();                                    // buffer consumed
+        if (threadIdx.x == 0 && j + 2 < sg.nb)
+            stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
+                       16u * min((unsigned)R, sg.cnt - (j + 2) * R), &sg.bar[q & 1]);
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            if (threadIdx.x + u * 1024 >= c) break;
+            float C[3][S];
+            const int base = (axis_local<MAS, G>(r[u].x, inv, halfcell, dims, o[0], C[0]) * E +
+                              axis_local<MAS, G>(r[u].y, inv, halfcell, dims, o[1], C[1])) * E +
+                             axis_local<MAS, G>(r[u].z, inv, halfcell, dims, o[2], C[2]);
+            if (FLOAT) {
+                float_scatter<MAS, E>((float *)smw, base, C);
+            } else {
+                if (MAS == PYL_MAS_CIC) bad |= (unsigned)!(C[0][1] >= 0.0f && C[1][1] >= 0.0f && C[2][1] >= 0.0f);
+                seen |= fx_scatter_or<MAS, E>(smw, base, C);
+            }
+        }
+    }
+    const int redo = __syncthreads_or((int)(bad | (seen >> 31)));
+    return (!FLOAT && redo) ? 1 : 0;
+}
+
+template <int MAS, bool FLOAT>
+__device__ __forceinline__ float fx_value(unsigned w)
+{
+    if (FLOAT) return __uint_as_float(w);
+    if (MAS == PYL_MAS_NGP) return __uint2float_rn(w);
+    return __fmul_rn(__uint2float_rn(w), FX_INV);
+}
+
+// Adds the bin's cells (with halo) into the grid; threads walk the flattened
+// cells 1024 apart with incremental (x, y, z) bin-local indices.
+template <int MAS, bool INTER, bool FLOAT>
+__device__ __forceinline__ void fx_write_out(const unsigned *smw, float *out, const int *o, int dims,
+                                             bool interior, float scale)
+{
+    using FS = FxShape<MAS, INTER>;
+    constexpr int E = FS::E, CELLS = FS::CELLS;
+    constexpr int DZ = 1024 % E, DY = (1024 / E) % E, DX = 1024 / (E * E);
+    int lz = threadIdx.x % E, ly = (threadIdx.x / E) % E, lx = threadIdx.x / (E * E);
+    if (interior) {
+        const unsigned gbase = ((unsigned)o[0] * dims + o[1]) * dims + o[2];
+        for (int c = threadIdx.x; c < CELLS; c += 1024) {
+            const unsigned w = smw[c];
+            if (w != 0u)
+                atomicAdd(out + (gbase + ((unsigned)lx * dims + ly) * dims + lz), __fmul_rn(fx_value<MAS, FLOAT>(w), scale));
+            lz += DZ;
+            ly += DY;
+            lx += DX;
+            if (lz >= E) { lz -= E; ly++; }
+            if (ly >= E) { ly -= E; lx++; }
+        }
+    } else {
+        const long long d = dims;
+        for (int c = threadIdx.x; c < CELLS; c += 1024) {
+            const unsigned w = smw[c];
+            if (w != 0u) {
+                const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d), gz = add_wrap(o[2], lz, d);
+                atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(fx_value<MAS, FLOAT>(w), scale));
+            }
+            lz += DZ;
+            ly += DY;
+            lx += DX;
+            if (lz >= E) { lz -= E; ly++; }
+            if (ly >= E) { ly -= E; lx++; }
+        }
+    }
+}
+
+// ---- owned-cell write-out --------------------------------------------------------
+// With dims a multiple of TB the bins tile the grid exactly, and every cell is the
+// core cell of one bin.  A bin stores its TB^3 core cells with plain coalesced
+// stores (fill + value for a fresh grid, old + value to accumulate) and its halo
+// cells (the + side layers that belong to the next bins) into a per-bin buffer;
+// halo_add_kernel then adds each bin's incoming halos into its core cells, in a
+// fixed order.  No global atomics, no separate fill pass, and every cell's sum is
+// formed in the same order on every run.
+// The halo of a bin is seven blocks, h = 1..7 with bits (x, y, z) = (4, 2, 1):
+// block h spans H layers along each axis whose bit is set and TB cells along the
+// others; bin-local cell (x + TB*hx, y + TB*hy, z + TB*hz) of block h is core cell
+// (x, y, z) of the bin offset by (hx, hy, hz).
+struct Owned {
+    bool on;             // false: atomic write-out of each bin with its halo
+    float *halo;         // per-bin halo blocks (plain grid, then shifted grid)
+    int fill_mode;       // 1: core = fill + value; 0: core = old + value
+    float fill;
+    long long stride;    // floats between the plain and the shifted grid's buffers
+};
+
+
+template <int MAS, bool INTER, bool FLOAT, int h>
+__device__ __forceinline__ void fx_store_halo_block(const unsigned *smw, float *halo_bin, float scale)
+{
+    constexpr int E = FxShape<MAS, INTER>::E, H = E - TB;
+    constexpr int EX = halo_ext(H, h & 4), EY = halo_ext(H, h & 2), EZ = halo_ext(H, h & 1);
+    constexpr int OX = (h & 4) ? TB : 0, OY = (h & 2) ? TB : 0, OZ = (h & 1) ? TB : 0;
+    constexpr int N = EX * EY * EZ, OFF = halo_block_off(H, h);
+    for (int i = threadIdx.x; i < N; i += 1024) {
+        const int z = i % EZ, y = (i / EZ) % EY, x = i / (EZ * EY);
+        const unsigned w = smw[((x + OX) * E + (y + OY)) * E + (z + OZ)];
+        halo_bin[OFF + i] = __fmul_rn(fx_value<MAS, FLOAT>(w), scale);
+    }
+}
+
+template <int MAS, bool INTER, bool FLOAT>
+__device__ __forceinline__ void fx_store_owned(const unsigned *smw, float *out, float *halo_bin, const int *o,
+                                               int dims, float scale, const Owned &ow)
+{
+    constexpr int E = FxShape<MAS, INTER>::E, H = E - TB;
+    // core: thread t holds (y, z) = (t / 32, t % 32) and walks x
+    const int ly = threadIdx.x >> 5, lz = threadIdx.x & 31;
+    const size_t plane = (size_t)dims * dims;
+    float *dst = out + ((size_t)o[0] * dims + (size_t)(o[1] + ly)) * dims + (o[2] + lz);
+    const unsigned *src = smw + ly * E + lz;
+    if (ow.fill_mode) {
+#pragma unroll 4
+        for (int lx = 0; lx < TB; lx++)
+            dst[lx * plane] = __fadd_rn(ow.fill, __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale));
+    } else {
+#pragma unroll 4
+        for (int lx = 0; lx < TB; lx++)
+            dst[lx * plane] = __fadd_rn(dst[lx * plane], __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale));
+    }
+    if constexpr (H > 0) {
+        fx_store_halo_block<MAS, INTER, FLOAT, 1>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 2>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 3>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 4>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 5>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 6>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 7>(smw, halo_bin, scale);
+    }
+}
+
+// Adds the halo blocks of the seven - side neighbours into each bin's core cells.
+// One CTA per bin and grid; every receiving cell (within H of the bin's low faces)
+// is read, summed with its incoming halo values in block order h = 1..7, and
+// written by one thread, so no atomics and a fixed order.  Rows with x < H or
+// y < H receive along their whole length (a warp per row); the remaining rows
+// receive only their first H cells (from the z block).
+template <int H>
+__global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid, float *__restrict__ grid2,
+                                                       const float *__restrict__ halo, long long stride, TileGeom g)
+{
+    constexpr int HC = halo_cells(H);
+    constexpr int ROWS_A = 2 * H * TB - H * H;          // rows (x, y) with x < H or y < H
+    constexpr int CELLS_B = (TB - H) * (TB - H) * H;    // first H cells of the other rows
+    __shared__ const float *src[8];
+    const int nt = g.nt;
+    const int gi = blockIdx.y;                          // 0: plain grid, 1: shifted grid
+    int tx, ty, tz;
+    tile_coords(blockIdx.x, g, tx, ty, tz);
+    if (tx >= nt || ty >= nt || tz >= nt) return;
+    float *out = gi ? grid2 : grid;
+    if (threadIdx.x < 8) {
+        const int h = threadIdx.x, hx = (h >> 2) & 1, hy = (h >> 1) & 1, hz = h & 1;
+        const unsigned key = tile_key_of((unsigned)((tx - hx + nt) % nt), (unsigned)((ty - hy + nt) % nt),
+                                         (unsigned)((tz - hz + nt) % nt), g);
+        src[h] = halo + gi * stride + (size_t)key * HC + halo_block_off(H, h);
+    }
+    __syncthreads();
+    const size_t dims = (size_t)g.dims;
+    float *bin = out + ((size_t)tx * TB * dims + (size_t)ty * TB) * dims + (size_t)tz * TB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < ROWS_A; r += 8) {
+        int x, y;
+        if (r < H * TB) { x = r / TB; y = r % TB; }
+        else { x = H + (r - H * TB) / H; y = (r - H * TB) % H; }
+        const int z = lane;
+        const int low = (x < H ? 4 : 0) | (y < H ? 2 : 0) | (z < H ? 1 : 0);
+        float *c = bin + ((size_t)x * dims + y) * dims + z;
+        float v = *c;
+#pragma unroll
+        for (int h = 1; h < 8; h++) {
+            if (h & ~low) continue;
+            const int EY = (h & 2) ? H : TB, EZ = (h & 1) ? H : TB;
+            v = __fadd_rn(v, src[h][(x * EY + y) * EZ + z]);
+        }
+        *c = v;
+    }
+    for (int i = threadIdx.x; i < CELLS_B; i += 256) {
+        const int z = i % H, row = i / H;
+        const int x = H + row / (TB - H), y = H + row % (TB - H);
+        float *c = bin + ((size_t)x * dims + y) * dims + z;
+        *c = __fadd_rn(*c, src[1][(x * TB + y) * H + z]);
+    }
+}
+
+// Both arithmetic modes of one grid: fixed point, float32 if that overflowed.
+// Returns false after a failed staging wait.
+template <int MAS, bool INTER, int R, int G>
+__device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float inv, float halfcell, int dims,
+                                        const int *o, unsigned *smw, float *out, bool interior, float scale,
+                                        const Owned &ow, float *halo_bin)
+{
+    int st = fx_accumulate<MAS, INTER, R, G, false>(sg, q0, inv, halfcell, dims, o, smw);
+    if (st < 0) return false;
+    q0 += sg.nb;
+    if (st == 0) {
+        if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow);
+        else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
+    } else {
+        if (fx_accumulate<MAS, INTER, R, G, true>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
+        q0 += sg.nb;
+        if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, scale, ow);
+        else fx_write_out<MAS, INTER, true>(smw, out, o, dims, interior, scale);
+    }
+    __syncthreads();                                        // cells read before the next pass zeroes them
+    return true;
+}
+
 template <int MAS, bool INTER, int R>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec)
+    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
+    Owned ow)
 {
     using FS = FxShape<MAS, INTER>;
-    constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
-    constexpr int PER = R / 1024;                       // records per thread and batch
+    constexpr int E = FS::E;
     extern __shared__ __align__(16) unsigned smw[];
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ int s_ok;
-    float *facc = (float *)smw;
-    float4 *inb = (float4 *)(smw + FS::SMEM / 4);       // [2][R]
     const long long tile = blockIdx.x;
     const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
-    if (begin == end) return;
-    const float scale = out_scale(sc);
     int tx, ty, tz;
     tile_coords(tile, g, tx, ty, tz);
+    if (tx >= g.nt || ty >= g.nt || tz >= g.nt) return;       // key past the grid: no cells
+    if (begin == end && !ow.on) return;                         // owned cells are stored even when empty
+    const float scale = out_scale(sc);
     const int o[3] = {tx * TB, ty * TB, tz * TB};
     const int dims = g.dims;
     const bool interior = o[0] + E <= dims && o[1] + E <= dims && o[2] + E <= dims &&
                           (long long)dims * dims * dims < (1LL << 32);
-    const unsigned cnt = end - begin;
-    const unsigned nb = (cnt + R - 1) / R;
+    FxStage sg;
+    sg.rec = rec;
+    sg.begin = begin;
+    sg.cnt = end - begin;
+    sg.nb = (sg.cnt + R - 1) / R;
+    sg.inb = (float4 *)(smw + FS::SMEM / 4);
+    sg.bar = bar;
+    sg.ok = &s_ok;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_fence_init();
     }
     __syncthreads();
-    unsigned q0 = 0;                                    // batches issued by this CTA so far
-    for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
-        for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
-            uint4 *z4 = (uint4 *)smw;
-            for (int c = threadIdx.x; c < FS::SMEM / 16; c += 1024) z4[c] = make_uint4(0u, 0u, 0u, 0u);
-            if (threadIdx.x == 0)
-                for (unsigned j = 0; j < 2 && j < nb; j++) {
-                    const unsigned q = q0 + j;
-                    stage_copy(inb + (q & 1) * R, rec + begin + j * R, 16u * min((unsigned)R, cnt - j * R),
-                               &bar[q & 1]);
-                }
-            __syncthreads();
-            unsigned bad = 0u, seen = 0u;
-            for (unsigned j = 0; j < nb; j++) {
-                const unsigned q = q0 + j;
-                if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[q & 1], (q >> 1) & 1u, &g_tma_error);
-                __syncthreads();
-                if (!s_ok) {
-                    if (threadIdx.x == 0 && j + 1 < nb)
-                        mbar_wait_bounded(&bar[(q + 1) & 1], ((q + 1) >> 1) & 1u, &g_tma_error);
-                    return;
-                }
-                const float4 *in = inb + (q & 1) * R;
-                const unsigned c = min((unsigned)R, cnt - j * R);
-                float4 r[PER];
-#pragma unroll
-                for (int u = 0; u < PER; u++) r[u] = in[threadIdx.x + u * 1024];
-                __syncthreads();                                    // buffer consumed
-                if (threadIdx.x == 0 && j + 2 < nb)
-                    stage_copy(inb + (q & 1) * R, rec + begin + (j + 2) * R, 16u * min((unsigned)R, cnt - (j + 2) * R),
-                               &bar[q & 1]);
-#pragma unroll
-                for (int u = 0; u < PER; u++) {
-                    if (threadIdx.x + u * 1024 >= c) break;
-                    float C[3][S];
-                    const int b0 = pass ? fx_support<MAS, 1, E>(r[u], inv, halfcell, dims, o, C)
-                                        : fx_support<MAS, 0, E>(r[u], inv, halfcell, dims, o, C);
-                    if (mode == 0) {
-                        if (MAS == PYL_MAS_CIC) bad |= (unsigned)!(C[0][1] >= 0.0f && C[1][1] >= 0.0f && C[2][1] >= 0.0f);
-                        seen |= fx_scatter_or<MAS, E>(smw, b0, C);
-                    } else {
-                        float_scatter<MAS, E>(facc, b0, C);
-                    }
-                }
-            }
-            q0 += nb;
-            if (__syncthreads_or((int)(bad | (seen >> 31))) && mode == 0) {   // redo this pass in float32
-                __syncthreads();
-                continue;
-            }
-            float *out = pass == 0 ? grid : grid2;
-            if (interior) {
-                const unsigned gbase = ((unsigned)o[0] * dims + o[1]) * dims + o[2];
-                for (int c = threadIdx.x; c < CELLS; c += 1024) {
-                    const unsigned w = smw[c];
-                    if (w == 0u) continue;
-                    const float v = mode == 1 ? __uint_as_float(w)
-                                              : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
-                                                                    : __fmul_rn(__uint2float_rn(w), FX_INV));
-                    const unsigned lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                    atomicAdd(out + (gbase + (lx * dims + ly) * dims + lz), __fmul_rn(v, scale));
-                }
-            } else {
-                const long long d = dims;
-                for (int c = threadIdx.x; c < CELLS; c += 1024) {
-                    const unsigned w = smw[c];
-                    if (w == 0u) continue;
-                    const float v = mode == 1 ? __uint_as_float(w)
-                                              : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
-                                                                    : __fmul_rn(__uint2float_rn(w), FX_INV));
-                    const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                    const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
-                                    gz = add_wrap(o[2], lz, d);
-                    atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
-                }
-            }
-            __syncthreads();
-            break;
-        }
-    }
+    unsigned q0 = 0;                                    // batches staged by this CTA so far
+    constexpr int HC = halo_cells(FS::H);
+    float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
+    if (!fx_grid<MAS, INTER, R, 0>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb)) return;
+    if (INTER)
+        fx_grid<MAS, INTER, R, 1>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
+                                  hb ? hb + ow.stride : nullptr);
 }
 
 // Records per staging buffer that fit beside the bin (0: no staging).
@@ -1192,7 +1432,7 @@ constexpr int fx_tma_batch()
 
 template <int MAS, bool I>
 int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                      float *grid2, OutScale sc, cudaStream_t st)
+                      float *grid2, OutScale sc, cudaStream_t st, const Owned &ow = Owned{false, nullptr, 0, 0.0f, 0})
 {
     using FS = FxShape<MAS, I>;
     constexpr int R = fx_tma_batch<MAS, I>();
@@ -1201,9 +1441,25 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
         static size_t done_t = 0;
         PYL_CUDA(ensure_smem(kern, smem, &done_t));
-        kern<<<(unsigned)g.ntiles, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n);
+        kern<<<(unsigned)g.ntiles, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n,
+                                                     ow);
         PYL_LAUNCH_CHECK();
+        if constexpr (FS::H > 0) {
+            if (ow.on) {
+                stage_mark(PYL_STAGE_DEPOSIT, false, st);
+                stage_mark(PYL_STAGE_HALO, true, st);
+                halo_add_kernel<FS::H><<<dim3((unsigned)g.ntiles, I ? 2 : 1), 256, 0, st>>>(grid, grid2, ow.halo,
+                                                                                          ow.stride, g);
+                PYL_LAUNCH_CHECK();
+                stage_mark(PYL_STAGE_HALO, false, st);
+                stage_mark(PYL_STAGE_DEPOSIT, true, st);
+            }
+        }
         return PYL_OK;
+    }
+    if (ow.on) {
+        set_error("owned-cell write-out needs the staged deposit");
+        return PYL_ERR_UNSUPPORTED;
     }
     auto kern = bin_deposit_fx_kernel<MAS, I>;
     static size_t done = 0;
@@ -1230,11 +1486,23 @@ int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, flo
 template <int MAS>
 int launch_tiled(const float *pos, const float *w, long long n, float *grid, float *grid2,
                  int dims, float inv, float halfcell, void *workspace, OutScale sc, cudaStream_t st,
-                 const RsdArgs *rsd = nullptr)
+                 const RsdArgs *rsd = nullptr, Owned ow = Owned{false, nullptr, 0, 0.0f, 0})
 {
+    if (ow.on && (w || !FxShape<MAS, true>::FITS)) {
+        set_error("owned-cell write-out is for unweighted fixed-point deposits");
+        return PYL_ERR_INVALID;
+    }
     TileGeom g = tile_geom(dims);
     TiledWs ws = tiled_layout(workspace, n, dims);
     const int T = (int)g.ntiles;
+    if (ow.on) {
+        if (!owned_applies(dims)) {
+            set_error("owned-cell write-out needs dims a multiple of 32");
+            return PYL_ERR_INVALID;
+        }
+        ow.halo = ws.halo;
+        ow.stride = (long long)g.ntiles * halo_cells(Support<MAS>::S - 1 + (grid2 ? 1 : 0));
+    }
     if (ws.smem_hist) {
         const int C = ws.chunks;
         // chunks start on multiples of 4 particles (48 bytes) for the bulk copies
@@ -1357,10 +1625,10 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
     if (w) rc = grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
                       : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
     else if (grid2) rc = FxShape<MAS, true>::FITS
-                             ? launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                             ? launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st, ow)
                              : launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
     else rc = FxShape<MAS, false>::FITS
-                  ? launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
+                  ? launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st, ow)
                   : launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
     stage_mark(PYL_STAGE_DEPOSIT, false, st);
     return rc;
@@ -1384,14 +1652,13 @@ using namespace pyl;
 extern "C" size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims, int mas,
                                         int strategy, int interlaced)
 {
-    (void)mas; (void)interlaced;
     if (n_particles < 0 || dims <= 0) return 0;
     const int s = pick_strategy(strategy, ndim, dims, n_particles);
     // + 256 bytes at the end: the mass sum and scale of pyl_ma_overdensity
     if (s == PYL_STRATEGY_SORTED && ndim == 3 && sorted_supported(n_particles, dims))
         return sorted_workspace_bytes(n_particles, dims) + 256;
     if (s == PYL_STRATEGY_TILED && ndim == 3)
-        return tiled_layout(nullptr, n_particles, dims).bytes + 256;
+        return tiled_layout(nullptr, n_particles, dims, owned_halo_floats(mas, dims, interlaced != 0)).bytes + 256;
     return 256;
 }
 
@@ -1426,12 +1693,17 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
                              nullptr, true, st);
     }
     if (s == PYL_STRATEGY_TILED && (ndim != 3 || n > 0xFFFFFFF0ll)) s = PYL_STRATEGY_ATOMIC;
+    Owned ow{false, nullptr, 0, 0.0f, 0};
     if (s == PYL_STRATEGY_TILED) {
         const size_t need = tiled_layout(nullptr, n, dims).bytes;
         if (workspace_bytes < need || workspace == nullptr) {
             set_error("pyl_ma: tiled strategy needs " + std::to_string(need) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
         }
+        // owned-cell write-out when the workspace also holds the halo blocks
+        const size_t need_owned =
+            tiled_layout(nullptr, n, dims, owned_halo_floats(mas, dims, grid_interlaced != nullptr)).bytes;
+        ow.on = owned_applies(dims) && weights == nullptr && workspace_bytes >= need_owned;
     }
     int rc = PYL_OK;
     if (n > 0) {
@@ -1439,7 +1711,7 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
     case M:                                                                                          \
         if (s == PYL_STRATEGY_TILED)                                                                 \
             rc = launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,        \
-                                 workspace, sc, st);                                                 \
+                                 workspace, sc, st, nullptr, ow);                                    \
         else if (ndim == 3)                                                                          \
             rc = launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st); \
         else                                                                                         \
@@ -1534,15 +1806,19 @@ int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     int s = pick_strategy(strategy, 3, dims, n);
     if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
-    const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
-    stage_mark(PYL_STAGE_FILL, true, st);
-    fill_kernel<<<blocks, 256, 0, st>>>(grid, cells, -1.0f);
-    PYL_LAUNCH_CHECK();
-    if (grid_interlaced) {
-        fill_kernel<<<blocks, 256, 0, st>>>(grid_interlaced, cells, -1.0f);
+    // the owned-cell write-out stores -1 + value into every cell: no fill pass
+    const Owned ow{s == PYL_STRATEGY_TILED && weights == nullptr && owned_applies(dims), nullptr, 1, -1.0f, 0};
+    if (!ow.on) {
+        const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
+        stage_mark(PYL_STAGE_FILL, true, st);
+        fill_kernel<<<blocks, 256, 0, st>>>(grid, cells, -1.0f);
         PYL_LAUNCH_CHECK();
+        if (grid_interlaced) {
+            fill_kernel<<<blocks, 256, 0, st>>>(grid_interlaced, cells, -1.0f);
+            PYL_LAUNCH_CHECK();
+        }
+        stage_mark(PYL_STAGE_FILL, false, st);
     }
-    stage_mark(PYL_STAGE_FILL, false, st);
     const RsdArgs *fused = nullptr;
     if (rsd) {
         if (s == PYL_STRATEGY_TILED && tiled_rsd_fusable(pos, dims)) {
@@ -1561,7 +1837,7 @@ int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float
     case M:                                                                                          \
         return s == PYL_STRATEGY_TILED                                                               \
                    ? launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,   \
-                                     workspace, sc, st, fused)                                       \
+                                     workspace, sc, st, fused, ow)                                   \
                    : launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
         PYL_OD(PYL_MAS_NGP)
         PYL_OD(PYL_MAS_CIC)

@@ -237,6 +237,41 @@ def test_coherent_placement_matches_atomic(MASL, N):
             del a1, a2, b1, b2
 
 
+@pytest.mark.parametrize('mas', MAS_LIST)
+@pytest.mark.parametrize('inter', [False, True])
+def test_owned_cell_write_out_accumulates(MASL, mas, inter):
+    """On grids that are a whole number of 32-cell bins the tiled deposit stores each
+    bin's own cells (old value + bin sum) and passes its halo to the next bins
+    through a buffer.  It must add onto a non-zero grid exactly like the atomic
+    strategy, wrap the halos of the last bins onto the first, and give identical
+    bits on a second run (the halo sums are added in a fixed order)."""
+    rng = np.random.default_rng(31)
+    N, L, n = 96, 1000.0, 2_000_000
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    # 100 particles in the last cells of the grid along x and z, the first along y:
+    # their halos wrap onto bins at the other faces
+    corner = rng.random((100, 3)).astype(np.float32) * np.float32(2 * L / N)
+    corner[:, 0] = np.float32(L) - corner[:, 0] * np.float32(0.999)
+    corner[:, 2] = np.float32(L) - corner[:, 2] * np.float32(0.999)
+    pos[:100] = torch.from_numpy(corner % np.float32(L)).cuda()
+    base = torch.from_numpy((rng.random((N, N, N)) * 5).astype(np.float32)).cuda()
+    if mas == 'NGP':
+        base = torch.floor(base)        # integer sums: any order gives the same bits
+    runs = []
+    for strategy in ('atomic', 'tiled', 'tiled'):
+        a = base.clone()
+        b = base.clone() if inter else None
+        MASL.MA(pos, a, L, mas, interlaced=b, strategy=strategy)
+        runs.append((a, b))
+    for i in range(2 if inter else 1):
+        ref, got, again = runs[0][i], runs[1][i], runs[2][i]
+        if mas == 'NGP':
+            assert torch.equal(ref, got)
+        else:
+            assert (ref - got).abs().max().item() <= 2e-6 * ref.abs().max().item()
+        assert torch.equal(got, again)
+
+
 @pytest.mark.parametrize('mas', ['CIC', 'TSC', 'PCS'])
 def test_fixed_point_overflow_falls_back(MASL, mas):
     """The tiled deposit accumulates a bin in 10.22 fixed point (cell sums below 1024).

@@ -202,14 +202,17 @@ def test_overdensity_deposit_matches_two_pass(weighted):
 
 
 @pytest.mark.parametrize('mas', ['NGP', 'CIC', 'TSC', 'PCS'])
-def test_overdensity_owned_cells_with_empty_bins(mas):
-    """The staged tiled deposit stores its bins' own cells itself (only the halo shells
-    are pre-filled with -1): particles packed into one corner of a ragged 200^3 grid
-    leave most bins empty, which must still read -1, and every cell must equal the
-    two-pass MA + delta = n/mean - 1, plain and interlaced."""
+@pytest.mark.parametrize('N', [200, 224])
+def test_overdensity_owned_cells_with_empty_bins(mas, N):
+    """Particles packed into one corner leave most bins empty, which must still read
+    -1, and every cell must equal the two-pass MA + delta = n/mean - 1, plain and
+    interlaced.  224^3 (a multiple of the 32-cell bin) takes the owned-cell write-out:
+    every bin, empty or not, stores -1 + its sum into its own cells and its halo
+    into a buffer that a second kernel adds to the next bins; the ragged 200^3 grid
+    fills with -1 and adds every bin with its halo atomically."""
     import pylians_gb300.MAS_library as MASL
     rng = np.random.default_rng(23)
-    N, L, n = 200, 1000.0, 1_500_000
+    L, n = 1000.0, 1_500_000
     pos = torch.from_numpy((rng.random((n, 3)) * 260.0 + 30.0).astype(np.float32)).cuda()
     d1 = torch.full((N, N, N), 7.0, device='cuda'); d2 = torch.full((N, N, N), 7.0, device='cuda')
     MASL.overdensity_device(pos, d1, L, mas, grid_interlaced=d2, strategy='tiled')
