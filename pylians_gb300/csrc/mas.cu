@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_kernel(
 // other copy.
 __device__ unsigned g_tma_error;
 
-constexpr int HT_BATCH = 2048;                  // histogram batch (particles)
-constexpr int HT_NBUF = 4;                      // batches in flight
+constexpr int HT_BATCH = 4096;                  // histogram batch (particles)
+constexpr int HT_NBUF = 2;                      // batches in flight
 
 // Particles of batch j wholly inside its bulk copy.
 __device__ __forceinline__ int staged_full(int cnt) { return (int)(((long long)cnt * 12 & ~15LL) / 12); }
@@ -990,8 +990,11 @@ TiledWs tiled_layout(void *base, long long n, int dims, size_t halo_floats = 0)
     return ws;
 }
 
-// Grids whose bins tile them exactly take the owned-cell write-out.
-inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= 2 * TB; }
+// Grids whose bins tile them exactly take the owned-cell write-out from 1024^3 up;
+// below that the fill pass plus atomic write-out measures as fast or faster (the
+// four-bin CTAs of the owned deposit leave too few CTAs to balance 152 SMs).
+constexpr int OWNED_MIN_DIMS = 1024;
+inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= OWNED_MIN_DIMS; }
 
 // Floats of the owned-cell halo buffers of both grids (0 when the grid does not
 // take the owned-cell write-out, or a non-interlaced NGP deposit has no halo).
@@ -1247,6 +1250,8 @@ __device__ __forceinline__ void fx_write_out(const unsigned *smw, float *out, co
 // block h spans H layers along each axis whose bit is set and TB cells along the
 // others; bin-local cell (x + TB*hx, y + TB*hy, z + TB*hz) of block h is core cell
 // (x, y, z) of the bin offset by (hx, hy, hz).
+constexpr int OWN_Z = 4;   // bins along z per CTA of the owned-cell deposit (one coarse block)
+
 struct Owned {
     bool on;             // false: atomic write-out of each bin with its halo
     float *halo;         // per-bin halo blocks (plain grid, then shifted grid)
@@ -1256,8 +1261,19 @@ struct Owned {
 };
 
 
+// The + z layers of a bin (its halo blocks 1, 3, 5, 7) land on the z < H layers of
+// the next bin along z (core cells, and blocks 2, 4, 6).  carry: those four blocks
+// of the bin run just before by this CTA, copied into shared memory in this order
+// (offsets carry_off), or null.
+__host__ __device__ constexpr int carry_off(int H, int h)
+{
+    return h == 1 ? 0 : h == 3 ? TB * TB * H : h == 5 ? TB * TB * H + TB * H * H : TB * TB * H + 2 * TB * H * H;
+}
+__host__ __device__ constexpr int carry_floats(int H) { return carry_off(H, 7) + H * H * H; }
+
 template <int MAS, bool INTER, bool FLOAT, int h>
-__device__ __forceinline__ void fx_store_halo_block(const unsigned *smw, float *halo_bin, float scale)
+__device__ __forceinline__ void fx_store_halo_block(const unsigned *smw, float *halo_bin, float scale,
+                                                    const float *carry)
 {
     constexpr int E = FxShape<MAS, INTER>::E, H = E - TB;
     constexpr int EX = halo_ext(H, h & 4), EY = halo_ext(H, h & 2), EZ = halo_ext(H, h & 1);
@@ -1266,46 +1282,74 @@ __device__ __forceinline__ void fx_store_halo_block(const unsigned *smw, float *
     for (int i = threadIdx.x; i < N; i += 1024) {
         const int z = i % EZ, y = (i / EZ) % EY, x = i / (EZ * EY);
         const unsigned w = smw[((x + OX) * E + (y + OY)) * E + (z + OZ)];
-        halo_bin[OFF + i] = __fmul_rn(fx_value<MAS, FLOAT>(w), scale);
+        float v = __fmul_rn(fx_value<MAS, FLOAT>(w), scale);
+        if constexpr (!(h & 1)) {
+            if (carry && z < H) v = __fadd_rn(v, carry[carry_off(H, h | 1) + (x * EY + y) * H + z]);
+        }
+        halo_bin[OFF + i] = v;
     }
 }
 
+// cs: the idle staging buffers (no bulk copy in flight during a write-out), where
+// the carried blocks of prev are gathered before use.
 template <int MAS, bool INTER, bool FLOAT>
 __device__ __forceinline__ void fx_store_owned(const unsigned *smw, float *out, float *halo_bin, const int *o,
-                                               int dims, float scale, const Owned &ow)
+                                               int dims, float scale, const Owned &ow, const float *prev,
+                                               float *cs)
 {
     constexpr int E = FxShape<MAS, INTER>::E, H = E - TB;
-    // core: thread t holds (y, z) = (t / 32, t % 32) and walks x
+    const float *carry = nullptr;
+    if constexpr (H > 0) {
+        if (prev) {
+            for (int i = threadIdx.x; i < carry_floats(H); i += 1024) {
+                const int h = i < carry_off(H, 3) ? 1 : i < carry_off(H, 5) ? 3 : i < carry_off(H, 7) ? 5 : 7;
+                cs[i] = prev[halo_block_off(H, h) + (i - carry_off(H, h))];
+            }
+            __syncthreads();
+            carry = cs;
+        }
+    }
+    // core: thread t holds (y, z) = (t / 32, t % 32) and walks x; z < H adds the
+    // carried block 1
     const int ly = threadIdx.x >> 5, lz = threadIdx.x & 31;
     const size_t plane = (size_t)dims * dims;
     float *dst = out + ((size_t)o[0] * dims + (size_t)(o[1] + ly)) * dims + (o[2] + lz);
     const unsigned *src = smw + ly * E + lz;
+    const float *cz = (carry && lz < H) ? carry + ly * H + lz : nullptr;
     if (ow.fill_mode) {
 #pragma unroll 4
-        for (int lx = 0; lx < TB; lx++)
-            dst[lx * plane] = __fadd_rn(ow.fill, __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale));
+        for (int lx = 0; lx < TB; lx++) {
+            float v = __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale);
+            if (cz) v = __fadd_rn(v, cz[lx * TB * H]);
+            dst[lx * plane] = __fadd_rn(ow.fill, v);
+        }
     } else {
 #pragma unroll 4
-        for (int lx = 0; lx < TB; lx++)
-            dst[lx * plane] = __fadd_rn(dst[lx * plane], __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale));
+        for (int lx = 0; lx < TB; lx++) {
+            float v = __fmul_rn(fx_value<MAS, FLOAT>(src[lx * E * E]), scale);
+            if (cz) v = __fadd_rn(v, cz[lx * TB * H]);
+            dst[lx * plane] = __fadd_rn(dst[lx * plane], v);
+        }
     }
     if constexpr (H > 0) {
-        fx_store_halo_block<MAS, INTER, FLOAT, 1>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 2>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 3>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 4>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 5>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 6>(smw, halo_bin, scale);
-        fx_store_halo_block<MAS, INTER, FLOAT, 7>(smw, halo_bin, scale);
+        fx_store_halo_block<MAS, INTER, FLOAT, 1>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 2>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 3>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 4>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 5>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 6>(smw, halo_bin, scale, carry);
+        fx_store_halo_block<MAS, INTER, FLOAT, 7>(smw, halo_bin, scale, carry);
     }
 }
 
-// Adds the halo blocks of the seven - side neighbours into each bin's core cells.
-// One CTA per bin and grid; every receiving cell (within H of the bin's low faces)
-// is read, summed with its incoming halo values in block order h = 1..7, and
-// written by one thread, so no atomics and a fixed order.  Rows with x < H or
-// y < H receive along their whole length (a warp per row); the remaining rows
-// receive only their first H cells (from the z block).
+// Adds the halo blocks of the - side neighbours into each bin's core cells.  The
+// deposit already carried the + z layers of a bin into the next bin of its CTA,
+// so only the first bin of each OWN_Z group along z takes the blocks with the z
+// bit set (1, 3, 5, 7); every bin takes blocks 2, 4, 6.  One CTA per bin and
+// grid; every receiving cell is read, summed with its incoming halo values in
+// block order, and written by one thread, so no atomics and a fixed order.  Rows
+// with x < H or y < H receive along their whole length (a warp per row); the
+// first H cells of the other rows receive only from the z block.
 template <int H>
 __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid, float *__restrict__ grid2,
                                                        const float *__restrict__ halo, long long stride, TileGeom g)
@@ -1330,12 +1374,13 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
     const size_t dims = (size_t)g.dims;
     float *bin = out + ((size_t)tx * TB * dims + (size_t)ty * TB) * dims + (size_t)tz * TB;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int zmask = tz % OWN_Z == 0 ? 7 : 6;          // blocks taken: all, or those without the z bit
     for (int r = warp; r < ROWS_A; r += 8) {
         int x, y;
         if (r < H * TB) { x = r / TB; y = r % TB; }
         else { x = H + (r - H * TB) / H; y = (r - H * TB) % H; }
         const int z = lane;
-        const int low = (x < H ? 4 : 0) | (y < H ? 2 : 0) | (z < H ? 1 : 0);
+        const int low = ((x < H ? 4 : 0) | (y < H ? 2 : 0) | (z < H ? 1 : 0)) & zmask;
         float *c = bin + ((size_t)x * dims + y) * dims + z;
         float v = *c;
 #pragma unroll
@@ -1346,7 +1391,7 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
         }
         *c = v;
     }
-    for (int i = threadIdx.x; i < CELLS_B; i += 256) {
+    for (int i = threadIdx.x; i < (zmask == 7 ? CELLS_B : 0); i += 256) {
         const int z = i % H, row = i / H;
         const int x = H + row / (TB - H), y = H + row % (TB - H);
         float *c = bin + ((size_t)x * dims + y) * dims + z;
@@ -1359,18 +1404,18 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
 template <int MAS, bool INTER, int R, int G>
 __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float inv, float halfcell, int dims,
                                         const int *o, unsigned *smw, float *out, bool interior, float scale,
-                                        const Owned &ow, float *halo_bin)
+                                        const Owned &ow, float *halo_bin, const float *prev)
 {
     int st = fx_accumulate<MAS, INTER, R, G, false>(sg, q0, inv, halfcell, dims, o, smw);
     if (st < 0) return false;
     q0 += sg.nb;
     if (st == 0) {
-        if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow);
+        if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
     } else {
         if (fx_accumulate<MAS, INTER, R, G, true>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
         q0 += sg.nb;
-        if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, scale, ow);
+        if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, true>(smw, out, o, dims, interior, scale);
     }
     __syncthreads();                                        // cells read before the next pass zeroes them
@@ -1388,25 +1433,9 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     extern __shared__ __align__(16) unsigned smw[];
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ int s_ok;
-    const long long tile = blockIdx.x;
-    const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
-    int tx, ty, tz;
-    tile_coords(tile, g, tx, ty, tz);
-    if (tx >= g.nt || ty >= g.nt || tz >= g.nt) return;       // key past the grid: no cells
-    if (begin == end && !ow.on) return;                         // owned cells are stored even when empty
     const float scale = out_scale(sc);
-    const int o[3] = {tx * TB, ty * TB, tz * TB};
     const int dims = g.dims;
-    const bool interior = o[0] + E <= dims && o[1] + E <= dims && o[2] + E <= dims &&
-                          (long long)dims * dims * dims < (1LL << 32);
-    FxStage sg;
-    sg.rec = rec;
-    sg.begin = begin;
-    sg.cnt = end - begin;
-    sg.nb = (sg.cnt + R - 1) / R;
-    sg.inb = (float4 *)(smw + FS::SMEM / 4);
-    sg.bar = bar;
-    sg.ok = &s_ok;
+    constexpr int HC = halo_cells(FS::H);
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -1414,12 +1443,38 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     }
     __syncthreads();
     unsigned q0 = 0;                                    // batches staged by this CTA so far
-    constexpr int HC = halo_cells(FS::H);
-    float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
-    if (!fx_grid<MAS, INTER, R, 0>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb)) return;
-    if (INTER)
-        fx_grid<MAS, INTER, R, 1>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
-                                  hb ? hb + ow.stride : nullptr);
+    // owned-cell write-out: the OWN_Z bins of a coarse block along z (consecutive
+    // keys) one after the other, each taking the + z layers of the one before
+    const int nbins = ow.on ? OWN_Z : 1;
+    bool have_prev = false;
+    for (int k = 0; k < nbins; k++) {
+        const long long tile = (long long)blockIdx.x * nbins + k;
+        const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
+        int tx, ty, tz;
+        tile_coords(tile, g, tx, ty, tz);
+        if (tx >= g.nt || ty >= g.nt || tz >= g.nt) break;     // keys past the grid: no cells
+        if (begin == end && !ow.on) return;                     // owned cells are stored even when empty
+        const int o[3] = {tx * TB, ty * TB, tz * TB};
+        const bool interior = o[0] + E <= dims && o[1] + E <= dims && o[2] + E <= dims &&
+                              (long long)dims * dims * dims < (1LL << 32);
+        FxStage sg;
+        sg.rec = rec;
+        sg.begin = begin;
+        sg.cnt = end - begin;
+        sg.nb = (sg.cnt + R - 1) / R;
+        sg.inb = (float4 *)(smw + FS::SMEM / 4);
+        sg.bar = bar;
+        sg.ok = &s_ok;
+        float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
+        const float *prev = have_prev && hb ? hb - HC : nullptr;
+        if (!fx_grid<MAS, INTER, R, 0>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
+            return;
+        if (INTER &&
+            !fx_grid<MAS, INTER, R, 1>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
+                                       hb ? hb + ow.stride : nullptr, prev ? prev + ow.stride : nullptr))
+            return;
+        have_prev = true;
+    }
 }
 
 // Records per staging buffer that fit beside the bin (0: no staging).
@@ -1436,13 +1491,14 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
 {
     using FS = FxShape<MAS, I>;
     constexpr int R = fx_tma_batch<MAS, I>();
+    static_assert(R == 0 || carry_floats(FS::H) * 4 <= 2 * R * 16, "carried blocks fit the staging buffers");
     if (R > 0) {
         auto kern = bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024)>;
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
         static size_t done_t = 0;
         PYL_CUDA(ensure_smem(kern, smem, &done_t));
-        kern<<<(unsigned)g.ntiles, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n,
-                                                     ow);
+        const unsigned ctas = (unsigned)(ow.on ? g.ntiles / OWN_Z : g.ntiles);
+        kern<<<ctas, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n, ow);
         PYL_LAUNCH_CHECK();
         if constexpr (FS::H > 0) {
             if (ow.on) {

@@ -381,8 +381,12 @@ inline int seq_chunk(int nz)
     return c + (c & 1);
 }
 
+// umulhi(kz, magic) = kz / chunk for the kz < 2^13 of any grid here
+inline unsigned seq_chunk_magic(int chunk) { return (unsigned)((0x100000000ull + chunk - 1) / chunk); }
+
+
 template <bool INTER, int AXIS>
-__global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk)
+__global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
     extern __shared__ float sm[];
     const PkDims d = a.d;
@@ -444,8 +448,6 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk)
             __syncwarp();
         }
         // pass 1: per-mode power and phase^2, coalesced along kz
-        int c = 0, rem = lane;                         // kz = c * chunk + rem
-        while (rem >= chunk) { rem -= chunk; c++; }
 #pragma unroll 2
         for (int kz = lane; kz < nz; kz += 32) {
             float2 v = __ldg(a.dk + row + kz);
@@ -461,9 +463,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk)
             float p2 = re * re + im * im;
             float phase = p2 > 0.0f ? atan_unit(re * rsqrtf(p2)) : 0.0f;
             if (hermitian_skip(kx, ky, kz, d)) { p2 = 0.0f; phase = 0.0f; }
-            stage[c * (chunk + 1) + rem] = make_float2(p2, phase * phase);
-            rem += 32;
-            while (rem >= chunk) { rem -= chunk; c++; }
+            stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(p2, phase * phase);   // kz + kz / chunk
         }
         __syncwarp();
         // pass 2: this lane's run of kz, sums kept while the bins stay the same
@@ -818,7 +818,7 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     do {                                                                           \
         static size_t done = 0;                                                    \
         PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms, &done));                \
-        pk_bin_seq_kernel<I, A><<<blocks, 256, sms, st>>>(a, chunk);               \
+        pk_bin_seq_kernel<I, A><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
             if (inter) {
                 if (axis == 0) PYL_SEQ(true, 0); else if (axis == 1) PYL_SEQ(true, 1); else PYL_SEQ(true, 2);

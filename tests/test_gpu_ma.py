@@ -240,13 +240,14 @@ def test_coherent_placement_matches_atomic(MASL, N):
 @pytest.mark.parametrize('mas', MAS_LIST)
 @pytest.mark.parametrize('inter', [False, True])
 def test_owned_cell_write_out_accumulates(MASL, mas, inter):
-    """On grids that are a whole number of 32-cell bins the tiled deposit stores each
-    bin's own cells (old value + bin sum) and passes its halo to the next bins
-    through a buffer.  It must add onto a non-zero grid exactly like the atomic
-    strategy, wrap the halos of the last bins onto the first, and give identical
-    bits on a second run (the halo sums are added in a fixed order)."""
+    """On 1024^3 grids (a whole number of 32-cell bins) the tiled deposit stores each
+    bin's own cells (old value + bin sum), carries its + z layers to the next bin of
+    its CTA and passes its other halo layers to the next bins through a buffer.  It
+    must add onto a non-zero grid exactly like the atomic strategy, wrap the halos
+    of the last bins onto the first, and give identical bits on a second run (the
+    halo sums are added in a fixed order)."""
     rng = np.random.default_rng(31)
-    N, L, n = 96, 1000.0, 2_000_000
+    N, L, n = 1024, 1000.0, 4_000_000
     pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
     # 100 particles in the last cells of the grid along x and z, the first along y:
     # their halos wrap onto bins at the other faces
@@ -254,7 +255,9 @@ def test_owned_cell_write_out_accumulates(MASL, mas, inter):
     corner[:, 0] = np.float32(L) - corner[:, 0] * np.float32(0.999)
     corner[:, 2] = np.float32(L) - corner[:, 2] * np.float32(0.999)
     pos[:100] = torch.from_numpy(corner % np.float32(L)).cuda()
-    base = torch.from_numpy((rng.random((N, N, N)) * 5).astype(np.float32)).cuda()
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(31)
+    base = torch.rand((N, N, N), generator=gen, device='cuda') * 5
     if mas == 'NGP':
         base = torch.floor(base)        # integer sums: any order gives the same bits
     runs = []

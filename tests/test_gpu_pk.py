@@ -202,14 +202,14 @@ def test_overdensity_deposit_matches_two_pass(weighted):
 
 
 @pytest.mark.parametrize('mas', ['NGP', 'CIC', 'TSC', 'PCS'])
-@pytest.mark.parametrize('N', [200, 224])
+@pytest.mark.parametrize('N', [200, 1024])
 def test_overdensity_owned_cells_with_empty_bins(mas, N):
     """Particles packed into one corner leave most bins empty, which must still read
     -1, and every cell must equal the two-pass MA + delta = n/mean - 1, plain and
-    interlaced.  224^3 (a multiple of the 32-cell bin) takes the owned-cell write-out:
-    every bin, empty or not, stores -1 + its sum into its own cells and its halo
-    into a buffer that a second kernel adds to the next bins; the ragged 200^3 grid
-    fills with -1 and adds every bin with its halo atomically."""
+    interlaced.  1024^3 takes the owned-cell write-out: every bin, empty or not,
+    stores -1 + its sum into its own cells and its halo into a buffer that a second
+    kernel adds to the next bins; the ragged 200^3 grid fills with -1 and adds every
+    bin with its halo atomically."""
     import pylians_gb300.MAS_library as MASL
     rng = np.random.default_rng(23)
     L, n = 1000.0, 1_500_000
