@@ -1144,6 +1144,10 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
     using FS = FxShape<MAS, INTER>;
     constexpr int S = Support<MAS>::S, E = FS::E;
     constexpr int PER = R / 1024;                       // records per thread and batch
+    // record of this thread in each 1024-record block: lanes take records 32 apart
+    // (rotated by the warp so the 16-byte reads spread over the banks), so input in
+    // spatial order does not put a warp's atomics on the same cells
+    const unsigned slot = (threadIdx.x & 31u) * 32u + (((threadIdx.x >> 5) + threadIdx.x) & 31u);
     uint4 *z4 = (uint4 *)smw;
     for (int c = threadIdx.x; c < FS::SMEM / 16; c += 1024) z4[c] = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0)
@@ -1167,14 +1171,14 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
         const unsigned c = min((unsigned)R, sg.cnt - j * R);
         float4 r[PER];
 #pragma unroll
-        for (int u = 0; u < PER; u++) r[u] = in[threadIdx.x + u * 1024];
+        for (int u = 0; u < PER; u++) r[u] = in[slot + u * 1024];
         __syncthreads();                                    // buffer consumed
         if (threadIdx.x == 0 && j + 2 < sg.nb)
             stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
                        16u * min((unsigned)R, sg.cnt - (j + 2) * R), &sg.bar[q & 1]);
 #pragma unroll
         for (int u = 0; u < PER; u++) {
-            if (threadIdx.x + u * 1024 >= c) break;
+            if (slot + u * 1024 >= c) continue;
             float C[3][S];
             const int base = (axis_local<MAS, G>(r[u].x, inv, halfcell, dims, o[0], C[0]) * E +
                               axis_local<MAS, G>(r[u].y, inv, halfcell, dims, o[1], C[1])) * E +
