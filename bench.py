@@ -457,11 +457,12 @@ def bench_learned():
 
 STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort', 'halo')
 
-# DRAM bytes per launch of the deposit kernel measured by ncu on the 512^3-particle,
-# 512^3-grid case (dram__bytes_read.sum + dram__bytes_write.sum; the summary and the
-# command are in profiles/bin_deposit_fx_cic_interlaced_512.md); both particles and
-# cells scale the traffic, so it is scaled by the particle count at equal density.
-DEPOSIT_TRAFFIC_512 = (4.117273e9 + 1.112000e9, 512 ** 3)
+# DRAM bytes per launch of the CIC-interlaced deposit kernel measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass of counters; summary and
+# commands in profiles/bin_deposit_fx_cic_interlaced_512.md), keyed by
+# (particles, grid): the 1024^3 bench step itself, and the 512^3 case.
+DEPOSIT_TRAFFIC = {(1024 ** 3, 1024): 29.152525824e9 + 10.270216960e9,
+                   (512 ** 3, 512): 4.017201e9 + 1.101149e9}
 
 
 def stage_times(pp, pos, reps):
@@ -509,23 +510,24 @@ def roofline(stages, n, dims, hbm, src):
       hist: 12 B/particle read;  place (level A): 12 B read + 16 B written per particle;
       place_b: 16 B read + 16 B written per particle;
       deposit: 16 B/particle record read + 2 grids x 4 B/cell written;
+      halo (owned-cell write-out): the halo blocks read once (4 B per halo cell
+        of each bin) + the receiving cells read and written (8 B each);
       fft_r2c: 2 x (4 B/cell read + 8 B/mode written);  pk_bin: 2 fields x 8 B/mode read.
     The dominant single kernel is the one reported."""
     cells = dims ** 3
     modes = dims * dims * (dims // 2 + 1)
+    bins = (dims // 32) ** 3
+    halo_cells = 34 ** 3 - 32 ** 3          # CIC interlaced: 2 halo layers per bin side
     alg = dict(fill=2 * 4.0 * cells, hist=12.0 * n, place=28.0 * n, place_b=32.0 * n,
                deposit=16.0 * n + 2 * 4.0 * cells, fft_r2c=2 * (4.0 * cells + 8.0 * modes),
-               pk_bin=2 * 8.0 * modes)
+               pk_bin=2 * 8.0 * modes, halo=2 * bins * halo_cells * (4.0 + 8.0))
     ms = dict(stages['density_phases'])
     ms['fft_r2c'] = stages['fft_r2c']
     ms['pk_bin'] = stages['pk_bin']
     ms = {k: v for k, v in ms.items() if k in alg}
     top = max(ms, key=lambda k: ms[k])
     achieved = alg[top] / (ms[top] / 1e3) / 1e9
-    traffic = None
-    if top == 'deposit':
-        b512, n512 = DEPOSIT_TRAFFIC_512
-        traffic = b512 * (n / n512)
+    traffic = DEPOSIT_TRAFFIC.get((n, dims)) if top == 'deposit' else None
     return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
                 frac=achieved / hbm, traffic=traffic, peak_source=src,
                 alg_bytes=alg[top], ms=ms[top],
