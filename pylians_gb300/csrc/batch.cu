@@ -481,8 +481,7 @@ extern "C" int pyl_ma_batch_tiled(const pyl_batch_real *reals, int n_reals, cons
     bt_place_kernel<<<grid, 1024, 0, st>>>(reals, items, n_items, tile_base, ws.cursor, (unsigned)total_particles,
                                            ws.rec, ws.counters + 1);
     PYL_LAUNCH_CHECK();
-    static size_t done = 0;
-    PYL_CUDA(ensure_smem(bt_deposit_kernel, BT_DEPOSIT_SMEM, &done));
+    PYL_CUDA(ensure_smem(bt_deposit_kernel, BT_DEPOSIT_SMEM));
     bt_deposit_kernel<<<(unsigned)num_sms(), 1024, BT_DEPOSIT_SMEM, st>>>(
         reals, n_reals, tile_base, total_tiles, ws.offsets, (unsigned)total_particles, ws.rec, ws.counters + 2);
     PYL_LAUNCH_CHECK();

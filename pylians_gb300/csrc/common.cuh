@@ -112,17 +112,15 @@ __device__ __forceinline__ float atan_unit(float x)
 // steady state so that launches can be captured in a CUDA graph).
 // Raises a kernel's dynamic shared-memory limit to at least `bytes`.  The limit
 // is a per-kernel attribute, so it only ever grows: one record per kernel and
-// device (several launch sites of one kernel may ask for different sizes).
-// `done` is a per-call-site fast path.
+// device (several launch sites of one kernel may ask for different sizes, and
+// each device of a process keeps its own attribute).
 size_t smem_limit_raise(const void *kernel, size_t bytes, cudaError_t *err);
 
 template <typename K>
-static inline cudaError_t ensure_smem(K kernel, size_t bytes, size_t *done)
+static inline cudaError_t ensure_smem(K kernel, size_t bytes)
 {
-    if (bytes <= *done) return cudaSuccess;
     cudaError_t e = cudaSuccess;
-    const size_t now = smem_limit_raise((const void *)kernel, bytes, &e);
-    if (e == cudaSuccess) *done = now;
+    smem_limit_raise((const void *)kernel, bytes, &e);
     return e;
 }
 

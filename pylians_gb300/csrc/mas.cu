@@ -1111,19 +1111,24 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
 // positions); TSC and PCS weights are in [0, 1] for any input.
 
 // Bin-local cell of a particle along one axis (0 <= loc < TB for the first cell
-// of the plain grid, loc <= TB for the shifted one) and the axis weights.
-template <int MAS, int G>
+// of the plain grid, loc <= TB for the shifted one) and the axis weights.  The
+// particle's bin came from the wrapped first cell, so loc = (f - o) mod dims: for
+// power-of-two grids (P2) a mask, otherwise the in-range test with the general
+// wrap for cells past the grid edge.
+template <int MAS, int G, bool P2>
 __device__ __forceinline__ int axis_local(float p, float inv, float halfcell, int dims, int o, float *C)
 {
     if (G == 0) {
         const int f = axis_weights<MAS>(p, inv, C);
         const int loc = f - o;
+        if (P2) return loc & (dims - 1);
         return (unsigned)loc < (unsigned)TB ? loc : wrap_index(f, dims) - o;
     }
     const int f0 = axis_first<MAS>(p, inv);
     const int f = axis_weights<MAS>(__fadd_rn(p, halfcell), inv, C);
     const int loc0 = f0 - o;
-    return ((unsigned)loc0 < (unsigned)TB ? loc0 : wrap_index(f0, dims) - o) + (f > f0 ? 1 : 0);
+    const int w0 = P2 ? (loc0 & (dims - 1)) : ((unsigned)loc0 < (unsigned)TB ? loc0 : wrap_index(f0, dims) - o);
+    return w0 + (f > f0 ? 1 : 0);
 }
 
 struct FxStage {
@@ -1137,7 +1142,7 @@ struct FxStage {
 // One pass over the bin's records into shared memory.  Returns 1 when the pass
 // must be redone in float32, 0 when done, -1 after a failed staging wait.
 // q0: batches staged on the two barriers before this pass.
-template <int MAS, bool INTER, int R, int G, bool FLOAT>
+template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2>
 __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, float inv, float halfcell, int dims,
                                              const int *o, unsigned *smw)
 {
@@ -1180,9 +1185,9 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
         for (int u = 0; u < PER; u++) {
             if (slot + u * 1024 >= c) continue;
             float C[3][S];
-            const int base = (axis_local<MAS, G>(r[u].x, inv, halfcell, dims, o[0], C[0]) * E +
-                              axis_local<MAS, G>(r[u].y, inv, halfcell, dims, o[1], C[1])) * E +
-                             axis_local<MAS, G>(r[u].z, inv, halfcell, dims, o[2], C[2]);
+            const int base = (axis_local<MAS, G, P2>(r[u].x, inv, halfcell, dims, o[0], C[0]) * E +
+                              axis_local<MAS, G, P2>(r[u].y, inv, halfcell, dims, o[1], C[1])) * E +
+                             axis_local<MAS, G, P2>(r[u].z, inv, halfcell, dims, o[2], C[2]);
             if (FLOAT) {
                 float_scatter<MAS, E>((float *)smw, base, C);
             } else {
@@ -1405,19 +1410,19 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
 
 // Both arithmetic modes of one grid: fixed point, float32 if that overflowed.
 // Returns false after a failed staging wait.
-template <int MAS, bool INTER, int R, int G>
+template <int MAS, bool INTER, int R, int G, bool P2>
 __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float inv, float halfcell, int dims,
                                         const int *o, unsigned *smw, float *out, bool interior, float scale,
                                         const Owned &ow, float *halo_bin, const float *prev)
 {
-    int st = fx_accumulate<MAS, INTER, R, G, false>(sg, q0, inv, halfcell, dims, o, smw);
+    int st = fx_accumulate<MAS, INTER, R, G, false, P2>(sg, q0, inv, halfcell, dims, o, smw);
     if (st < 0) return false;
     q0 += sg.nb;
     if (st == 0) {
         if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
     } else {
-        if (fx_accumulate<MAS, INTER, R, G, true>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
+        if (fx_accumulate<MAS, INTER, R, G, true, P2>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
         q0 += sg.nb;
         if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, true>(smw, out, o, dims, interior, scale);
@@ -1426,7 +1431,7 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
     return true;
 }
 
-template <int MAS, bool INTER, int R>
+template <int MAS, bool INTER, int R, bool P2>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
     float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
@@ -1471,10 +1476,10 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
         sg.ok = &s_ok;
         float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
         const float *prev = have_prev && hb ? hb - HC : nullptr;
-        if (!fx_grid<MAS, INTER, R, 0>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
+        if (!fx_grid<MAS, INTER, R, 0, P2>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
             return;
         if (INTER &&
-            !fx_grid<MAS, INTER, R, 1>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
+            !fx_grid<MAS, INTER, R, 1, P2>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
                                        hb ? hb + ow.stride : nullptr, prev ? prev + ow.stride : nullptr))
             return;
         have_prev = true;
@@ -1497,10 +1502,11 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
     constexpr int R = fx_tma_batch<MAS, I>();
     static_assert(R == 0 || carry_floats(FS::H) * 4 <= 2 * R * 16, "carried blocks fit the staging buffers");
     if (R > 0) {
-        auto kern = bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024)>;
+        const bool p2 = (g.dims & (g.dims - 1)) == 0;
+        auto kern = p2 ? bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024), true>
+                       : bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024), false>;
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
-        static size_t done_t = 0;
-        PYL_CUDA(ensure_smem(kern, smem, &done_t));
+        PYL_CUDA(ensure_smem(kern, smem));
         const unsigned ctas = (unsigned)(ow.on ? g.ntiles / OWN_Z : g.ntiles);
         kern<<<ctas, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n, ow);
         PYL_LAUNCH_CHECK();
@@ -1522,8 +1528,7 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         return PYL_ERR_UNSUPPORTED;
     }
     auto kern = bin_deposit_fx_kernel<MAS, I>;
-    static size_t done = 0;
-    PYL_CUDA(ensure_smem(kern, FS::SMEM, &done));
+    PYL_CUDA(ensure_smem(kern, FS::SMEM));
     kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc,
                                                      ws.n);
     PYL_LAUNCH_CHECK();
@@ -1536,8 +1541,7 @@ int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, flo
 {
     using TS = TileShape<MAS, I, FX>;
     auto kern = bin_deposit_kernel<MAS, W, I, FX>;
-    static size_t done = 0;
-    PYL_CUDA(ensure_smem(kern, TS::SMEM, &done));
+    PYL_CUDA(ensure_smem(kern, TS::SMEM));
     kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
@@ -1569,7 +1573,6 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         const long long chunk = ((n + C - 1) / C + 3) / 4 * 4;
         const bool tma = (((uintptr_t)pos) & 15) == 0;
         const size_t sm = sizeof(unsigned) * T;
-        static size_t d1 = 0, d2 = 0, d3 = 0, d4 = 0;
         // grids past TWO_LEVEL_TILES bins choose their placement by input coherence
         const bool counted = rsd || (tma && hist_tma_smem(T) <= 227 * 1024);
         const bool gated = counted && tma && ws.tmp;
@@ -1577,16 +1580,15 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         stage_mark(PYL_STAGE_HIST, true, st);
         if (gated) PYL_CUDA(cudaMemsetAsync(ws.same, 0, sizeof(unsigned long long), st));
         if (rsd) {                                 // callers check tiled_rsd_fusable first
-            static size_t d5 = 0;
-            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS, true>, hist_tma_smem(T), &d5));
+            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS, true>, hist_tma_smem(T)));
             chunk_hist_tma_kernel<MAS, true><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist, *rsd,
                                                                                  same);
         } else if (counted) {
-            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS>, hist_tma_smem(T), &d4));
+            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS>, hist_tma_smem(T)));
             chunk_hist_tma_kernel<MAS><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist,
                                                                           RsdArgs{}, same);
         } else {
-            PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm, &d1));
+            PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm));
             chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
         }
         PYL_LAUNCH_CHECK();
@@ -1599,14 +1601,13 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         if (!ws.tmp && tma && level_a_tma_smem(T) <= 227 * 1024) {
             // at most TWO_LEVEL_TILES bins: level A with one bucket per bin writes the
             // final [bin][chunk] layout in one pass
-            static size_t dw = 0, du = 0;
             const size_t sat = level_a_tma_smem(T);
             if (w) {
-                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat, &dw));
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat));
                 level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                          ws.offsets, ws.rec, 1);
             } else {
-                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat, &du));
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat));
                 level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                           ws.offsets, ws.rec, 1);
             }
@@ -1614,18 +1615,17 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
             const int NCO = g.nc * g.nc * g.nc;
             const size_t sa = sizeof(unsigned) * ((3 * NCO + 32 + 3) & ~3) + sizeof(float4) * LA_BATCH +
                               sizeof(unsigned short) * LA_BATCH;
-            static size_t da = 0, db = 0, dta = 0, dtb = 0, dtc = 0;
             const size_t sat = level_a_tma_smem(NCO);
             // coherent when at least 3/4 of the particles share their predecessor's bin
             const unsigned long long thresh = (unsigned long long)n - (unsigned long long)n / 4;
             const Gate coherent{same, thresh, 1}, incoherent{same, thresh, 0};
             if (gated) {
                 if (w) {
-                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
+                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm));
                     chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                          ws.offsets, ws.rec, coherent);
                 } else {
-                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm, &d3));
+                    PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm));
                     chunk_scatter_kernel<MAS, false><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                           ws.offsets, ws.rec, coherent);
                 }
@@ -1633,37 +1633,37 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
             }
             if (tma && sat <= 227 * 1024) {
                 if (w) {
-                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat, &dta));
+                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat));
                     level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                              ws.offsets, ws.tmp, 0, incoherent);
                 } else {
-                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat, &dtb));
+                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat));
                     level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                               ws.offsets, ws.tmp, 0, incoherent);
                 }
             } else if (w) {
-                PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa, &da));
+                PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa));
                 level_a_kernel<MAS, true><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                     ws.offsets, ws.tmp);
             } else {
-                PYL_CUDA(ensure_smem(level_a_kernel<MAS, false>, sa, &db));
+                PYL_CUDA(ensure_smem(level_a_kernel<MAS, false>, sa));
                 level_a_kernel<MAS, false><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                      ws.offsets, ws.tmp);
             }
             PYL_LAUNCH_CHECK();
             stage_mark(PYL_STAGE_PLACE, false, st);
             stage_mark(PYL_STAGE_PLACE_B, true, st);
-            PYL_CUDA(ensure_smem(level_b_tma_kernel<MAS>, level_b_tma_smem(), &dtc));
+            PYL_CUDA(ensure_smem(level_b_tma_kernel<MAS>, level_b_tma_smem()));
             level_b_tma_kernel<MAS><<<(unsigned)(C * NCO), LBT_THREADS, level_b_tma_smem(), st>>>(
                 ws.tmp, C, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n, incoherent);
             PYL_LAUNCH_CHECK();
             stage_mark(PYL_STAGE_PLACE_B, false, st);
         } else if (w) {
-            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm, &d2));
+            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm));
             chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                  ws.offsets, ws.rec);
         } else {
-            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm, &d3));
+            PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, false>, sm));
             chunk_scatter_kernel<MAS, false><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                   ws.offsets, ws.rec);
         }

@@ -816,8 +816,7 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
             PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
 #define PYL_SEQ(I, A)                                                              \
     do {                                                                           \
-        static size_t done = 0;                                                    \
-        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms, &done));                \
+        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms));                \
         pk_bin_seq_kernel<I, A><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
             if (inter) {
@@ -838,8 +837,7 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, n_fields), st));
 #define PYL_BIN(I, A, FF)                                                          \
     do {                                                                           \
-        static size_t done = 0;                                                    \
-        PYL_CUDA(ensure_smem(pk_bin_kernel<I, A, FF>, smem, &done));               \
+        PYL_CUDA(ensure_smem(pk_bin_kernel<I, A, FF>, smem));               \
         pk_bin_kernel<I, A, FF><<<blocks, 256, smem, st>>>(a);                     \
     } while (0)
 #define PYL_BIN_F(I, A)                                                            \
@@ -908,8 +906,7 @@ extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace
     PYL_CUDA(cudaMemsetAsync(geom, 0, sizeof(double) * pyl_pk_geometry_len(dims), st));
 #define PYL_GEOM(A)                                                                \
     do {                                                                           \
-        static size_t done = 0;                                                    \
-        PYL_CUDA(ensure_smem(pk_geometry_kernel<A>, smem, &done));                 \
+        PYL_CUDA(ensure_smem(pk_geometry_kernel<A>, smem));                 \
         pk_geometry_kernel<A><<<blocks, 256, smem, st>>>(a);                       \
     } while (0)
     if (axis == 0) PYL_GEOM(0); else if (axis == 1) PYL_GEOM(1); else PYL_GEOM(2);

@@ -89,8 +89,7 @@ extern "C" int pyl_pk_plane_bin(const void *dk1, const void *dk2, int dims, int 
     PYL_CHECK_ARG(smem <= 200 * 1024, "grid too large for the shared-memory bins");
     cudaStream_t st = (cudaStream_t)stream;
     PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * 5 * nb, st));
-    static size_t done = 0;
-    PYL_CUDA(ensure_smem(plane_bin_kernel, smem, &done));
+    PYL_CUDA(ensure_smem(plane_bin_kernel, smem));
     int blocks = (dims + 255) / 256;
     plane_bin_kernel<<<blocks, 256, smem, st>>>((const float2 *)dk1, (const float2 *)dk2, dims, mas_p1, mas_p2,
                                                 nb, sums);
