@@ -1017,85 +1017,8 @@ inline size_t owned_halo_floats(int mas, int dims, bool inter)
 // positions below 0, non-finite positions) or a cell sum that wraps sets a
 // flag, and the pass is redone with float32 shared atomics.  The grids (plain,
 // then interlaced) are deposited one after the other; the second pass reads the
-// bin's particles again from L2.
-template <int MAS, bool INTER>
-__global__ void __launch_bounds__(1024) bin_deposit_fx_kernel(
-    const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec)
-{
-    using FS = FxShape<MAS, INTER>;
-    const float scale = out_scale(sc);
-    constexpr int S = Support<MAS>::S, E = FS::E, CELLS = FS::CELLS;
-    extern __shared__ __align__(16) unsigned smw[];
-    float *facc = (float *)smw;
-    const long long tile = blockIdx.x;
-    const unsigned end = min(offsets[tile + 1], n_rec), begin = min(offsets[tile], end);
-    if (begin == end) return;
-    int tx, ty, tz;
-    tile_coords(tile, g, tx, ty, tz);
-    const int o[3] = {tx * TB, ty * TB, tz * TB};
-    const long long d = g.dims;
-    const unsigned T = blockDim.x;
-    for (int pass = 0; pass < (INTER ? 2 : 1); pass++) {
-        for (int mode = 0; mode < 2; mode++) {          // 0: fixed point, 1: float fallback
-            uint4 *z4 = (uint4 *)smw;
-            for (int c = threadIdx.x; c < FS::SMEM / 16; c += T) z4[c] = make_uint4(0u, 0u, 0u, 0u);
-            __syncthreads();
-            unsigned bad = 0u;
-            unsigned long long i = begin + threadIdx.x;
-            // two particles in flight per thread
-            for (; i + T < end; i += 2ull * T) {
-                const float4 r0 = rec[i], r1 = rec[i + T];
-                float C0[3][S], C1[3][S];
-                const int b0 = pass ? fx_support<MAS, 1, E>(r0, inv, halfcell, g.dims, o, C0)
-                                    : fx_support<MAS, 0, E>(r0, inv, halfcell, g.dims, o, C0);
-                const int b1 = pass ? fx_support<MAS, 1, E>(r1, inv, halfcell, g.dims, o, C1)
-                                    : fx_support<MAS, 0, E>(r1, inv, halfcell, g.dims, o, C1);
-                if (mode == 0) {
-                    bad |= (unsigned)!(fx_weights_ok<MAS>(C0) && fx_weights_ok<MAS>(C1));
-                    bad |= fx_scatter<MAS, E>(smw, b0, C0);
-                    bad |= fx_scatter<MAS, E>(smw, b1, C1);
-                } else {
-                    float_scatter<MAS, E>(facc, b0, C0);
-                    float_scatter<MAS, E>(facc, b1, C1);
-                }
-            }
-            if (i < end) {
-                const float4 r0 = rec[i];
-                float C0[3][S];
-                const int b0 = pass ? fx_support<MAS, 1, E>(r0, inv, halfcell, g.dims, o, C0)
-                                    : fx_support<MAS, 0, E>(r0, inv, halfcell, g.dims, o, C0);
-                if (mode == 0) {
-                    bad |= (unsigned)!fx_weights_ok<MAS>(C0);
-                    bad |= fx_scatter<MAS, E>(smw, b0, C0);
-                } else {
-                    float_scatter<MAS, E>(facc, b0, C0);
-                }
-            }
-            if (__syncthreads_or((int)bad) && mode == 0) {   // redo this pass in float32
-                __syncthreads();
-                continue;
-            }
-            float *out = pass == 0 ? grid : grid2;
-            for (int c = threadIdx.x; c < CELLS; c += T) {
-                const unsigned w = smw[c];
-                if (w == 0u) continue;
-                const float v = mode == 1 ? __uint_as_float(w)
-                                          : (MAS == PYL_MAS_NGP ? __uint2float_rn(w)
-                                                                : __fmul_rn(__uint2float_rn(w), FX_INV));
-                const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
-                                gz = add_wrap(o[2], lz, d);
-                atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
-            }
-            __syncthreads();
-            break;
-        }
-    }
-}
-
-// ---- TMA-staged full-bin deposit ----------------------------------------------
-// Same arithmetic and results as bin_deposit_fx_kernel, with these changes:
+// bin's particles again (partly from L2).
+// The deposit:
 //   * each pass streams the bin's records through two shared-memory buffers of
 //     R records filled by bulk copies (batch q+2 loads while batch q deposits);
 //   * the overflow test ORs the old values returned by the atomics and checks
@@ -1523,16 +1446,8 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         }
         return PYL_OK;
     }
-    if (ow.on) {
-        set_error("owned-cell write-out needs the staged deposit");
-        return PYL_ERR_UNSUPPORTED;
-    }
-    auto kern = bin_deposit_fx_kernel<MAS, I>;
-    PYL_CUDA(ensure_smem(kern, FS::SMEM));
-    kern<<<(unsigned)g.ntiles, 1024, FS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc,
-                                                     ws.n);
-    PYL_LAUNCH_CHECK();
-    return PYL_OK;
+    set_error("no staging buffers fit beside this bin");
+    return PYL_ERR_UNSUPPORTED;
 }
 
 template <int MAS, bool W, bool I, bool FX>
@@ -1949,7 +1864,9 @@ namespace pyl {
 namespace {
 constexpr long long NOALLOC_MAX_PARTICLES = 1LL << 19;   // 524,288 particles
 constexpr int NOALLOC_MAX_DIMS = 512;                    // <= (512/32)^3 = 4096 bins
-constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;      // 16 MiB per device
+// 524288 particles on a 512^3 grid: two record buffers (two-level placement) of
+// 8 MiB + 2.4 MiB of chunk histograms
+constexpr size_t NOALLOC_SCRATCH_BYTES = 20u << 20;      // 20 MiB per device
 
 // Held by every GPU that loads the library until the process exits.
 __device__ __align__(256) unsigned char g_ma_scratch[NOALLOC_SCRATCH_BYTES];

@@ -4,7 +4,7 @@ Some callers of this library cannot allocate device memory around a call: code
 that runs while a CUDA graph is being captured, plugins hosted by a framework
 that owns the device allocator, loops that allocate nothing after start-up.
 pyl_ma_noalloc serves them with binning scratch compiled into the library
-(16 MiB per device; at most 524288 particles and dims <= 512).
+(20 MiB per device; at most 524288 particles and dims <= 512).
 
 The test calls it twice in a row (the shared scratch keeps the previous call's
 contents) and compares each result with pyl_ma, the allocating entry point, on
@@ -67,6 +67,21 @@ def test_noalloc_matches_pyl_ma_twice(lib, mas, weighted, inter):
             else:
                 err = (got - ref).abs().max().item()
                 assert err <= 2e-6 * ref.abs().max().item(), 'call %d: max diff %g' % (call, err)
+
+
+def test_noalloc_largest_request(lib):
+    """The documented maximum (524288 particles on a 512^3 grid, which takes the
+    two-level placement and so two record buffers) fits the fixed scratch and
+    matches pyl_ma."""
+    rng = np.random.default_rng(7)
+    N, L, n = 512, 1000.0, 1 << 19
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    ref, _ = _reference(lib, pos, None, N, L, 2, False)
+    g = torch.zeros((N, N, N), device='cuda')
+    rc = lib.pyl_ma_noalloc(_p(pos), None, n, _p(g), None, N, L, 2, None)
+    assert rc == 0, lib.pyl_last_error()
+    torch.cuda.synchronize()
+    assert (g - ref).abs().max().item() <= 2e-6 * ref.abs().max().item()
 
 
 def test_noalloc_rejects_oversized_requests(lib):
