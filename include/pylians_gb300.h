@@ -97,7 +97,7 @@ int pyl_ma_overdensity_rsd(float *pos, const float *vel, const float *weights, i
  * during CUDA-graph capture, plugins inside a host framework that owns the
  * device allocator, real-time loops that allocate nothing after start-up).
  * Same deposit as pyl_ma with the tiled strategy (3D grids only, grid +=,
- * optional interlaced grid), but the binning scratch lives in a fixed 20 MiB
+ * optional interlaced grid), but the binning scratch lives in a fixed 24 MiB
  * array compiled into the library, held by every GPU that loads it until the
  * process exits.  Limits: n_particles <= 524288 and dims <= 512; larger
  * requests return PYL_ERR_INVALID.  The first call on a device looks up the

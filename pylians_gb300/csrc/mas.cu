@@ -499,15 +499,19 @@ __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *pos, 
 
 inline size_t hist_tma_smem(long long ntiles) { return (size_t)HT_NBUF * HT_BATCH * 12 + sizeof(unsigned) * ntiles; }
 
-constexpr int LAT_U = 4, LAT_BATCH = LA_THREADS * LAT_U;     // 4096 particles per batch
+constexpr int LAT_U = 4;                                    // particles per thread and batch
 constexpr int LA_NBUF = 2;                                  // batches in flight
 
-template <int MAS, bool WEIGHTED>
-__global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
+// NT threads per CTA: 1024 for the one-pass placement by bin (up to 1024 bins,
+// scanned by one block scan), 512 for level A of two (two CTAs per SM, so one
+// CTA's shared-memory sort overlaps the other's memory traffic).
+template <int MAS, bool WEIGHTED, int NT>
+__global__ void __launch_bounds__(NT) level_a_tma_kernel(
     const float *__restrict__ pos, const float *__restrict__ w, long long n, long long chunk, float inv,
     TileGeom g, const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets,
     float4 *__restrict__ tmp, int by_tile, Gate gate = Gate{nullptr, 0ull, 0})
 {
+    constexpr int BATCH = NT * LAT_U;
     extern __shared__ __align__(16) unsigned char araw[];
     __shared__ __align__(8) unsigned long long bar[LA_NBUF];
     __shared__ int s_ok;
@@ -516,10 +520,10 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     // (one pass into the final layout, for grids of at most TWO_LEVEL_TILES bins)
     const int T = (int)g.ntiles;
     const int NCO = by_tile ? T : g.nc * g.nc * g.nc;
-    float *inb = (float *)araw;                                            // [LA_NBUF][LAT_BATCH * 3]
-    float4 *stage = (float4 *)(araw + LA_NBUF * LAT_BATCH * 12);
-    unsigned short *sco = (unsigned short *)(stage + LAT_BATCH);
-    unsigned *cur = (unsigned *)(sco + LAT_BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
+    float *inb = (float *)araw;                                            // [LA_NBUF][BATCH * 3]
+    float4 *stage = (float4 *)(araw + LA_NBUF * BATCH * 12);
+    unsigned short *sco = (unsigned short *)(stage + BATCH);
+    unsigned *cur = (unsigned *)(sco + BATCH), *bcnt = cur + NCO, *gst = bcnt + NCO, *wt = gst + NCO;
     const unsigned *row = colpre + (long long)blockIdx.x * T;
     for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
         if (by_tile) {
@@ -531,7 +535,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         }
     }
     const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
-    const long long nbat = e > b ? (e - b + LAT_BATCH - 1) / LAT_BATCH : 0;
+    const long long nbat = e > b ? (e - b + BATCH - 1) / BATCH : 0;
     if (threadIdx.x == 0) {
         for (int q = 0; q < LA_NBUF; q++) mbar_init(&bar[q], 1);
         mbar_fence_init();
@@ -539,16 +543,16 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     __syncthreads();
     if (threadIdx.x == 0)
         for (long long j = 0; j < LA_NBUF && j < nbat; j++) {
-            const long long s0 = b + j * LAT_BATCH;
-            stage_copy(inb + (j % LA_NBUF) * LAT_BATCH * 3, pos + 3 * s0,
-                       staged_bytes(min((long long)LAT_BATCH, e - s0)), &bar[j % LA_NBUF]);
+            const long long s0 = b + j * BATCH;
+            stage_copy(inb + (j % LA_NBUF) * BATCH * 3, pos + 3 * s0,
+                       staged_bytes(min((long long)BATCH, e - s0)), &bar[j % LA_NBUF]);
         }
     for (long long j = 0; j < nbat; j++) {
-        const long long s0 = b + j * LAT_BATCH;
-        const int c = (int)min((long long)LAT_BATCH, e - s0);
+        const long long s0 = b + j * BATCH;
+        const int c = (int)min((long long)BATCH, e - s0);
         const int full = staged_full(c);
         const int buf = (int)(j % LA_NBUF);
-        const float *in = inb + buf * LAT_BATCH * 3;
+        const float *in = inb + buf * BATCH * 3;
         if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&bar[buf], (unsigned)((j / LA_NBUF) & 1), &g_tma_error);
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) bcnt[co] = 0u;
         __syncthreads();
@@ -562,7 +566,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         unsigned co_u[LAT_U], rank[LAT_U];
 #pragma unroll
         for (int u = 0; u < LAT_U; u++) {
-            const int i = threadIdx.x + u * LA_THREADS;
+            const int i = threadIdx.x + u * NT;
             co_u[u] = 0xffffffffu;
             if (i < c) {
                 if (i < full) r[u] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 1.0f);
@@ -579,8 +583,8 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
         }
         __syncthreads();
         if (threadIdx.x == 0 && j + LA_NBUF < nbat) {            // this buffer is consumed
-            const long long s2 = b + (j + LA_NBUF) * LAT_BATCH;
-            stage_copy(inb + buf * LAT_BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)LAT_BATCH, e - s2)),
+            const long long s2 = b + (j + LA_NBUF) * BATCH;
+            stage_copy(inb + buf * BATCH * 3, pos + 3 * s2, staged_bytes(min((long long)BATCH, e - s2)),
                        &bar[buf]);
         }
         for (int co = threadIdx.x; co < NCO; co += blockDim.x) {
@@ -598,7 +602,7 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
             }
         }
         __syncthreads();
-        for (int sidx = threadIdx.x; sidx < c; sidx += LA_THREADS) {
+        for (int sidx = threadIdx.x; sidx < c; sidx += NT) {
             const unsigned co = sco[sidx];
             const unsigned dst = gst[co] + ((unsigned)sidx - bcnt[co]);      // n < 2^32
             if (dst < (unsigned)n) tmp[dst] = stage[sidx];
@@ -607,17 +611,21 @@ __global__ void __launch_bounds__(LA_THREADS) level_a_tma_kernel(
     }
 }
 
-inline size_t level_a_tma_smem(int nco)
+inline size_t level_a_tma_smem(int nco, int nt)
 {
-    return (size_t)LA_NBUF * LAT_BATCH * 12 + sizeof(float4) * LAT_BATCH + sizeof(unsigned short) * LAT_BATCH +
+    const size_t batch = (size_t)nt * LAT_U;
+    return (size_t)LA_NBUF * batch * 12 + sizeof(float4) * batch + sizeof(unsigned short) * batch +
            sizeof(unsigned) * (3 * nco + 32);
 }
 
 constexpr int LBT_THREADS = 512, LBT_U = 4, LBT_BATCH = LBT_THREADS * LBT_U;   // 2048 records
 
+// One CTA per (group of G consecutive chunks, coarse block): the group's records of
+// a coarse block are contiguous in tmp, and each bin's records of the group are
+// contiguous in the final layout, so a group sorts as one segment.
 template <int MAS>
 __global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
-    const float4 *__restrict__ tmp, int C, float inv, TileGeom g, const unsigned *__restrict__ colpre,
+    const float4 *__restrict__ tmp, int C, int G, float inv, TileGeom g, const unsigned *__restrict__ colpre,
     const unsigned *__restrict__ total, const unsigned *__restrict__ offsets, float4 *__restrict__ rec,
     unsigned n, Gate gate = Gate{nullptr, 0ull, 0})
 {
@@ -632,13 +640,14 @@ __global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
     unsigned char *slo = (unsigned char *)(stage + LBT_BATCH);
     const int NCO = g.nc * g.nc * g.nc;
     const int T = (int)g.ntiles;
-    const int c = blockIdx.x / NCO, co = blockIdx.x % NCO;
+    const int c = (blockIdx.x / NCO) * G, co = blockIdx.x % NCO;
+    const int c_end = min(c + G, C);
     if (threadIdx.x < 32) {
         unsigned pre = 0, len = 0;
         for (int l = threadIdx.x; l < 64; l += 32) {
             const int t = co * 64 + l;
             const unsigned cp = colpre[(long long)c * T + t];
-            const unsigned nx = c + 1 < C ? colpre[(long long)(c + 1) * T + t] : total[t];
+            const unsigned nx = c_end < C ? colpre[(long long)c_end * T + t] : total[t];
             fcur[l] = offsets[t] + cp;
             pre += cp;
             len += nx - cp;
@@ -950,6 +959,16 @@ __host__ __device__ constexpr int halo_block_off(int H, int h)
 __host__ __device__ constexpr int halo_cells(int H) { return halo_block_off(H, 8); }   // (TB + H)^3 - TB^3
 static_assert(halo_cells(2) == 34 * 34 * 34 - TB * TB * TB, "halo blocks cover the + side layers");
 
+// Two-level placement over at most 128 coarse blocks (grids up to 512^3): level A
+// runs two 512-thread CTAs per SM over twice as many chunks (2048-particle batches
+// still give each coarse block runs of about 16 records).  Larger grids keep one
+// 1024-thread CTA per SM with 4096-particle batches (512 coarse blocks: 8 records
+// per run; halving the batch measured 1 ms slower at 1024^3).
+inline bool two_level_small(const TileGeom &g)
+{
+    return g.ntiles > TWO_LEVEL_TILES && g.ntiles <= HIST_MAX_TILES && (long long)g.nc * g.nc * g.nc <= 128;
+}
+
 struct TiledWs {
     unsigned n;                  // particles binned
     unsigned *hist, *total, *offsets;
@@ -970,7 +989,7 @@ TiledWs tiled_layout(void *base, long long n, int dims, size_t halo_floats = 0)
     TiledWs ws;
     ws.n = (unsigned)n;
     ws.smem_hist = g.ntiles <= HIST_MAX_TILES;
-    ws.chunks = num_sms() < MAX_CHUNKS ? num_sms() : MAX_CHUNKS;
+    ws.chunks = min(two_level_small(g) ? 2 * num_sms() : num_sms(), MAX_CHUNKS);
     const size_t hist_len = ws.smem_hist ? (size_t)ws.chunks * g.ntiles : (size_t)g.ntiles;
     size_t off = 0;
     char *b = (char *)base;
@@ -1513,24 +1532,25 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         PYL_LAUNCH_CHECK();
         stage_mark(PYL_STAGE_HIST, false, st);
         stage_mark(PYL_STAGE_PLACE, true, st);
-        if (!ws.tmp && tma && level_a_tma_smem(T) <= 227 * 1024) {
+        if (!ws.tmp && tma && level_a_tma_smem(T, 1024) <= 227 * 1024) {
             // at most TWO_LEVEL_TILES bins: level A with one bucket per bin writes the
             // final [bin][chunk] layout in one pass
-            const size_t sat = level_a_tma_smem(T);
+            const size_t sat = level_a_tma_smem(T, 1024);
             if (w) {
-                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat));
-                level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true, 1024>, sat));
+                level_a_tma_kernel<MAS, true, 1024><<<C, 1024, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                          ws.offsets, ws.rec, 1);
             } else {
-                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat));
-                level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
+                PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false, 1024>, sat));
+                level_a_tma_kernel<MAS, false, 1024><<<C, 1024, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
                                                                           ws.offsets, ws.rec, 1);
             }
         } else if (ws.tmp) {
             const int NCO = g.nc * g.nc * g.nc;
             const size_t sa = sizeof(unsigned) * ((3 * NCO + 32 + 3) & ~3) + sizeof(float4) * LA_BATCH +
                               sizeof(unsigned short) * LA_BATCH;
-            const size_t sat = level_a_tma_smem(NCO);
+            const int lat = two_level_small(g) ? 512 : 1024;
+            const size_t sat = level_a_tma_smem(NCO, lat);
             // coherent when at least 3/4 of the particles share their predecessor's bin
             const unsigned long long thresh = (unsigned long long)n - (unsigned long long)n / 4;
             const Gate coherent{same, thresh, 1}, incoherent{same, thresh, 0};
@@ -1547,15 +1567,15 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
                 PYL_LAUNCH_CHECK();
             }
             if (tma && sat <= 227 * 1024) {
-                if (w) {
-                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, true>, sat));
-                    level_a_tma_kernel<MAS, true><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                             ws.offsets, ws.tmp, 0, incoherent);
-                } else {
-                    PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, false>, sat));
-                    level_a_tma_kernel<MAS, false><<<C, LA_THREADS, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist,
-                                                                              ws.offsets, ws.tmp, 0, incoherent);
-                }
+#define PYL_LEVEL_A(WW, NT)                                                                                   \
+    do {                                                                                                     \
+        PYL_CUDA(ensure_smem(level_a_tma_kernel<MAS, WW, NT>, sat));                                         \
+        level_a_tma_kernel<MAS, WW, NT><<<C, NT, sat, st>>>(pos, w, n, chunk, inv, g, ws.hist, ws.offsets,   \
+                                                           ws.tmp, 0, incoherent);                           \
+    } while (0)
+                if (w) { if (lat == 512) PYL_LEVEL_A(true, 512); else PYL_LEVEL_A(true, 1024); }
+                else   { if (lat == 512) PYL_LEVEL_A(false, 512); else PYL_LEVEL_A(false, 1024); }
+#undef PYL_LEVEL_A
             } else if (w) {
                 PYL_CUDA(ensure_smem(level_a_kernel<MAS, true>, sa));
                 level_a_kernel<MAS, true><<<C, LA_THREADS, sa, st>>>(pos, w, n, chunk, inv, g, ws.hist,
@@ -1569,8 +1589,9 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
             stage_mark(PYL_STAGE_PLACE, false, st);
             stage_mark(PYL_STAGE_PLACE_B, true, st);
             PYL_CUDA(ensure_smem(level_b_tma_kernel<MAS>, level_b_tma_smem()));
-            level_b_tma_kernel<MAS><<<(unsigned)(C * NCO), LBT_THREADS, level_b_tma_smem(), st>>>(
-                ws.tmp, C, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n, incoherent);
+            const int G = (C + num_sms() - 1) / num_sms();           // chunks per level-B segment
+            level_b_tma_kernel<MAS><<<(unsigned)(((C + G - 1) / G) * NCO), LBT_THREADS, level_b_tma_smem(), st>>>(
+                ws.tmp, C, G, inv, g, ws.hist, ws.total, ws.offsets, ws.rec, (unsigned)n, incoherent);
             PYL_LAUNCH_CHECK();
             stage_mark(PYL_STAGE_PLACE_B, false, st);
         } else if (w) {
@@ -1865,8 +1886,8 @@ namespace {
 constexpr long long NOALLOC_MAX_PARTICLES = 1LL << 19;   // 524,288 particles
 constexpr int NOALLOC_MAX_DIMS = 512;                    // <= (512/32)^3 = 4096 bins
 // 524288 particles on a 512^3 grid: two record buffers (two-level placement) of
-// 8 MiB + 2.4 MiB of chunk histograms
-constexpr size_t NOALLOC_SCRATCH_BYTES = 20u << 20;      // 20 MiB per device
+// 8 MiB + 4.8 MiB of chunk histograms (two chunks per SM)
+constexpr size_t NOALLOC_SCRATCH_BYTES = 24u << 20;      // 24 MiB per device
 
 // Held by every GPU that loads the library until the process exits.
 __device__ __align__(256) unsigned char g_ma_scratch[NOALLOC_SCRATCH_BYTES];

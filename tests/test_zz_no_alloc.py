@@ -4,7 +4,7 @@ Some callers of this library cannot allocate device memory around a call: code
 that runs while a CUDA graph is being captured, plugins hosted by a framework
 that owns the device allocator, loops that allocate nothing after start-up.
 pyl_ma_noalloc serves them with binning scratch compiled into the library
-(20 MiB per device; at most 524288 particles and dims <= 512).
+(24 MiB per device; at most 524288 particles and dims <= 512).
 
 The test calls it twice in a row (the shared scratch keeps the previous call's
 contents) and compares each result with pyl_ma, the allocating entry point, on
