@@ -205,13 +205,13 @@ def test_two_level_placement_matches_atomic(MASL, mas):
         del a1, a2, b1, b2
 
 
-@pytest.mark.parametrize('N', [384, 544])
+@pytest.mark.parametrize('N', [384, 544, 1024])
 def test_coherent_placement_matches_atomic(MASL, N):
     """Particles in spatial order (a jittered lattice, z fastest) share their
-    predecessor's bin, so the tiled strategy places them in one pass: by bin in shared
-    memory up to 4096 bins (384^3: 12^3 bins), straight to the bin otherwise (544^3).
-    Half-shuffled input (coherence near 1/2) takes the two-level sorts.  All must
-    equal the atomic strategy."""
+    predecessor's bin, so on grids of more than 1024 bins the tiled strategy places
+    them straight to their bins in one pass (384^3, 544^3; 1024^3 also stores its
+    own cells and passes halos on).  Half-shuffled input (coherence near 1/2) takes
+    the two-level sorts.  All must equal the atomic strategy."""
     rng = np.random.default_rng(13)
     L, M = 1000.0, 160
     g = (np.arange(M, dtype=np.float32) + 0.5) * np.float32(L / M)
