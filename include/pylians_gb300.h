@@ -272,7 +272,7 @@ int pyl_pk_plane_bins(int dims);
 int pyl_pk_plane_bin(const void *dk1, const void *dk2, int dims, int mas_p1, int mas_p2, double *sums,
                      void *stream);
 
-/* ---- smoothing (smoothing_library.pyx:20-123) ---------------------------------
+/* ---- smoothing (smoothing_library.pyx:20-114) ---------------------------------
  * pyl_filter_grid replaces the real-space part of FT_filter: field [dims]^3 gets
  * the Top-Hat (gaussian = 0: 1 where d^2 <= (R dims/BoxSize)^2) or Gaussian
  * (exp(-d^2 / (2 R_grid^2))) filter divided by its float64 sum (written to *norm);

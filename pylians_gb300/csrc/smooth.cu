@@ -1,4 +1,4 @@
-// smoothing_library (smoothing_library.pyx:20-123): the real-space filter of
+// smoothing_library (smoothing_library.pyx:20-114): the real-space filter of
 // FT_filter on the grid and the Fourier-space product of field_smoothing.
 //   pyl_filter_grid: Top-Hat (1 where d^2 <= R_grid^2) or Gaussian
 //     (exp(-d^2 / (2 R_grid^2)), float64 exp rounded to float), R_grid =

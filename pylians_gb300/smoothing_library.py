@@ -1,4 +1,4 @@
-"""Drop-in for Pylians' smoothing_library on the GPU (smoothing_library.pyx:20-123).
+"""Drop-in for Pylians' smoothing_library on the GPU (smoothing_library.pyx:20-114).
 
   FT_filter(BoxSize, R, dims, Filter, threads): the Fourier transform of a
     'Top-Hat' or 'Gaussian' filter of radius R placed on a dims^3 grid and

@@ -220,7 +220,7 @@ def make_plane(MASL, PKL):
 
 
 def make_smoothing(MASL):
-    """smoothing_library.FT_filter and field_smoothing (smoothing_library.pyx:20-123):
+    """smoothing_library.FT_filter and field_smoothing (smoothing_library.pyx:20-114):
     Top-Hat and Gaussian filters on 32^3 and 15^3 grids, applied to a CIC field."""
     SL = build_ref.load_smoothing()
     out = {}
