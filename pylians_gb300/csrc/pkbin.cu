@@ -74,6 +74,8 @@ struct BinArgs {
     int chunks;            // axis 0/1: CTAs per plane
     int rows_per_cta;      // axis 2: table entries per CTA
     int warp_arrays;       // axis 2: per-warp kz arrays in shared memory
+    float *part;           // one field: per-CTA partial sums in global memory (null: shared memory)
+    int part_stride;       // floats per CTA: 3D bins x 4, then k_per bins (axes 0/1)
 };
 
 struct BinSmem {
@@ -417,6 +419,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     float *w1 = w2 + nz;
     const int kz_begin = lane * chunk;
     const int kz_end = min(nz, kz_begin + chunk);
+    float *part = a.part ? a.part + (long long)blockIdx.x * a.part_stride : nullptr;
     float r1 = 0.0f;
     int cur_ring = -1;
 
@@ -506,16 +509,21 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
                     new2 = (kper + 1) * (kper + 1) <= kp2;
                 }
                 if (new3 || kz + 1 == kz_end) {
-                    float *b3 = acc3 + ki * 4;
-                    if (s0 != 0.0f) atomicAdd(b3, s0);
-                    if (s2 != 0.0f) atomicAdd(b3 + 1, s2);
-                    if (s4 != 0.0f) atomicAdd(b3 + 2, s4);
-                    if (sp != 0.0f) atomicAdd(b3 + 3, sp);
+                    if (part) {                         // one vector reduction in L2
+                        atomicAdd(reinterpret_cast<float4 *>(part + ki * 4), make_float4(s0, s2, s4, sp));
+                    } else {                            // float shared atomics: compare-and-swap loops
+                        float *b3 = acc3 + ki * 4;
+                        if (s0 != 0.0f) atomicAdd(b3, s0);
+                        if (s2 != 0.0f) atomicAdd(b3 + 1, s2);
+                        if (s4 != 0.0f) atomicAdd(b3 + 2, s4);
+                        if (sp != 0.0f) atomicAdd(b3 + 3, sp);
+                    }
                     s0 = s2 = s4 = sp = 0.0f;
                     ki += new3 ? 1 : 0;
                 }
                 if (AXIS != 2 && (new2 || kz + 1 == kz_end)) {
-                    if (sd != 0.0f) atomicAdd(acc2 + kper, sd);
+                    if (part) atomicAdd(part + d.nb3 * 4 + kper, sd);
+                    else if (sd != 0.0f) atomicAdd(acc2 + kper, sd);
                     sd = 0.0f;
                     kper += new2 ? 1 : 0;
                 }
@@ -539,23 +547,59 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < d.nb3 * 4; i += blockDim.x) {
-        const float v = acc3[i];
-        if (v == 0.0f) continue;
-        const int bin = i >> 2, s = i & 3;
-        if (s < 3) atomicAdd(P3 + (long long)bin * 3 + s, (double)v);
-        else atomicAdd(PH + bin, (double)v);
+    if (!part) {
+        for (int i = threadIdx.x; i < d.nb3 * 4; i += blockDim.x) {
+            const float v = acc3[i];
+            if (v == 0.0f) continue;
+            const int bin = i >> 2, s = i & 3;
+            if (s < 3) atomicAdd(P3 + (long long)bin * 3 + s, (double)v);
+            else atomicAdd(PH + bin, (double)v);
+        }
     }
     if (AXIS != 2) {
         for (int i = threadIdx.x; i < d.nb1; i += blockDim.x) {
             const float v = acc1[i];
             if (v != 0.0f) atomicAdd(P1 + i, (double)v);
         }
-        const int kpar = abs(freq_of(it.plane, dims));
-        for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) {
-            const float v = acc2[i];
+        if (!part) {
+            const int kpar = abs(freq_of(it.plane, dims));
+            for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) {
+                const float v = acc2[i];
+                if (v == 0.0f) continue;
+                atomicAdd(P2 + (long long)(d.kmax_par + 1) * i + kpar, (double)v);
+            }
+        }
+    }
+}
+
+// Per-CTA partial sums of pk_bin_seq_kernel into the float64 sums.  3D slots:
+// blockIdx.y splits the CTAs into groups, each thread sums one slot over its
+// group in float64.  k_per slots (axes 0/1): each CTA's plane fixes k_par, so a
+// thread per (CTA, k_per) adds its value where it belongs.
+__global__ void __launch_bounds__(256) pk_part_reduce_kernel(const float *__restrict__ part, int n_cta,
+                                                             int stride, int per_group, int chunks, int axis,
+                                                             PkDims d, double *__restrict__ sums)
+{
+    double *P3 = sums, *PH = P3 + (long long)d.nb3 * 3;
+    double *P2 = PH + d.nb3 + d.nb1;
+    const int n3 = d.nb3 * 4;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c0 = blockIdx.y * per_group, c1 = min(n_cta, c0 + per_group);
+    if (s < n3) {
+        double acc = 0.0;
+        for (int c = c0; c < c1; c++) acc += (double)part[(long long)c * stride + s];
+        if (acc != 0.0) {
+            const int bin = s >> 2, k = s & 3;
+            if (k < 3) atomicAdd(P3 + (long long)bin * 3 + k, acc);
+            else atomicAdd(PH + bin, acc);
+        }
+    } else if (axis != 2 && s < n3 + d.kmax_per + 1) {
+        const int kper = s - n3;
+        for (int c = c0; c < c1; c++) {
+            const float v = part[(long long)c * stride + s];
             if (v == 0.0f) continue;
-            atomicAdd(P2 + (long long)(d.kmax_par + 1) * i + kpar, (double)v);
+            const int kpar = abs(freq_of(c / chunks, d.dims));
+            atomicAdd(P2 + (long long)(d.kmax_par + 1) * kper + kpar, (double)v);
         }
     }
 }
@@ -738,16 +782,45 @@ inline int plane_chunks(int dims)
 constexpr int RING_ROWS_PER_CTA = 256;
 constexpr size_t SMEM_LIMIT = 200 * 1024;
 
+// One-field launches (pk_bin_seq_kernel): axes 0/1 give each plane c CTAs, enough
+// for several waves at 2-3 resident CTAs per SM; axis 2 walks the ring table.
+inline int seq_plane_chunks(int dims)
+{
+    int c = 1;
+    while ((long long)dims * c < 8LL * num_sms() && c * 2 * NW <= dims) c *= 2;
+    return c;
+}
+
+struct SeqPart {
+    unsigned blocks;
+    int stride;           // floats per CTA (a multiple of 4: float4 slots stay aligned)
+    size_t bytes;
+};
+
+inline SeqPart seq_part(const PkDims &d, int axis)
+{
+    SeqPart p;
+    p.blocks = axis == 2 ? (unsigned)(((long long)d.dims * d.dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA)
+                         : (unsigned)(d.dims * seq_plane_chunks(d.dims));
+    p.stride = (d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1) + 3) & ~3;
+    p.bytes = align256(sizeof(float) * (size_t)p.blocks * p.stride);
+    return p;
+}
+
 }  // namespace
 }  // namespace pyl
 
 using namespace pyl;
 
+// axis 2: the ring table; one field: the per-CTA partial sums of the bin flushes
+// (without them, the flushes fall back to float shared-memory atomics).
 extern "C" size_t pyl_pk_workspace_size(int dims, int n_fields, int axis)
 {
-    (void)n_fields;
-    if (dims < 2 || axis != 2) return 0;
-    return ring_layout(nullptr, pk_dims(dims)).bytes;
+    if (dims < 2) return 0;
+    const PkDims d = pk_dims(dims);
+    size_t bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
+    if (n_fields == 1) bytes += seq_part(d, axis).bytes;
+    return bytes;
 }
 
 extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_fields, int64_t field_stride,
@@ -776,6 +849,8 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     a.geom = nullptr;
     a.d = d;
     a.rows = nullptr;
+    a.part = nullptr;
+    a.part_stride = 0;
     for (int f = 0; f < MAX_FIELDS; f++) {
         a.mas_p[f] = f < n_fields ? host_mas_p[f] : 0;
         PYL_CHECK_ARG(a.mas_p[f] >= 0 && a.mas_p[f] <= 4, "MAS exponent must be 0..4");
@@ -805,15 +880,19 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     if (n_fields == 1 && (axis != 2 || a.warp_arrays)) {
         const int chunk = seq_chunk(d.nz);
         if (axis != 2) {
-            // enough CTAs for several waves at 2-3 resident CTAs per SM
-            int c = 1;
-            while ((long long)dims * c < 8LL * num_sms() && c * 2 * NW <= dims) c *= 2;
-            a.chunks = c;
-            blocks = (unsigned)(dims * c);
+            a.chunks = seq_plane_chunks(dims);
+            blocks = (unsigned)(dims * a.chunks);
         }
         const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk).total;
         if (sms <= SMEM_LIMIT) {
             PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
+            const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
+            const SeqPart sp = seq_part(d, axis);
+            a.part_stride = sp.stride;
+            if (workspace != nullptr && workspace_bytes >= ring_bytes + sp.bytes && sp.blocks == blocks) {
+                a.part = (float *)((char *)workspace + ring_bytes);
+                PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride, st));
+            }
 #define PYL_SEQ(I, A)                                                              \
     do {                                                                           \
         PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms));                \
@@ -826,6 +905,13 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
             }
 #undef PYL_SEQ
             PYL_LAUNCH_CHECK();
+            if (a.part) {
+                const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
+                const int groups = 16, per_group = (int)((blocks + groups - 1) / groups);
+                pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups), 256, 0, st>>>(
+                    a.part, (int)blocks, sp.stride, per_group, a.chunks, axis, d, sums);
+                PYL_LAUNCH_CHECK();
+            }
             return PYL_OK;
         }
     }
@@ -877,6 +963,8 @@ extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace
     a.geom = geom;
     a.d = d;
     a.rows = nullptr;
+    a.part = nullptr;
+    a.part_stride = 0;
     for (int f = 0; f < MAX_FIELDS; f++) a.mas_p[f] = 0;
     unsigned blocks;
     if (axis == 2) {
