@@ -19,6 +19,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -133,7 +134,10 @@ class ClockSampler(object):
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, 'gpurun_out', 'clocks_bench.csv')
+        # the raw samples (kept beside the run's other output when PYL_CLOCKS_DIR
+        # names a directory); the JSON line carries their summary
+        out_dir = os.environ.get('PYL_CLOCKS_DIR') or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, 'clocks_bench_%d.csv' % os.getpid())
 
     def start(self):
         try:
@@ -309,14 +313,23 @@ def main():
                                 interlaced=True, strategy=a.strategy, parallelism='replicas',
                                 l2_flush='inputs larger than L2 (12.9 GB positions)'),
                     e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
-                    gpu_launches=KERNELS_PER_STEP * a.steps, stages_ms=stages,
+                    gpu_launches=kernels_per_step(dims) * a.steps, stages_ms=stages,
                     secondary=secondary)
         print(json.dumps(line))
 
 
-# our kernels per step: 2 fills, histogram, column scan, tile scan, level-A and level-B
-# placement, deposit, P(k) bin
-KERNELS_PER_STEP = 9
+def kernels_per_step(dims):
+    """This library's kernel launches in one CIC-interlaced step (cuFFT's not counted):
+    histogram, column scan, tile scan; placement (by bin in one pass up to 1024 bins,
+    else the coherence-gated direct scatter + level A + level B); the deposit; on grids
+    of 1024^3 and up (multiples of 32) the halo kernel, below that two fills; P(k)
+    binning and the reduction of its per-CTA partial sums."""
+    nt = -(-dims // 32)
+    nc = -(-nt // 4)
+    tiles = nc ** 3 * 64
+    owned = dims % 32 == 0 and dims >= 1024
+    placement = 1 if tiles <= 1024 else 3
+    return 3 + placement + 1 + (1 if owned else 2) + 2
 
 
 def bench_zeldovich(reps=3):
