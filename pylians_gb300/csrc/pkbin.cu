@@ -360,16 +360,18 @@ struct SeqSmem {
     int corr, ph, acc3, acc1, acc2, w, stage, total;
 };
 
-__host__ __device__ inline SeqSmem seq_smem(const PkDims &d, int axis, bool inter, int chunk)
+// part: the 3D and k_per flushes go to global partial sums, so their shared
+// arrays are left out (more resident CTAs).
+__host__ __device__ inline SeqSmem seq_smem(const PkDims &d, int axis, bool inter, int chunk, bool part)
 {
     SeqSmem s;
     int o = 0;
     s.corr = o; o += d.dims;
     o = (o + 3) & ~3;
     s.ph = o; o += inter ? 2 * d.dims : 0;
-    s.acc3 = o; o += d.nb3 * 4;
+    s.acc3 = o; o += part ? 0 : d.nb3 * 4;
     s.acc1 = o; o += d.nb1;
-    s.acc2 = o; o += axis == 2 ? 0 : d.kmax_per + 1;
+    s.acc2 = o; o += (axis == 2 || part) ? 0 : d.kmax_per + 1;
     s.w = o; o += axis == 2 ? NW * 2 * d.nz : 0;
     o = (o + 3) & ~3;
     s.stage = o; o += NW * 2 * 32 * (chunk + 1);
@@ -393,7 +395,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     extern __shared__ float sm[];
     const PkDims d = a.d;
     const int dims = d.dims, nz = d.nz;
-    const SeqSmem L = seq_smem(d, AXIS, INTER, chunk);
+    const SeqSmem L = seq_smem(d, AXIS, INTER, chunk, a.part != nullptr);
     float *corr = sm + L.corr;
     float2 *ph = (float2 *)(sm + L.ph);
     float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
@@ -883,13 +885,14 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
             a.chunks = seq_plane_chunks(dims);
             blocks = (unsigned)(dims * a.chunks);
         }
-        const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk).total;
+        const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
+        const SeqPart sp = seq_part(d, axis);
+        const bool use_part = workspace != nullptr && workspace_bytes >= ring_bytes + sp.bytes && sp.blocks == blocks;
+        const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk, use_part).total;
         if (sms <= SMEM_LIMIT) {
             PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
-            const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
-            const SeqPart sp = seq_part(d, axis);
             a.part_stride = sp.stride;
-            if (workspace != nullptr && workspace_bytes >= ring_bytes + sp.bytes && sp.blocks == blocks) {
+            if (use_part) {
                 a.part = (float *)((char *)workspace + ring_bytes);
                 PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride, st));
             }
