@@ -135,46 +135,6 @@ __device__ __forceinline__ int fx_support(const float4 &r, float inv, float half
     return base;
 }
 
-// All weights non-negative and not NaN (CIC: u >= 0; TSC/PCS weights are >= 0
-// for finite positions by construction).
-template <int MAS>
-__device__ __forceinline__ bool fx_weights_ok(const float (*C)[Support<MAS>::S])
-{
-    if (MAS == PYL_MAS_NGP) return true;
-    bool ok = true;
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int j = 0; j < Support<MAS>::S; j++) ok = ok && C[a][j] >= 0.0f;
-    return ok;
-}
-
-template <int MAS, int E>
-__device__ __forceinline__ unsigned fx_scatter(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
-{
-    constexpr int S = Support<MAS>::S;
-    if (MAS == PYL_MAS_NGP) {
-        atomicAdd(acc + base, 1u);       // a bin holds < 2^32 particles: no wrap
-        return 0u;
-    }
-    unsigned wrapped = 0u;
-#pragma unroll
-    for (int l = 0; l < S; l++)
-#pragma unroll
-        for (int m = 0; m < S; m++) {
-            const float c01 = __fmul_rn(C[0][l], C[1][m]);
-            const int row = base + (l * E + m) * E;
-#pragma unroll
-            for (int q = 0; q < S; q++) {
-                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
-                const unsigned qv = __float_as_uint(x) - FX_MAGIC_BITS;
-                const unsigned old = atomicAdd(acc + row + q, qv);
-                wrapped |= (unsigned)(old + qv < old);
-            }
-        }
-    return wrapped;
-}
-
 template <int MAS, int E>
 __device__ __forceinline__ void float_scatter(float *acc, int base, const float (*C)[Support<MAS>::S])
 {
@@ -190,11 +150,13 @@ __device__ __forceinline__ void float_scatter(float *acc, int base, const float 
         }
 }
 
-template <int MAS, int E>
+// COUNT: unweighted NGP adds one integer count per particle; otherwise every
+// corner adds its fixed-point weight (weighted NGP: C holds the scaled weight).
+template <int MAS, int E, bool COUNT = (MAS == PYL_MAS_NGP)>
 __device__ __forceinline__ unsigned fx_scatter_or(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
 {
     constexpr int S = Support<MAS>::S;
-    if (MAS == PYL_MAS_NGP) {
+    if (COUNT) {
         atomicAdd(acc + base, 1u);
         return 0u;
     }

@@ -785,135 +785,48 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *__restr
     if (threadIdx.x == blockDim.x - 1) offsets[n] = (unsigned)part[threadIdx.x];
 }
 
-// Deposit sub-tile: half a bin along x (TB/2 x TB x TB cells) plus the halo.
-template <int MAS, bool INTER, bool FIXED>
-struct TileShape {
-    static constexpr int H = Support<MAS>::S - 1 + (INTER ? 1 : 0);   // halo on the + side
-    static constexpr int HX = TB / 2;
-    static constexpr int EX = HX + H, E = TB + H;
-    static constexpr int CELLS = EX * E * E;
-    // FIXED: lo + hi words of one grid at a time; float: one word per grid, both grids
-    static constexpr size_t SMEM = sizeof(unsigned) * CELLS * (FIXED ? 2 : (INTER ? 2 : 1));
-};
+// Weighted deposits accumulate weight / max|weight| in the fixed-point sums when the
+// weights span at most a factor W_FX_RANGE (contributions are exact to 2^-23 of
+// the largest weight, about the float rounding of the reference's sums); wider
+// ranges, all-zero or non-finite weights take the float32 shared-memory sums.
+// abs_range_kernel: max and min of the non-zero |w| (NaN skipped) as float bits,
+// which order like unsigned integers for non-negative floats.
+constexpr float W_FX_RANGE = 16.0f;
 
-// Exact signed 64-bit fixed-point accumulation (2^-32 units) from two 32-bit
-// shared-memory integer atomics: the low word's carry goes to the high word.
-// Integer sums do not depend on the order of the adds.
-__device__ __forceinline__ void fx_add(unsigned *lo, unsigned *hi, int c, float v)
+__global__ void __launch_bounds__(256) abs_range_kernel(const float *__restrict__ w, long long n,
+                                                        unsigned *__restrict__ bits)
 {
-    // signed: floor gives the (possibly negative) integer part, the fraction is in [0, 1)
-    const float fi = floorf(v);
-    const unsigned qh = (unsigned)__float2int_rz(fi);
-    const unsigned ql = __float2uint_rn(__fsub_rn(v, fi) * 4294967296.0f);
-    unsigned carry = 0;
-    if (ql) {
-        const unsigned old = atomicAdd(lo + c, ql);
-        carry = (unsigned)(old + ql) < old ? 1u : 0u;
+    float hi = 0.0f, lo = __int_as_float(0x7f800000);       // +inf
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float a = fabsf(__ldg(w + i));
+        if (a > hi) hi = a;                                 // comparisons are false for NaN
+        if (a > 0.0f && a < lo) lo = a;
     }
-    if (qh + carry) atomicAdd(hi + c, qh + carry);
-}
-
-__device__ __forceinline__ float fx_value(unsigned lo, unsigned hi)
-{
-    return __fadd_rn((float)(int)hi, __uint2float_rn(lo) * 2.3283064365386963e-10f);
-}
-
-// Weights and local first cells of one particle for the plain (G=0) or the
-// half-cell-shifted (G=1) grid; loc relative to the sub-tile origin o.
-template <int MAS, int G>
-__device__ __forceinline__ void particle_support(const float *p, float inv, float halfcell, int dims,
-                                                 const int *o, int lx0, int fx0,
-                                                 float (*C)[Support<MAS>::S], int *loc)
-{
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int f0 = a == 0 ? fx0 : axis_first<MAS>(p[a], inv);
-        loc[a] = a == 0 ? lx0 : wrap_index(f0, dims) - o[a];
-        if (G == 1) {
-            // the half-cell shift moves the first cell by 0 or +1; the clamp only
-            // matters for non-finite or astronomically large positions
-            const int f = axis_weights<MAS>(__fadd_rn(p[a], halfcell), inv, C[a]);
-            loc[a] += f > f0 ? 1 : 0;
-        } else {
-            axis_weights<MAS>(p[a], inv, C[a]);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (hi > 0.0f) atomicMax(bits, __float_as_uint(hi));
+        atomicMin(bits + 1, __float_as_uint(lo));
     }
 }
 
-// One CTA per TB^3 bin.  The bin is deposited as two x-halves; each half is a
-// shared-memory block with the + side halo, added to the grid(s) with coalesced
-// red.global.add when done.  FIXED (unweighted only): exact order-independent
-// fixed-point sums, one grid per pass over the bin's particles; otherwise float32
-// shared atomics, both grids in one pass.  Re-reads of a bin's particles hit L2.
-template <int MAS, bool WEIGHTED, bool INTER, bool FIXED>
-__global__ void __launch_bounds__(1024) bin_deposit_kernel(
-    const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
-    float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc)
+// wsc: [0] max bits, [1] min bits (from abs_range_kernel), [2] 1 / max|w| (1 on
+// the float path), [3] output scale (x max|w| on the fixed-point path; x 2^-22
+// for NGP, whose fixed-point sums are read as counts), [4] 1: float path.
+__global__ void w_scale_kernel(float *wsc, float host_scale, const float *dev_scale, int ngp)
 {
-    using TS = TileShape<MAS, INTER, FIXED>;
-    const float scale = out_scale(sc);
-    constexpr int S = Support<MAS>::S, E = TS::E, HX = TS::HX, CELLS = TS::CELLS;
-    extern __shared__ unsigned smw[];
-    const long long tile = blockIdx.x;
-    const unsigned begin = offsets[tile], end = offsets[tile + 1];
-    if (begin == end) return;
-    int tx, ty, tz;
-    tile_coords(tile, g, tx, ty, tz);
-    const long long d = g.dims;
-    constexpr int PASSES = FIXED && INTER ? 2 : 1;
-    for (int half = 0; half < 2; half++) {
-        const int o[3] = {tx * TB + half * HX, ty * TB, tz * TB};
-        if (o[0] >= g.dims) break;                  // ragged last bin: no second half
-        for (int pass = 0; pass < PASSES; pass++) {
-            constexpr int WORDS = FIXED ? 2 * CELLS : (INTER ? 2 : 1) * CELLS;
-            for (int c = threadIdx.x; c < WORDS; c += blockDim.x) smw[c] = 0u;
-            __syncthreads();
-            for (unsigned i = begin + threadIdx.x; i < end; i += blockDim.x) {
-                const float4 r = rec[i];
-                const float p[3] = {r.x, r.y, r.z};
-                const int fx0 = axis_first<MAS>(p[0], inv);
-                const int lx0 = wrap_index(fx0, g.dims) - o[0];
-                if (lx0 < 0 || lx0 >= HX) continue;          // the other half's particle
-                float C[3][S];
-                int loc[3];
-#pragma unroll
-                for (int gi = 0; gi < (FIXED ? 1 : (INTER ? 2 : 1)); gi++) {
-                    const int G = FIXED ? pass : gi;
-                    if (G == 0) particle_support<MAS, 0>(p, inv, halfcell, g.dims, o, lx0, fx0, C, loc);
-                    else        particle_support<MAS, 1>(p, inv, halfcell, g.dims, o, lx0, fx0, C, loc);
-                    float *facc = (float *)smw + gi * CELLS;
-#pragma unroll
-                    for (int l = 0; l < S; l++)
-#pragma unroll
-                        for (int m = 0; m < S; m++) {
-                            const float c01 = __fmul_rn(C[0][l], C[1][m]);
-                            const int row = ((loc[0] + l) * E + (loc[1] + m)) * E + loc[2];
-#pragma unroll
-                            for (int q = 0; q < S; q++) {
-                                float v = __fmul_rn(c01, C[2][q]);
-                                if (WEIGHTED) v = __fmul_rn(v, r.w);
-                                if (FIXED) fx_add(smw, smw + CELLS, row + q, v);
-                                else atomicAdd(facc + row + q, v);
-                            }
-                        }
-                }
-            }
-            __syncthreads();
-            for (int gi = 0; gi < (FIXED ? 1 : (INTER ? 2 : 1)); gi++) {
-                float *out = (FIXED ? pass : gi) == 0 ? grid : grid2;
-                const float *facc = (const float *)smw + gi * CELLS;
-                for (int c = threadIdx.x; c < CELLS; c += blockDim.x) {
-                    const float v = FIXED ? fx_value(smw[c], smw[CELLS + c]) : facc[c];
-                    if (v == 0.0f) continue;
-                    const int lz = c % E, ly = (c / E) % E, lx = c / (E * E);
-                    const long long gx = add_wrap(o[0], lx, d), gy = add_wrap(o[1], ly, d),
-                                    gz = add_wrap(o[2], lz, d);
-                    atomicAdd(out + (gx * d + gy) * d + gz, __fmul_rn(v, scale));
-                }
-            }
-            __syncthreads();
-        }
-    }
+    const unsigned *bits = (const unsigned *)wsc;
+    const float wmax = __uint_as_float(bits[0]), wmin = __uint_as_float(bits[1]);
+    const bool fx = wmax > 0.0f && isfinite(wmax) && wmax <= W_FX_RANGE * wmin;
+    const float base = dev_scale ? *dev_scale : host_scale;
+    wsc[2] = fx ? __frcp_rn(wmax) : 1.0f;
+    const float s = fx ? __fmul_rn(base, wmax) : base;
+    wsc[3] = ngp ? __fmul_rn(s, FX_INV) : s;
+    reinterpret_cast<int *>(wsc)[4] = fx ? 0 : 1;
 }
 
 __global__ void scale_kernel(float *g, long long n, float div)
@@ -976,6 +889,7 @@ struct TiledWs {
     float4 *tmp;                 // two-level placement: the coarse-block layout
     float *halo;                 // owned-cell write-out: per-bin halo blocks
     unsigned long long *same;    // coherence count of the histogram pass
+    float *wsc;                  // weighted deposits: w_scale_kernel's 5 words
     int chunks;
     bool smem_hist;
     size_t bytes;
@@ -997,6 +911,7 @@ TiledWs tiled_layout(void *base, long long n, int dims, size_t halo_floats = 0)
     ws.total = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * g.ntiles, 256);
     ws.offsets = (unsigned *)(b + off); off = align_up(off + sizeof(unsigned) * (g.ntiles + 1), 256);
     ws.same = (unsigned long long *)(b + off); off = align_up(off + sizeof(unsigned long long), 256);
+    ws.wsc = (float *)(b + off); off = align_up(off + sizeof(float) * 8, 256);
     ws.rec = (float4 *)(b + off); off = align_up(off + sizeof(float4) * (size_t)n, 256);
     ws.tmp = nullptr;
     if (ws.smem_hist && g.ntiles > TWO_LEVEL_TILES) {
@@ -1079,6 +994,8 @@ struct FxStage {
     float4 *inb;                       // [2][R] staging buffers
     unsigned long long *bar;           // one mbarrier per buffer
     int *ok;
+    const float *inv_w;                // weighted: 1 / max |w| (weights scaled into [-1, 1]); null: unweighted
+    const int *use_float;              // weighted: 1 -> float32 sums from the start
 };
 
 // One pass over the bin's records into shared memory.  Returns 1 when the pass
@@ -1104,6 +1021,8 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
                        &sg.bar[q & 1]);
         }
     __syncthreads();
+    const bool weighted = sg.inv_w != nullptr;
+    const float inv_w = weighted ? *sg.inv_w : 1.0f;
     unsigned bad = 0u, seen = 0u;
     for (unsigned j = 0; j < sg.nb; j++) {
         const unsigned q = q0 + j;
@@ -1130,11 +1049,22 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
             const int base = (axis_local<MAS, G, P2>(r[u].x, inv, halfcell, dims, o[0], C[0]) * E +
                               axis_local<MAS, G, P2>(r[u].y, inv, halfcell, dims, o[1], C[1])) * E +
                              axis_local<MAS, G, P2>(r[u].z, inv, halfcell, dims, o[2], C[2]);
+            float wq = 1.0f;
+            if (weighted) {                                 // the scaled weight joins the x weights
+                wq = __fmul_rn(r[u].w, inv_w);
+#pragma unroll
+                for (int l = 0; l < S; l++) C[0][l] = __fmul_rn(C[0][l], wq);
+            }
             if (FLOAT) {
                 float_scatter<MAS, E>((float *)smw, base, C);
             } else {
                 if (MAS == PYL_MAS_CIC) bad |= (unsigned)!(C[0][1] >= 0.0f && C[1][1] >= 0.0f && C[2][1] >= 0.0f);
-                seen |= fx_scatter_or<MAS, E>(smw, base, C);
+                if (weighted) {
+                    bad |= (unsigned)!(wq >= 0.0f);            // negative or NaN weight
+                    seen |= fx_scatter_or<MAS, E, false>(smw, base, C);
+                } else {
+                    seen |= fx_scatter_or<MAS, E>(smw, base, C);
+                }
             }
         }
     }
@@ -1357,17 +1287,23 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
                                         const int *o, unsigned *smw, float *out, bool interior, float scale,
                                         const Owned &ow, float *halo_bin, const float *prev)
 {
-    int st = fx_accumulate<MAS, INTER, R, G, false, P2>(sg, q0, inv, halfcell, dims, o, smw);
-    if (st < 0) return false;
-    q0 += sg.nb;
+    int st = 1;                                             // float32 from the start
+    if (!(sg.use_float && *sg.use_float)) {
+        st = fx_accumulate<MAS, INTER, R, G, false, P2>(sg, q0, inv, halfcell, dims, o, smw);
+        if (st < 0) return false;
+        q0 += sg.nb;
+    }
     if (st == 0) {
         if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
     } else {
         if (fx_accumulate<MAS, INTER, R, G, true, P2>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
         q0 += sg.nb;
-        if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
-        else fx_write_out<MAS, INTER, true>(smw, out, o, dims, interior, scale);
+        // weighted NGP: `scale` carries the 2^-22 of the fixed-point sums, which
+        // float sums do not need
+        const float fs = (MAS == PYL_MAS_NGP && sg.inv_w) ? __fmul_rn(scale, FX_SCALE) : scale;
+        if (ow.on) fx_store_owned<MAS, INTER, true>(smw, out, halo_bin, o, dims, fs, ow, prev, (float *)sg.inb);
+        else fx_write_out<MAS, INTER, true>(smw, out, o, dims, interior, fs);
     }
     __syncthreads();                                        // cells read before the next pass zeroes them
     return true;
@@ -1377,7 +1313,7 @@ template <int MAS, bool INTER, int R, bool P2>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
     float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
-    Owned ow)
+    Owned ow, const float *inv_w)
 {
     using FS = FxShape<MAS, INTER>;
     constexpr int E = FS::E;
@@ -1416,6 +1352,8 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
         sg.inb = (float4 *)(smw + FS::SMEM / 4);
         sg.bar = bar;
         sg.ok = &s_ok;
+        sg.inv_w = inv_w;
+        sg.use_float = inv_w ? reinterpret_cast<const int *>(inv_w + 2) : nullptr;
         float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
         const float *prev = have_prev && hb ? hb - HC : nullptr;
         if (!fx_grid<MAS, INTER, R, 0, P2>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
@@ -1438,7 +1376,7 @@ constexpr int fx_tma_batch()
 
 template <int MAS, bool I>
 int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                      float *grid2, OutScale sc, cudaStream_t st, const Owned &ow = Owned{false, nullptr, 0, 0.0f, 0})
+                      float *grid2, OutScale sc, cudaStream_t st, const Owned &ow, const float *inv_w)
 {
     using FS = FxShape<MAS, I>;
     constexpr int R = fx_tma_batch<MAS, I>();
@@ -1450,7 +1388,7 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
         PYL_CUDA(ensure_smem(kern, smem));
         const unsigned ctas = (unsigned)(ow.on ? g.ntiles / OWN_Z : g.ntiles);
-        kern<<<ctas, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n, ow);
+        kern<<<ctas, 1024, smem, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc, ws.n, ow, inv_w);
         PYL_LAUNCH_CHECK();
         if constexpr (FS::H > 0) {
             if (ow.on) {
@@ -1469,27 +1407,13 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
     return PYL_ERR_UNSUPPORTED;
 }
 
-template <int MAS, bool W, bool I, bool FX>
-int launch_deposit(const TiledWs &ws, TileGeom g, float inv, float halfcell, float *grid,
-                   float *grid2, OutScale sc, cudaStream_t st)
-{
-    using TS = TileShape<MAS, I, FX>;
-    auto kern = bin_deposit_kernel<MAS, W, I, FX>;
-    PYL_CUDA(ensure_smem(kern, TS::SMEM));
-    kern<<<(unsigned)g.ntiles, 1024, TS::SMEM, st>>>(ws.rec, ws.offsets, g, inv, halfcell, grid, grid2, sc);
-    PYL_LAUNCH_CHECK();
-    return PYL_OK;
-}
 
 template <int MAS>
 int launch_tiled(const float *pos, const float *w, long long n, float *grid, float *grid2,
                  int dims, float inv, float halfcell, void *workspace, OutScale sc, cudaStream_t st,
                  const RsdArgs *rsd = nullptr, Owned ow = Owned{false, nullptr, 0, 0.0f, 0})
 {
-    if (ow.on && (w || !FxShape<MAS, true>::FITS)) {
-        set_error("owned-cell write-out is for unweighted fixed-point deposits");
-        return PYL_ERR_INVALID;
-    }
+
     TileGeom g = tile_geom(dims);
     TiledWs ws = tiled_layout(workspace, n, dims);
     const int T = (int)g.ntiles;
@@ -1617,15 +1541,20 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         PYL_LAUNCH_CHECK();
     }
     stage_mark(PYL_STAGE_DEPOSIT, true, st);
-    int rc;
-    if (w) rc = grid2 ? launch_deposit<MAS, true, true, false>(ws, g, inv, halfcell, grid, grid2, sc, st)
-                      : launch_deposit<MAS, true, false, false>(ws, g, inv, halfcell, grid, grid2, sc, st);
-    else if (grid2) rc = FxShape<MAS, true>::FITS
-                             ? launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st, ow)
-                             : launch_deposit<MAS, false, true, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
-    else rc = FxShape<MAS, false>::FITS
-                  ? launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st, ow)
-                  : launch_deposit<MAS, false, false, true>(ws, g, inv, halfcell, grid, grid2, sc, st);
+    static_assert(FxShape<MAS, true>::FITS, "a bin with its halo fits shared memory");
+    const float *inv_w = nullptr;
+    if (w) {
+        PYL_CUDA(cudaMemsetAsync(ws.wsc, 0, sizeof(unsigned), st));
+        PYL_CUDA(cudaMemsetAsync(ws.wsc + 1, 0x7f, sizeof(unsigned), st));      // 0x7f7f7f7f: finite, large
+        abs_range_kernel<<<grid_blocks(n, 256, 4), 256, 0, st>>>(w, n, (unsigned *)ws.wsc);
+        PYL_LAUNCH_CHECK();
+        w_scale_kernel<<<1, 1, 0, st>>>(ws.wsc, sc.host, sc.dev, MAS == PYL_MAS_NGP ? 1 : 0);
+        PYL_LAUNCH_CHECK();
+        inv_w = ws.wsc + 2;
+        sc = OutScale{0.0f, ws.wsc + 3};
+    }
+    const int rc = grid2 ? launch_deposit_fx<MAS, true>(ws, g, inv, halfcell, grid, grid2, sc, st, ow, inv_w)
+                         : launch_deposit_fx<MAS, false>(ws, g, inv, halfcell, grid, grid2, sc, st, ow, inv_w);
     stage_mark(PYL_STAGE_DEPOSIT, false, st);
     return rc;
 }
@@ -1699,7 +1628,7 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
         // owned-cell write-out when the workspace also holds the halo blocks
         const size_t need_owned =
             tiled_layout(nullptr, n, dims, owned_halo_floats(mas, dims, grid_interlaced != nullptr)).bytes;
-        ow.on = owned_applies(dims) && weights == nullptr && workspace_bytes >= need_owned;
+        ow.on = owned_applies(dims) && workspace_bytes >= need_owned;
     }
     int rc = PYL_OK;
     if (n > 0) {
@@ -1803,7 +1732,7 @@ int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float
     int s = pick_strategy(strategy, 3, dims, n);
     if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
     // the owned-cell write-out stores -1 + value into every cell: no fill pass
-    const Owned ow{s == PYL_STRATEGY_TILED && weights == nullptr && owned_applies(dims), nullptr, 1, -1.0f, 0};
+    const Owned ow{s == PYL_STRATEGY_TILED && owned_applies(dims), nullptr, 1, -1.0f, 0};
     if (!ow.on) {
         const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
         stage_mark(PYL_STAGE_FILL, true, st);

@@ -275,6 +275,31 @@ def test_owned_cell_write_out_accumulates(MASL, mas, inter):
         assert torch.equal(got, again)
 
 
+@pytest.mark.parametrize('mas', MAS_LIST)
+def test_weighted_fixed_point_edge_weights(MASL, mas):
+    """Weighted tiled deposits accumulate weight / max|weight| in fixed point: weights
+    spanning six decades, a negative weight (the bin is redone in float32) and all
+    zero weights must all match the oracle (tolerance 2e-6 of the grid maximum)."""
+    rng = np.random.default_rng(41)
+    N, L, n = 96, 1000.0, 1_500_000
+    pos = (rng.random((n, 3)) * L).astype(np.float32)
+    wide = (10.0 ** rng.uniform(-3, 3, n)).astype(np.float32)
+    neg = (rng.random(n) + 0.5).astype(np.float32)
+    neg[12345] = -2.0
+    zero = np.zeros(n, np.float32)
+    for W in (wide, neg, zero):
+        g = torch.zeros((N, N, N), device='cuda')
+        g2 = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(torch.from_numpy(pos).cuda(), g, L, mas, torch.from_numpy(W).cuda(), interlaced=g2,
+                strategy='tiled')
+        o = np.zeros((N, N, N), np.float32)
+        O.MA(pos, o, L, mas, W, threads=os.cpu_count() or 1)
+        got = g.cpu().numpy()
+        assert np.abs(got - o).max() <= 2e-6 * max(np.abs(o).max(), 1e-30), (mas, np.abs(got - o).max())
+        if not W.any():
+            assert not got.any() and not g2.cpu().numpy().any()
+
+
 @pytest.mark.parametrize('mas', ['CIC', 'TSC', 'PCS'])
 def test_fixed_point_overflow_falls_back(MASL, mas):
     """The tiled deposit accumulates a bin in 10.22 fixed point (cell sums below 1024).
