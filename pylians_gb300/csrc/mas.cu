@@ -126,6 +126,7 @@ constexpr int MAX_CHUNKS = 512;
 struct TileGeom {
     int dims, nt, nc;      // grid side, tiles per axis, coarse blocks (4^3 tiles) per axis
     long long ntiles;      // number of tile keys: nc^3 * 64 (keys of tiles past the grid stay empty)
+    unsigned mask;         // dims - 1 for power-of-two grids (cells wrap by a mask), else 0
 };
 
 __host__ __device__ inline TileGeom tile_geom(int dims)
@@ -135,6 +136,7 @@ __host__ __device__ inline TileGeom tile_geom(int dims)
     g.nt = (dims + TB - 1) / TB;
     g.nc = (g.nt + 3) / 4;
     g.ntiles = (long long)g.nc * g.nc * g.nc * 64;
+    g.mask = (dims & (dims - 1)) == 0 ? (unsigned)dims - 1u : 0u;
     return g;
 }
 
@@ -163,7 +165,8 @@ __device__ __forceinline__ unsigned tile_key(const float *p, float inv, const Ti
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int f = axis_first<MAS>(p[a], inv);
-        c[a] = (unsigned)f < (unsigned)g.dims ? (unsigned)f : (unsigned)wrap_index(f, g.dims);   // rare: past the edge
+        if (g.mask) c[a] = (unsigned)f & g.mask;                 // a uniform branch: the same for all threads
+        else c[a] = (unsigned)f < (unsigned)g.dims ? (unsigned)f : (unsigned)wrap_index(f, g.dims);   // rare: past the edge
     }
     return tile_key_of(c[0] / TB, c[1] / TB, c[2] / TB, g);
 }
