@@ -468,10 +468,12 @@ __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *pos, 
                     mbar_wait_bounded(&bar[k % HT_NBUF], (unsigned)((k / HT_NBUF) & 1), &g_tma_error);
             return;
         }
+        // every batch but a chunk's last is fully staged: no per-particle fallback test
+        const bool all_staged = full == HT_BATCH;
         for (int i = threadIdx.x; i < c; i += blockDim.x) {
             float p[3];
             const long long q = s0 + i;
-            if (i < full) { p[0] = in[3 * i]; p[1] = in[3 * i + 1]; p[2] = in[3 * i + 2]; }
+            if (all_staged || i < full) { p[0] = in[3 * i]; p[1] = in[3 * i + 1]; p[2] = in[3 * i + 2]; }
             else { p[0] = pos[3 * q]; p[1] = pos[3 * q + 1]; p[2] = pos[3 * q + 2]; }
             if (RSD) {
                 const float sh = rsd_shift(p[rsd.axis], __ldg(rsd.vel + 3 * q + rsd.axis), rsd.factor, rsd.box);
@@ -565,14 +567,15 @@ __global__ void __launch_bounds__(NT) level_a_tma_kernel(
                     mbar_wait_bounded(&bar[q % LA_NBUF], (unsigned)((q / LA_NBUF) & 1), &g_tma_error);
             return;
         }
+        const bool all_staged = full == BATCH;              // every batch but a chunk's last
         float4 r[LAT_U];
         unsigned co_u[LAT_U], rank[LAT_U];
 #pragma unroll
         for (int u = 0; u < LAT_U; u++) {
             const int i = threadIdx.x + u * NT;
             co_u[u] = 0xffffffffu;
-            if (i < c) {
-                if (i < full) r[u] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 1.0f);
+            if (all_staged || i < c) {
+                if (all_staged || i < full) r[u] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 1.0f);
                 else {
                     const long long q = s0 + i;
                     r[u] = make_float4(__ldg(pos + 3 * q), __ldg(pos + 3 * q + 1), __ldg(pos + 3 * q + 2), 1.0f);
