@@ -200,8 +200,10 @@ int pyl_fft_cache_clear(void);
  * pyl_pk_geometry fills the data-independent part (device, float64, zeroed):
  *   K1 [nb1] sum |k_par|, N1 [nb1], N2 [nb2], K3 [nb3] sum |k|, N3 [nb3]
  * (mode counts are exact integers stored as float64).
- * Both take a workspace of pyl_pk_workspace_size() bytes (non-zero for axis 2
- * only, where the rows are visited in k_per order).
+ * Both take a workspace of pyl_pk_workspace_size() bytes: for axis 2 the table
+ * that visits rows in k_per order (required), and for one field the per-CTA
+ * partial sums of the bin flushes (optional: with a smaller workspace the
+ * flushes go to shared memory, slower; same sums up to float32 rounding order).
  */
 int64_t pyl_pk_sums_len(int dims, int n_fields);
 int64_t pyl_pk_geometry_len(int dims);

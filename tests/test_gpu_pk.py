@@ -223,3 +223,34 @@ def test_overdensity_owned_cells_with_empty_bins(mas, N):
         ref = g.double() / mean - 1.0
         assert (d.double() - ref).abs().max().item() <= 1e-5 * ref.abs().max().item()
         assert torch.equal(d[g == 0], torch.full_like(d[g == 0], -1.0))
+
+
+@pytest.mark.parametrize('axis', [0, 2])
+def test_pk_bin_partials_match_shared_sums(PKL, axis):
+    """One-field binning flushes into per-CTA global partial sums when the caller's
+    workspace holds them (pyl_pk_workspace_size) and into shared memory otherwise
+    (axis 0 without a workspace; axis 2 with only the ring table): both must give the
+    same sums (float32 partials added in different orders: rtol 1e-5 of each bin's
+    monopole scale)."""
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr, stream_ptr
+    L = _lib.load()
+    rng = np.random.default_rng(12)
+    N = 96
+    a = torch.from_numpy(rng.standard_normal((N, N, N)).astype(np.float32)).cuda()
+    b = torch.from_numpy(rng.standard_normal((N, N, N)).astype(np.float32)).cuda()
+    dk = torch.empty((2, N, N, N // 2 + 1), dtype=torch.complex64, device='cuda')
+    _lib.call('pyl_fft_r2c', ptr(torch.stack([a, b])), ptr(dk), N, 2, stream_ptr())
+    n = L.pyl_pk_sums_len(N, 1)
+    mp, keep = PKL.ctypes_int_array([2])
+    full = L.pyl_pk_workspace_size(N, 1, axis)
+    ring = L.pyl_pk_workspace_size(N, 2, 2) if axis == 2 else 0    # ring table only (two fields: no partials)
+    ws = torch.empty(full, dtype=torch.uint8, device='cuda')
+    out = []
+    for nbytes in (full, ring):
+        s = torch.empty(n, dtype=torch.float64, device='cuda')
+        _lib.call('pyl_pk_bin', ptr(dk[0]), ptr(dk[1]), 1, 0, N, axis, mp, ptr(s),
+                  ptr(ws) if nbytes else None, nbytes, stream_ptr())
+        out.append(s.cpu().numpy())
+    scale = np.abs(out[1]).max()
+    np.testing.assert_allclose(out[0], out[1], rtol=1e-5, atol=1e-6 * scale)
