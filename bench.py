@@ -470,12 +470,16 @@ def bench_learned():
 
 STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort', 'halo')
 
-# DRAM bytes per launch of the CIC-interlaced deposit kernel measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum, one pass of counters; summary and
-# commands in profiles/bin_deposit_fx_cic_interlaced_512.md), keyed by
-# (particles, grid): the 1024^3 bench step itself, and the 512^3 case.
-DEPOSIT_TRAFFIC = {(1024 ** 3, 1024): 29.152525824e9 + 10.270216960e9,
-                   (512 ** 3, 512): 4.017201e9 + 1.101149e9}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one pass of
+# counters) of each kernel of the CIC-interlaced step measured by ncu, keyed by
+# (particles, grid); summaries and commands in profiles/cic_interlaced_pk_1024_launches.md
+# and profiles/bin_deposit_fx_cic_interlaced_512.md.
+KERNEL_TRAFFIC = {
+    (1024 ** 3, 1024): dict(hist=12.886015232e9 + 0.003792896e9, place=13.224840192e9 + 17.387312896e9,
+                            place_b=17.348109568e9 + 17.283051776e9, deposit=29.109039872e9 + 10.267560960e9,
+                            halo=4.200761600e9 + 1.484157952e9, pk_bin=8.636224512e9 + 0.022080000e9),
+    (512 ** 3, 512): dict(deposit=4.017201e9 + 1.101149e9),
+}
 
 
 def stage_times(pp, pos, reps):
@@ -540,11 +544,12 @@ def roofline(stages, n, dims, hbm, src):
     ms = {k: v for k, v in ms.items() if k in alg}
     top = max(ms, key=lambda k: ms[k])
     achieved = alg[top] / (ms[top] / 1e3) / 1e9
-    traffic = DEPOSIT_TRAFFIC.get((n, dims)) if top == 'deposit' else None
+    measured = KERNEL_TRAFFIC.get((n, dims), {})
     return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
-                frac=achieved / hbm, traffic=traffic, peak_source=src,
+                frac=achieved / hbm, traffic=measured.get(top), peak_source=src,
                 alg_bytes=alg[top], ms=ms[top],
-                all_kernels={k: dict(ms=ms[k], gbs=alg[k] / (ms[k] / 1e3) / 1e9, frac=alg[k] / (ms[k] / 1e3) / 1e9 / hbm)
+                all_kernels={k: dict(ms=ms[k], gbs=alg[k] / (ms[k] / 1e3) / 1e9,
+                                     frac=alg[k] / (ms[k] / 1e3) / 1e9 / hbm, traffic=measured.get(k))
                              for k in ms})
 
 
