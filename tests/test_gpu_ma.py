@@ -237,6 +237,26 @@ def test_coherent_placement_matches_atomic(MASL, N):
             del a1, a2, b1, b2
 
 
+def test_owned_cell_write_out_ragged_groups(MASL):
+    """1056^3 = 33 bins of 32 per side: owned-cell write-out on a grid that is not a
+    power of two (cells wrap by the general rule) whose last group of bins along z
+    holds a single bin; plain and interlaced CIC and weighted TSC against the atomic
+    strategy."""
+    rng = np.random.default_rng(57)
+    N, L, n = 1056, 1000.0, 3_000_000
+    pos = torch.from_numpy((rng.random((n, 3)) * L).astype(np.float32)).cuda()
+    w = torch.from_numpy((rng.random(n) + 0.5).astype(np.float32)).cuda()
+    for mas, W in (('CIC', None), ('TSC', w)):
+        a1 = torch.zeros((N, N, N), device='cuda'); a2 = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(pos, a1, L, mas, W, interlaced=a2, strategy='atomic')
+        b1 = torch.zeros((N, N, N), device='cuda'); b2 = torch.zeros((N, N, N), device='cuda')
+        MASL.MA(pos, b1, L, mas, W, interlaced=b2, strategy='tiled')
+        for a, b in ((a1, b1), (a2, b2)):
+            assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
+        del a1, a2, b1, b2
+        torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize('mas', MAS_LIST)
 @pytest.mark.parametrize('inter', [False, True])
 def test_owned_cell_write_out_accumulates(MASL, mas, inter):
