@@ -150,6 +150,26 @@ __device__ __forceinline__ void float_scatter(float *acc, int base, const float 
         }
 }
 
+// Adds the S^3 fixed-point corner weights without reading the old values back
+// (wraps are then found from the bin's total, see fx_accumulate).
+template <int MAS, int E>
+__device__ __forceinline__ void fx_scatter_add(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
+{
+    constexpr int S = Support<MAS>::S;
+#pragma unroll
+    for (int l = 0; l < S; l++)
+#pragma unroll
+        for (int m = 0; m < S; m++) {
+            const float c01 = __fmul_rn(C[0][l], C[1][m]);
+            const int row = base + (l * E + m) * E;
+#pragma unroll
+            for (int q = 0; q < S; q++) {
+                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
+                atomicAdd(acc + row + q, __float_as_uint(x) - FX_MAGIC_BITS);
+            }
+        }
+}
+
 // COUNT: unweighted NGP adds one integer count per particle; otherwise every
 // corner adds its fixed-point weight (weighted NGP: C holds the scaled weight).
 template <int MAS, int E, bool COUNT = (MAS == PYL_MAS_NGP)>

@@ -1007,7 +1007,7 @@ struct FxStage {
 // One pass over the bin's records into shared memory.  Returns 1 when the pass
 // must be redone in float32, 0 when done, -1 after a failed staging wait.
 // q0: batches staged on the two barriers before this pass.
-template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2>
+template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2, bool TOT>
 __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, float inv, float halfcell, int dims,
                                              const int *o, unsigned *smw)
 {
@@ -1029,6 +1029,18 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
     __syncthreads();
     const bool weighted = sg.inv_w != nullptr;
     const float inv_w = weighted ? *sg.inv_w : 1.0f;
+    // Unweighted CIC/TSC/PCS find wrapped cells from the bin's total instead of
+    // the atomics' old values: a particle's S^3 rounded corners add up to 2^22
+    // within S^3 + 8 units, so the cells of a bin sum to cnt * 2^22 within
+    // cnt (S^3 + 8), and every wrap of a cell takes 2^32 off that sum.  That tells
+    // wraps apart while 2 cnt (S^3 + 8) < 2^32.  Summing the bin's cells costs
+    // about what the old-value ORs save at one particle per cell, and the second
+    // path inside one kernel slowed the 1024^3 grid of 1024^3 particles, so TOT
+    // (a separate kernel) is launched from two particles per bin cell on average
+    // (512^3 grids of 1024^3 particles: deposit 11.4 -> 10.8 ms).
+    constexpr unsigned long long PER_P = (unsigned long long)S * S * S + 8;
+    const bool by_total = TOT && !FLOAT && MAS != PYL_MAS_NGP && !weighted &&
+                          (unsigned long long)sg.cnt * PER_P < (1ull << 31);
     unsigned bad = 0u, seen = 0u;
     for (unsigned j = 0; j < sg.nb; j++) {
         const unsigned q = q0 + j;
@@ -1068,10 +1080,29 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
                 if (weighted) {
                     bad |= (unsigned)!(wq >= 0.0f);            // negative or NaN weight
                     seen |= fx_scatter_or<MAS, E, false>(smw, base, C);
+                } else if (by_total) {
+                    fx_scatter_add<MAS, E>(smw, base, C);
                 } else {
                     seen |= fx_scatter_or<MAS, E>(smw, base, C);
                 }
             }
+        }
+    }
+    if (TOT && by_total) {
+        __shared__ unsigned long long s_tot[32];
+        __syncthreads();                                    // every atomic of the pass done
+        unsigned long long t = 0;
+        for (int c = threadIdx.x; c < FS::CELLS; c += 1024) t += smw[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if ((threadIdx.x & 31) == 0) s_tot[threadIdx.x >> 5] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long tot = 0;
+            for (int w = 0; w < 32; w++) tot += s_tot[w];
+            const long long diff = (long long)tot - (long long)((unsigned long long)sg.cnt << 22);
+            const long long bound = (long long)((unsigned long long)sg.cnt * PER_P);
+            if (diff > bound || diff < -bound) bad = 1u;
         }
     }
     const int redo = __syncthreads_or((int)(bad | (seen >> 31)));
@@ -1288,14 +1319,14 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
 
 // Both arithmetic modes of one grid: fixed point, float32 if that overflowed.
 // Returns false after a failed staging wait.
-template <int MAS, bool INTER, int R, int G, bool P2>
+template <int MAS, bool INTER, int R, int G, bool P2, bool TOT>
 __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float inv, float halfcell, int dims,
                                         const int *o, unsigned *smw, float *out, bool interior, float scale,
                                         const Owned &ow, float *halo_bin, const float *prev)
 {
     int st = 1;                                             // float32 from the start
     if (!(sg.use_float && *sg.use_float)) {
-        st = fx_accumulate<MAS, INTER, R, G, false, P2>(sg, q0, inv, halfcell, dims, o, smw);
+        st = fx_accumulate<MAS, INTER, R, G, false, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw);
         if (st < 0) return false;
         q0 += sg.nb;
     }
@@ -1303,7 +1334,7 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
         if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
     } else {
-        if (fx_accumulate<MAS, INTER, R, G, true, P2>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
+        if (fx_accumulate<MAS, INTER, R, G, true, P2, false>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
         q0 += sg.nb;
         // weighted NGP: `scale` carries the 2^-22 of the fixed-point sums, which
         // float sums do not need
@@ -1315,7 +1346,7 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
     return true;
 }
 
-template <int MAS, bool INTER, int R, bool P2>
+template <int MAS, bool INTER, int R, bool P2, bool TOT>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
     float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
@@ -1362,10 +1393,10 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
         sg.use_float = inv_w ? reinterpret_cast<const int *>(inv_w + 2) : nullptr;
         float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
         const float *prev = have_prev && hb ? hb - HC : nullptr;
-        if (!fx_grid<MAS, INTER, R, 0, P2>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
+        if (!fx_grid<MAS, INTER, R, 0, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
             return;
         if (INTER &&
-            !fx_grid<MAS, INTER, R, 1, P2>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
+            !fx_grid<MAS, INTER, R, 1, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
                                        hb ? hb + ow.stride : nullptr, prev ? prev + ow.stride : nullptr))
             return;
         have_prev = true;
@@ -1388,9 +1419,16 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
     constexpr int R = fx_tma_batch<MAS, I>();
     static_assert(R == 0 || carry_floats(FS::H) * 4 <= 2 * R * 16, "carried blocks fit the staging buffers");
     if (R > 0) {
+        constexpr int RR = R > 0 ? R : 1024;
         const bool p2 = (g.dims & (g.dims - 1)) == 0;
-        auto kern = p2 ? bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024), true>
-                       : bin_deposit_fx_tma_kernel<MAS, I, (R > 0 ? R : 1024), false>;
+        // bin-total wrap detection: unweighted non-NGP deposits of two or more
+        // particles per bin cell on average
+        const bool tot = MAS != PYL_MAS_NGP && !inv_w &&
+                         (double)ws.n >= 2.0 * (double)g.nt * g.nt * g.nt * (double)FS::CELLS;
+        auto kern = p2 ? (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, true, true>
+                              : bin_deposit_fx_tma_kernel<MAS, I, RR, true, false>)
+                       : (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, false, true>
+                              : bin_deposit_fx_tma_kernel<MAS, I, RR, false, false>);
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
         PYL_CUDA(ensure_smem(kern, smem));
         const unsigned ctas = (unsigned)(ow.on ? g.ntiles / OWN_Z : g.ntiles);
