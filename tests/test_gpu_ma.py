@@ -338,6 +338,37 @@ def test_fixed_point_overflow_falls_back(MASL, mas):
     assert np.abs(g.cpu().numpy() - o).max() <= 5e-3 * o.max()
 
 
+@pytest.mark.parametrize('mas', ['CIC', 'TSC', 'PCS'])
+@pytest.mark.parametrize('inter', [False, True])
+@pytest.mark.parametrize('clump', [0, 60000])
+def test_dense_bins_find_wraps_from_the_total(MASL, mas, inter, clump):
+    """From two particles per bin cell on average (here 1.1M particles in the eight
+    32^3 bins of a 64^3 grid) the deposit skips reading back the old cell values and
+    finds fixed-point wraps from the bin's total instead.  Uniform particles must
+    match the oracle like every other fixed-point deposit; a clump of 60000
+    particles at one position pushes cells past 1024 and its bin must be redone in
+    float32, on both grids."""
+    N, L = 64, 1000.0
+    rng = np.random.default_rng(17)
+    pos = np.concatenate([np.full((clump, 3), 123.4, np.float32),
+                          (rng.random((1_100_000 - clump, 3)) * L).astype(np.float32)])
+    g1 = torch.zeros((N, N, N), device='cuda')
+    g2 = torch.zeros((N, N, N), device='cuda') if inter else None
+    MASL.MA(torch.from_numpy(pos).cuda(), g1, L, mas, interlaced=g2, strategy='tiled')
+    grids = [(g1, pos)]
+    if inter:
+        grids.append((g2, (pos + np.float32(0.5 * L / N)).astype(np.float32)))
+    for g, p in grids:
+        o = np.zeros((N, N, N), np.float32)
+        O.MA(p, o, L, mas, threads=os.cpu_count() or 1)
+        got = g.cpu().numpy()
+        if clump:
+            assert o.max() > 1024
+            assert np.abs(got - o).max() <= 5e-3 * o.max()
+        else:
+            close(got, o, False, 5e-6)
+
+
 def test_sorted_is_reproducible(MASL):
     """The sorted strategy sums every cell in one fixed order (neighbouring base cells,
     then particle index), with no atomics: two runs give identical bits, weighted and
