@@ -994,12 +994,17 @@ __device__ __forceinline__ int axis_local(float p, float inv, float halfcell, in
     return w0 + (f > f0 ? 1 : 0);
 }
 
+// Staging state of a deposit CTA (at namespace scope: addressed as constants,
+// no registers).
+__shared__ __align__(8) unsigned long long fx_bar[2];   // one mbarrier per buffer
+__shared__ unsigned fx_rel[2];     // per buffer: warps done reading it, counted up forever
+__shared__ unsigned fx_last[2];    // per buffer: batch number of the last copy into it (~0u: none)
+__shared__ int fx_fail;            // a wait of this CTA gave up
+
 struct FxStage {
     const float4 *rec;
     unsigned begin, cnt, nb;           // the bin's records and their batches
     float4 *inb;                       // [2][R] staging buffers
-    unsigned long long *bar;           // one mbarrier per buffer
-    int *ok;
     const float *inv_w;                // weighted: 1 / max |w| (weights scaled into [-1, 1]); null: unweighted
     const int *use_float;              // weighted: 1 -> float32 sums from the start
 };
@@ -1007,6 +1012,14 @@ struct FxStage {
 // One pass over the bin's records into shared memory.  Returns 1 when the pass
 // must be redone in float32, 0 when done, -1 after a failed staging wait.
 // q0: batches staged on the two barriers before this pass.
+//
+// No block-wide barrier per batch: every warp waits on the buffer's mbarrier
+// itself, reads its records into registers and counts itself out of the buffer;
+// the last of the 32 warps issues the copy of the batch two ahead into it.  Warps
+// drift up to a batch apart instead of meeting twice per 2048 records.  A failed
+// wait marks the CTA; the others skip their records, no new copies are issued,
+// and after the pass thread 0 drains the copies in flight (bounded) before the
+// CTA leaves.
 template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2, bool TOT>
 __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, float inv, float halfcell, int dims,
                                              const int *o, unsigned *smw)
@@ -1020,12 +1033,15 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
     const unsigned slot = (threadIdx.x & 31u) * 32u + (((threadIdx.x >> 5) + threadIdx.x) & 31u);
     uint4 *z4 = (uint4 *)smw;
     for (int c = threadIdx.x; c < FS::SMEM / 16; c += 1024) z4[c] = make_uint4(0u, 0u, 0u, 0u);
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
+        fence_proxy_async_smem();                       // earlier generic use of the buffers (carried blocks)
         for (unsigned j = 0; j < 2 && j < sg.nb; j++) {
             const unsigned q = q0 + j;
             stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + j * R, 16u * min((unsigned)R, sg.cnt - j * R),
-                       &sg.bar[q & 1]);
+                       &fx_bar[q & 1]);
+            fx_last[q & 1] = q;
         }
+    }
     __syncthreads();
     const bool weighted = sg.inv_w != nullptr;
     const float inv_w = weighted ? *sg.inv_w : 1.0f;
@@ -1044,22 +1060,28 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
     unsigned bad = 0u, seen = 0u;
     for (unsigned j = 0; j < sg.nb; j++) {
         const unsigned q = q0 + j;
-        if (threadIdx.x == 0) *sg.ok = mbar_wait_bounded(&sg.bar[q & 1], (q >> 1) & 1u, &g_tma_error);
-        __syncthreads();
-        if (!*sg.ok) {
-            if (threadIdx.x == 0 && j + 1 < sg.nb)
-                mbar_wait_bounded(&sg.bar[(q + 1) & 1], ((q + 1) >> 1) & 1u, &g_tma_error);
-            return -1;
-        }
+        int got = 0;
+        if ((threadIdx.x & 31) == 0) got = mbar_wait_bounded(&fx_bar[q & 1], (q >> 1) & 1u, &g_tma_error);
+        got = __shfl_sync(0xffffffffu, got, 0);             // lane 0's wait orders the copy for the warp
+        __syncwarp();
         const float4 *in = sg.inb + (q & 1) * R;
         const unsigned c = min((unsigned)R, sg.cnt - j * R);
-        float4 r[PER];
+        float4 r[PER];                                      // (unused after a failed wait)
 #pragma unroll
         for (int u = 0; u < PER; u++) r[u] = in[slot + u * 1024];
-        __syncthreads();                                    // buffer consumed
-        if (threadIdx.x == 0 && j + 2 < sg.nb)
-            stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
-                       16u * min((unsigned)R, sg.cnt - (j + 2) * R), &sg.bar[q & 1]);
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) {
+            if (!got) atomicOr(&fx_fail, 1);
+            __threadfence_block();                          // this warp's reads before its count
+            const unsigned done = atomicAdd(&fx_rel[q & 1], 1u);
+            if ((done & 31u) == 31u && j + 2 < sg.nb && !*(volatile int *)&fx_fail) {
+                fence_proxy_async_smem();
+                stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
+                           16u * min((unsigned)R, sg.cnt - (j + 2) * R), &fx_bar[q & 1]);
+                fx_last[q & 1] = q + 2;
+            }
+        }
+        if (!got) continue;
 #pragma unroll
         for (int u = 0; u < PER; u++) {
             if (slot + u * 1024 >= c) continue;
@@ -1106,6 +1128,13 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
         }
     }
     const int redo = __syncthreads_or((int)(bad | (seen >> 31)));
+    if (*(volatile int *)&fx_fail) {
+        if (threadIdx.x == 0)
+            for (int b = 0; b < 2; b++)
+                if (fx_last[b] != ~0u) mbar_drain_bounded(&fx_bar[b], (fx_last[b] >> 1) & 1u);
+        __syncthreads();
+        return -1;
+    }
     return (!FLOAT && redo) ? 1 : 0;
 }
 
@@ -1355,15 +1384,16 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     using FS = FxShape<MAS, INTER>;
     constexpr int E = FS::E;
     extern __shared__ __align__(16) unsigned smw[];
-    __shared__ __align__(8) unsigned long long bar[2];
-    __shared__ int s_ok;
     const float scale = out_scale(sc);
     const int dims = g.dims;
     constexpr int HC = halo_cells(FS::H);
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        mbar_init(&fx_bar[0], 1);
+        mbar_init(&fx_bar[1], 1);
         mbar_fence_init();
+        fx_rel[0] = fx_rel[1] = 0u;
+        fx_last[0] = fx_last[1] = ~0u;
+        fx_fail = 0;
     }
     __syncthreads();
     unsigned q0 = 0;                                    // batches staged by this CTA so far
@@ -1387,8 +1417,6 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
         sg.cnt = end - begin;
         sg.nb = (sg.cnt + R - 1) / R;
         sg.inb = (float4 *)(smw + FS::SMEM / 4);
-        sg.bar = bar;
-        sg.ok = &s_ok;
         sg.inv_w = inv_w;
         sg.use_float = inv_w ? reinterpret_cast<const int *>(inv_w + 2) : nullptr;
         float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;

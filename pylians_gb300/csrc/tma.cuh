@@ -3,9 +3,11 @@
 // through shared memory in double-buffered batches.
 //
 // Rules the callers keep: source and destination 16-byte aligned, sizes a
-// multiple of 16 bytes; one thread initialises the barriers and issues the
-// copies; one thread waits, with an iteration limit, and publishes the outcome
-// through shared memory so that the whole CTA proceeds or leaves together.
+// multiple of 16 bytes; one thread initialises the barriers and issues each
+// copy; waits have an iteration limit, and either one thread waits and
+// publishes the outcome through shared memory or every thread waits for itself
+// and the CTA agrees on the outcome at its next barrier, so that the whole CTA
+// proceeds or leaves together.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -69,6 +71,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     }
     atomicOr(err, 1u);
     return false;
+}
+
+// Waits for phase `parity` of `bar` for at most MBAR_WAIT_CYCLES whatever the
+// error word says: the drain of a CTA's own copies after a failed wait.
+__device__ __forceinline__ bool mbar_drain_bounded(unsigned long long *bar, unsigned parity)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > MBAR_WAIT_CYCLES) return false;
+    return true;
+}
+
+// Orders this thread's (and, after a barrier, the CTA's) generic-proxy accesses
+// of shared memory before later bulk copies into it.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Issues one bulk copy of `bytes` (multiple of 16, may be 0) into dst, arming
