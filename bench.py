@@ -475,9 +475,9 @@ STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort', 'halo')
 # (particles, grid); summaries and commands in profiles/cic_interlaced_pk_1024_launches.md
 # and profiles/bin_deposit_fx_cic_interlaced_512.md.
 KERNEL_TRAFFIC = {
-    (1024 ** 3, 1024): dict(hist=12.886015232e9 + 0.003792896e9, place=13.224840192e9 + 17.387312896e9,
-                            place_b=17.348109568e9 + 17.283051776e9, deposit=29.109039872e9 + 10.267560960e9,
-                            halo=4.200761600e9 + 1.484157952e9, pk_bin=8.636224512e9 + 0.022080000e9),
+    (1024 ** 3, 1024): dict(hist=12.8850e9 + 0.0053e9, place=13.2252e9 + 17.3872e9,
+                            place_b=17.3480e9 + 17.2813e9, deposit=29.0944e9 + 10.2683e9,
+                            halo=4.2000e9 + 1.4836e9, pk_bin=8.6382e9 + 0.0223e9),
     (512 ** 3, 512): dict(deposit=4.017201e9 + 1.101149e9),
 }
 

@@ -424,8 +424,132 @@ __device__ __forceinline__ float rsd_shift(float p, float v, float factor, float
     return s;
 }
 
-template <int MAS, bool RSD = false>
+// One CTA per SM (grids binned by as many chunks as SMs).  No block barrier per
+// batch: lane 0 of each warp waits on the buffer's mbarrier, the warp copies its
+// four particles of the batch to registers (44 registers a thread) and counts
+// itself out of the buffer, and the last of the 32 warps issues the copy HT_NBUF
+// batches ahead into it (1024^3 particles on a 1024^3 grid: 3.13 -> 2.92 ms).  A
+// failed wait marks the CTA: no further copies, and the copies in flight are
+// drained (bounded) before it leaves without a row.
+template <int MAS, bool RSD>
 __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *pos, long long n,
+                                                              long long chunk, float inv, TileGeom g,
+                                                              unsigned *__restrict__ hist, RsdArgs rsd = RsdArgs{},
+                                                              unsigned long long *coh = nullptr)
+{
+    constexpr int HB = HT_BATCH;
+    constexpr int PER = HB / 1024;          // particles per thread and batch
+    __shared__ unsigned s_same;             // particles in the same bin as their predecessor
+    extern __shared__ __align__(16) unsigned char hraw[];
+    __shared__ __align__(8) unsigned long long bar[HT_NBUF];
+    __shared__ unsigned s_rel[HT_NBUF];     // warps done reading each buffer, counted up forever
+    __shared__ long long s_last[HT_NBUF];   // batch of the last copy into each buffer (-1: none)
+    __shared__ int s_fail;
+    const int T = (int)g.ntiles;
+    const int lane = threadIdx.x & 31;
+    float *inb = (float *)hraw;                                  // [HT_NBUF][HB * 3]
+    unsigned *cnt = (unsigned *)(hraw + HT_NBUF * HB * 12);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0;
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    const long long nbat = e > b ? (e - b + HB - 1) / HB : 0;
+    unsigned my_same = 0u;                  // lane 0 of each warp: its warp's count
+    if (threadIdx.x == 0) {
+        s_same = 0u;
+        s_fail = 0;
+        for (int k = 0; k < HT_NBUF; k++) {
+            mbar_init(&bar[k], 1);
+            s_rel[k] = 0u;
+            s_last[k] = -1;
+        }
+        mbar_fence_init();
+        for (long long j = 0; j < HT_NBUF && j < nbat; j++) {
+            const long long s0 = b + j * HB;
+            stage_copy(inb + (j % HT_NBUF) * HB * 3, pos + 3 * s0,
+                       staged_bytes(min((long long)HB, e - s0)), &bar[j % HT_NBUF]);
+            s_last[j % HT_NBUF] = j;
+        }
+    }
+    __syncthreads();
+    for (long long j = 0; j < nbat; j++) {
+        const long long s0 = b + j * HB;
+        const int c = (int)min((long long)HB, e - s0);
+        const int full = staged_full(c);
+        const int buf = (int)(j % HT_NBUF);
+        const float *in = inb + buf * HB * 3;
+        int got = 0;
+        if (lane == 0) got = mbar_wait_bounded(&bar[buf], (unsigned)((j / HT_NBUF) & 1), &g_tma_error);
+        got = __shfl_sync(0xffffffffu, got, 0);             // lane 0's wait orders the copy for the warp
+        __syncwarp();
+        // every batch but a chunk's last is fully staged: no per-particle fallback test
+        const bool all_staged = full == HB;
+        float p[PER][3];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int i = threadIdx.x + u * 1024;
+            const long long q = s0 + i;
+            if (all_staged || i < full) {
+                p[u][0] = in[3 * i]; p[u][1] = in[3 * i + 1]; p[u][2] = in[3 * i + 2];
+            } else if (i < c) {
+                p[u][0] = pos[3 * q]; p[u][1] = pos[3 * q + 1]; p[u][2] = pos[3 * q + 2];
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (!got) atomicOr(&s_fail, 1);
+            __threadfence_block();                          // this warp's reads before its count
+            const unsigned done = atomicAdd(&s_rel[buf], 1u);
+            if ((done & 31u) == 31u && j + HT_NBUF < nbat && !*(volatile int *)&s_fail) {
+                const long long s2 = b + (j + HT_NBUF) * HB;
+                fence_proxy_async_smem();
+                stage_copy(inb + buf * HB * 3, pos + 3 * s2, staged_bytes(min((long long)HB, e - s2)),
+                           &bar[buf]);
+                s_last[buf] = j + HT_NBUF;
+            }
+        }
+        if (!got) continue;
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int i = threadIdx.x + u * 1024;
+            if (!all_staged && i >= c) break;               // past the chunk's end
+            const long long q = s0 + i;
+            if (RSD) {                              // selects, not a dynamic index (no local array)
+                const int ax = rsd.axis;
+                const float pa = ax == 0 ? p[u][0] : (ax == 1 ? p[u][1] : p[u][2]);
+                const float sh = rsd_shift(pa, __ldg(rsd.vel + 3 * q + ax), rsd.factor, rsd.box);
+                p[u][0] = ax == 0 ? sh : p[u][0];
+                p[u][1] = ax == 1 ? sh : p[u][1];
+                p[u][2] = ax == 2 ? sh : p[u][2];
+                rsd.pos[3 * q + ax] = sh;
+            }
+            const unsigned key = tile_key<MAS>(p[u], inv, g);
+            atomicAdd(cnt + key, 1u);
+            if (coh) {                              // the warp's lanes hold consecutive particles
+                const unsigned prev = __shfl_up_sync(__activemask(), key, 1);
+                const unsigned same = __ballot_sync(__activemask(), (threadIdx.x & 31) && prev == key);
+                my_same += (unsigned)__popc(same);
+            }
+        }
+    }
+    if (coh && lane == 0 && my_same) atomicAdd(&s_same, my_same);
+    __syncthreads();
+    if (s_fail) {
+        if (threadIdx.x == 0)
+            for (int k = 0; k < HT_NBUF; k++)
+                if (s_last[k] >= 0) mbar_drain_bounded(&bar[k], (unsigned)((s_last[k] / HT_NBUF) & 1));
+        return;
+    }
+    unsigned *row = hist + (long long)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = cnt[t];
+    if (coh && threadIdx.x == 0 && s_same) atomicAdd(coh, (unsigned long long)s_same);
+}
+
+// Two CTAs per SM (grids binned by twice as many chunks as SMs): thread 0 waits
+// and the CTA meets at two barriers per batch, with 30 registers a thread.  (The
+// barrier-free loop above needs 44 registers; held to 32 it spills, and on
+// 2048-particle batches it took 3.8 ms against 2.6 ms for 1024^3 particles on a
+// 512^3 grid.)
+template <int MAS, bool RSD>
+__global__ void __launch_bounds__(1024) chunk_hist_tma_sync_kernel(const float *pos, long long n,
                                                               long long chunk, float inv, TileGeom g,
                                                               unsigned *__restrict__ hist, RsdArgs rsd = RsdArgs{},
                                                               unsigned long long *coh = nullptr)
@@ -1013,14 +1137,18 @@ struct FxStage {
 // must be redone in float32, 0 when done, -1 after a failed staging wait.
 // q0: batches staged on the two barriers before this pass.
 //
-// No block-wide barrier per batch: every warp waits on the buffer's mbarrier
-// itself, reads its records into registers and counts itself out of the buffer;
-// the last of the 32 warps issues the copy of the batch two ahead into it.  Warps
-// drift up to a batch apart instead of meeting twice per 2048 records.  A failed
-// wait marks the CTA; the others skip their records, no new copies are issued,
-// and after the pass thread 0 drains the copies in flight (bounded) before the
-// CTA leaves.
-template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2, bool TOT>
+// FREE (owned-cell launches, four bins per CTA): no block-wide barrier per
+// batch.  Lane 0 of every warp waits on the buffer's mbarrier, the warp reads its
+// records into registers and counts itself out of the buffer; the last of the 32
+// warps issues the copy of the batch two ahead into it.  Warps drift up to a
+// batch apart instead of meeting twice per 2048 records (1024^3 interlaced
+// deposit 13.4 -> 12.5 ms).  One bin per CTA (the red.global write-out) measured
+// faster with thread 0 waiting and two barriers per batch (512^3 particles on a
+// 512^3 grid, interlaced: 1.83 against 2.03 ms), so those launches keep them;
+// both loops in one kernel (a runtime switch) made both slower.
+// A failed wait marks the CTA; no new copies are issued, and after the pass
+// thread 0 drains the copies in flight (bounded) before the CTA leaves.
+template <int MAS, bool INTER, int R, int G, bool FLOAT, bool P2, bool TOT, bool FREE>
 __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, float inv, float halfcell, int dims,
                                              const int *o, unsigned *smw)
 {
@@ -1060,22 +1188,37 @@ __device__ __forceinline__ int fx_accumulate(const FxStage &sg, unsigned q0, flo
     unsigned bad = 0u, seen = 0u;
     for (unsigned j = 0; j < sg.nb; j++) {
         const unsigned q = q0 + j;
-        int got = 0;
-        if ((threadIdx.x & 31) == 0) got = mbar_wait_bounded(&fx_bar[q & 1], (q >> 1) & 1u, &g_tma_error);
-        got = __shfl_sync(0xffffffffu, got, 0);             // lane 0's wait orders the copy for the warp
-        __syncwarp();
         const float4 *in = sg.inb + (q & 1) * R;
         const unsigned c = min((unsigned)R, sg.cnt - j * R);
         float4 r[PER];                                      // (unused after a failed wait)
+        int got = 1;
+        if constexpr (FREE) {
+            if ((threadIdx.x & 31) == 0) got = mbar_wait_bounded(&fx_bar[q & 1], (q >> 1) & 1u, &g_tma_error);
+            got = __shfl_sync(0xffffffffu, got, 0);         // lane 0's wait orders the copy for the warp
+            __syncwarp();
 #pragma unroll
-        for (int u = 0; u < PER; u++) r[u] = in[slot + u * 1024];
-        __syncwarp();
-        if ((threadIdx.x & 31) == 0) {
-            if (!got) atomicOr(&fx_fail, 1);
-            __threadfence_block();                          // this warp's reads before its count
-            const unsigned done = atomicAdd(&fx_rel[q & 1], 1u);
-            if ((done & 31u) == 31u && j + 2 < sg.nb && !*(volatile int *)&fx_fail) {
-                fence_proxy_async_smem();
+            for (int u = 0; u < PER; u++) r[u] = in[slot + u * 1024];
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) {
+                if (!got) atomicOr(&fx_fail, 1);
+                __threadfence_block();                      // this warp's reads before its count
+                const unsigned done = atomicAdd(&fx_rel[q & 1], 1u);
+                if ((done & 31u) == 31u && j + 2 < sg.nb && !*(volatile int *)&fx_fail) {
+                    fence_proxy_async_smem();
+                    stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
+                               16u * min((unsigned)R, sg.cnt - (j + 2) * R), &fx_bar[q & 1]);
+                    fx_last[q & 1] = q + 2;
+                }
+            }
+        } else {                                            // thread 0 waits, the CTA meets twice
+            if (threadIdx.x == 0 && !mbar_wait_bounded(&fx_bar[q & 1], (q >> 1) & 1u, &g_tma_error))
+                fx_fail = 1;
+            __syncthreads();
+            if (*(volatile int *)&fx_fail) break;
+#pragma unroll
+            for (int u = 0; u < PER; u++) r[u] = in[slot + u * 1024];
+            __syncthreads();                                // buffer consumed
+            if (threadIdx.x == 0 && j + 2 < sg.nb) {
                 stage_copy(sg.inb + (q & 1) * R, sg.rec + sg.begin + (j + 2) * R,
                            16u * min((unsigned)R, sg.cnt - (j + 2) * R), &fx_bar[q & 1]);
                 fx_last[q & 1] = q + 2;
@@ -1348,14 +1491,14 @@ __global__ void __launch_bounds__(256) halo_add_kernel(float *__restrict__ grid,
 
 // Both arithmetic modes of one grid: fixed point, float32 if that overflowed.
 // Returns false after a failed staging wait.
-template <int MAS, bool INTER, int R, int G, bool P2, bool TOT>
+template <int MAS, bool INTER, int R, int G, bool P2, bool TOT, bool FREE>
 __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float inv, float halfcell, int dims,
                                         const int *o, unsigned *smw, float *out, bool interior, float scale,
                                         const Owned &ow, float *halo_bin, const float *prev)
 {
     int st = 1;                                             // float32 from the start
     if (!(sg.use_float && *sg.use_float)) {
-        st = fx_accumulate<MAS, INTER, R, G, false, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw);
+        st = fx_accumulate<MAS, INTER, R, G, false, P2, TOT, FREE>(sg, q0, inv, halfcell, dims, o, smw);
         if (st < 0) return false;
         q0 += sg.nb;
     }
@@ -1363,7 +1506,7 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
         if (ow.on) fx_store_owned<MAS, INTER, false>(smw, out, halo_bin, o, dims, scale, ow, prev, (float *)sg.inb);
         else fx_write_out<MAS, INTER, false>(smw, out, o, dims, interior, scale);
     } else {
-        if (fx_accumulate<MAS, INTER, R, G, true, P2, false>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
+        if (fx_accumulate<MAS, INTER, R, G, true, P2, false, FREE>(sg, q0, inv, halfcell, dims, o, smw) < 0) return false;
         q0 += sg.nb;
         // weighted NGP: `scale` carries the 2^-22 of the fixed-point sums, which
         // float sums do not need
@@ -1375,7 +1518,7 @@ __device__ __forceinline__ bool fx_grid(const FxStage &sg, unsigned &q0, float i
     return true;
 }
 
-template <int MAS, bool INTER, int R, bool P2, bool TOT>
+template <int MAS, bool INTER, int R, bool P2, bool TOT, bool FREE>
 __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     const float4 *__restrict__ rec, const unsigned *__restrict__ offsets, TileGeom g, float inv,
     float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
@@ -1421,10 +1564,10 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
         sg.use_float = inv_w ? reinterpret_cast<const int *>(inv_w + 2) : nullptr;
         float *hb = ow.on && HC > 0 ? ow.halo + tile * HC : nullptr;
         const float *prev = have_prev && hb ? hb - HC : nullptr;
-        if (!fx_grid<MAS, INTER, R, 0, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
+        if (!fx_grid<MAS, INTER, R, 0, P2, TOT, FREE>(sg, q0, inv, halfcell, dims, o, smw, grid, interior, scale, ow, hb, prev))
             return;
         if (INTER &&
-            !fx_grid<MAS, INTER, R, 1, P2, TOT>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
+            !fx_grid<MAS, INTER, R, 1, P2, TOT, FREE>(sg, q0, inv, halfcell, dims, o, smw, grid2, interior, scale, ow,
                                        hb ? hb + ow.stride : nullptr, prev ? prev + ow.stride : nullptr))
             return;
         have_prev = true;
@@ -1453,10 +1596,15 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         // particles per bin cell on average
         const bool tot = MAS != PYL_MAS_NGP && !inv_w &&
                          (double)ws.n >= 2.0 * (double)g.nt * g.nt * g.nt * (double)FS::CELLS;
-        auto kern = p2 ? (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, true, true>
-                              : bin_deposit_fx_tma_kernel<MAS, I, RR, true, false>)
-                       : (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, false, true>
-                              : bin_deposit_fx_tma_kernel<MAS, I, RR, false, false>);
+        // owned-cell launches: no block barriers per batch
+        auto kern = ow.on ? (p2 ? (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, true, true, true>
+                                       : bin_deposit_fx_tma_kernel<MAS, I, RR, true, false, true>)
+                                : (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, false, true, true>
+                                       : bin_deposit_fx_tma_kernel<MAS, I, RR, false, false, true>))
+                          : (p2 ? (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, true, true, false>
+                                       : bin_deposit_fx_tma_kernel<MAS, I, RR, true, false, false>)
+                                : (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, false, true, false>
+                                       : bin_deposit_fx_tma_kernel<MAS, I, RR, false, false, false>));
         const size_t smem = FS::SMEM + 2 * (size_t)R * 16;
         PYL_CUDA(ensure_smem(kern, smem));
         const unsigned ctas = (unsigned)(ow.on ? g.ntiles / OWN_Z : g.ntiles);
@@ -1509,14 +1657,16 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
         unsigned long long *same = gated ? ws.same : nullptr;
         stage_mark(PYL_STAGE_HIST, true, st);
         if (gated) PYL_CUDA(cudaMemsetAsync(ws.same, 0, sizeof(unsigned long long), st));
+        const bool two = two_level_small(g);       // two chunks (CTAs) per SM
+        const size_t hsm = hist_tma_smem(T);
         if (rsd) {                                 // callers check tiled_rsd_fusable first
-            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS, true>, hist_tma_smem(T)));
-            chunk_hist_tma_kernel<MAS, true><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist, *rsd,
-                                                                                 same);
+            auto k = two ? chunk_hist_tma_sync_kernel<MAS, true> : chunk_hist_tma_kernel<MAS, true>;
+            PYL_CUDA(ensure_smem(k, hsm));
+            k<<<C, 1024, hsm, st>>>(pos, n, chunk, inv, g, ws.hist, *rsd, same);
         } else if (counted) {
-            PYL_CUDA(ensure_smem(chunk_hist_tma_kernel<MAS>, hist_tma_smem(T)));
-            chunk_hist_tma_kernel<MAS><<<C, 1024, hist_tma_smem(T), st>>>(pos, n, chunk, inv, g, ws.hist,
-                                                                          RsdArgs{}, same);
+            auto k = two ? chunk_hist_tma_sync_kernel<MAS, false> : chunk_hist_tma_kernel<MAS, false>;
+            PYL_CUDA(ensure_smem(k, hsm));
+            k<<<C, 1024, hsm, st>>>(pos, n, chunk, inv, g, ws.hist, RsdArgs{}, same);
         } else {
             PYL_CUDA(ensure_smem(chunk_hist_kernel<MAS>, sm));
             chunk_hist_kernel<MAS><<<C, 1024, sm, st>>>(pos, n, chunk, inv, g, ws.hist);
