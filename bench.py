@@ -311,7 +311,7 @@ def main():
                     config=dict(workload='cic_interlaced_pk_np%d^3_grid%d^3' % (side, dims),
                                 particles=n, grid=dims, box_mpc_h=BOX, axis=0, MAS='CIC',
                                 interlaced=True, strategy=a.strategy, parallelism='replicas',
-                                l2_flush='inputs larger than L2 (12.9 GB positions)'),
+                                l2_flush='inputs larger than L2 (%.1f GB positions)' % (12.0 * n / 1e9)),
                     e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
                     gpu_launches=kernels_per_step(dims) * a.steps, stages_ms=stages,
                     secondary=secondary)
