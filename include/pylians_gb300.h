@@ -28,7 +28,7 @@ extern "C" {
 #define PYL_ERR_CUDA 2        /* a CUDA runtime call failed */
 #define PYL_ERR_CUFFT 3       /* a cuFFT call failed */
 #define PYL_ERR_WORKSPACE 4   /* workspace smaller than *_workspace_size() */
-#define PYL_ERR_UNSUPPORTED 5 /* valid request this build does not implement */
+#define PYL_ERR_UNSUPPORTED 5 /* valid request the library does not implement */
 
 /* mass-assignment schemes: the reference's MAS_function indices (Pk_library.pyx:75-81) */
 #define PYL_MAS_NONE 0

@@ -10,7 +10,7 @@ Every array in the fixtures is an OUTPUT of the reference's own code
 (MAS_library.MA / *c3D, Pk_library.Pk / XPk, bispectrum_library.Bk) on
 seeded synthetic inputs that are stored beside it.  The inputs follow the
 reference's unit tests (Test/test_MAS.py:10-84: seed 1, uniform particles in a
-unit box, W = 3.0) and the survey configurations (1000 Mpc/h box, uniform
+unit box, W = 3.0) and the benchmark workloads (1000 Mpc/h box, uniform
 particles, CIC overdensity), shrunk so the fixtures stay small.
 """
 import contextlib
