@@ -58,6 +58,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest of every rank's x (one all_reduce MAX in float64 on `device`,
+    a CUDA device under NCCL, 'cpu' under gloo); x itself for one rank."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.item()
+
+
+def whole_job_rate(units_per_rank, steps, world, ms):
+    """Units per second of the whole job: every replica processes units_per_rank
+    per step, and the job takes the slowest rank's ms."""
+    return units_per_rank * steps * world / (ms / 1e3)
+
+
 # ------------------------------------------------------------------ CPU baseline
 def cpu_chain(pos, dims, threads):
     """The reference's CPU path on `pos`: MAS_c.c-style OpenMP CIC into two grids,
@@ -220,13 +237,9 @@ def main():
         pp.step(pos)
     e1.record()
     torch.cuda.synchronize(); barrier()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = t.item()
-    value = n * a.steps * world / (ms / 1e3)
+    value = whole_job_rate(n, a.steps, world, ms)
     res = pp.result()
     assert int(res.Nmodes3D.sum()) + 1 == (dims ** 3 - 8) // 2 + 8
 
@@ -274,9 +287,9 @@ def main():
         run(k2)
         e1.record()
         torch.cuda.synchronize(); barrier()
-        ms2 = e0.elapsed_time(e1)
-        wall = (time.perf_counter() - t0) * 1e3
-        e2e = dict(value=n * k2 * world / (ms2 / 1e3), unit=UNIT,
+        ms2 = max_over_ranks(e0.elapsed_time(e1), world, dev)
+        wall = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+        e2e = dict(value=whole_job_rate(n, k2, world, ms2), unit=UNIT,
                    h2d_bytes_per_step=int(host.numel() * 4),
                    d2h_bytes_per_step=int(sums_host.numel() * 8), ms_per_step=ms2 / k2,
                    host_wall_ms_per_step=wall / k2, overlap='h2d of step i+1 under compute of step i')
