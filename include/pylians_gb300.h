@@ -40,7 +40,8 @@ extern "C" {
 /* scatter strategies for pyl_ma */
 #define PYL_STRATEGY_AUTO 0   /* library picks by grid size and particle count */
 #define PYL_STRATEGY_ATOMIC 1 /* one thread per particle, atomics into the grid */
-#define PYL_STRATEGY_TILED 2  /* bin particles by tile, deposit tiles in shared memory */
+#define PYL_STRATEGY_TILED 2  /* bin particles by tile, deposit tiles in shared memory;
+                                 3D and fewer than 2^32 - 16 particles (else ATOMIC runs) */
 #define PYL_STRATEGY_SORTED 3 /* radix sort by cell + fixed-order per-cell gather: bit-reproducible */
 
 const char *pyl_strerror(int status);
