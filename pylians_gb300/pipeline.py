@@ -13,7 +13,6 @@ scaled by 1/mean), so there is no separate normalisation pass.  Every launch goe
 stream, so a whole step can be captured in a CUDA graph (`capture()`), and the
 grids, FFT outputs and sums stay allocated across steps.
 """
-import numpy as np
 import torch
 
 from . import _lib

@@ -3,7 +3,6 @@ float64 oracle (oracle.mlp_forward_backward), and what the trained network gains
 over the uncorrected coarse, non-interlaced estimator on held-out fields."""
 import numpy as np
 import pytest
-import torch
 
 import oracle as O
 
