@@ -93,3 +93,44 @@ def test_python_facade_errors_without_gpu():
     from pylians_gb300._lib import PylError
     with pytest.raises(PylError):
         MASL.MA(np.zeros((4, 3), np.float32), np.zeros((8, 8, 8), np.float32), 1.0, 'CIC')
+
+
+def test_overdensity_rejects_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)   # never dereferenced: validation fails first
+    nan = float('nan')
+    assert lib.pyl_ma_overdensity(buf, None, 0, buf, None, 16, 1.0, 2, 0, None, 0, None) == 1
+    assert 'at least one particle' in lib.pyl_last_error().decode()
+    assert lib.pyl_ma_overdensity(buf, None, 10, buf, None, 16, nan, 2, 0, None, 0, None) == 1
+    assert 'BoxSize' in lib.pyl_last_error().decode()
+    assert lib.pyl_ma_overdensity(buf, None, 10, buf, None, 16, 1.0, 5, 0, None, 0, None) == 1
+    assert 'MAS' in lib.pyl_last_error().decode()
+    # the redshift-space variant: line of sight, Hubble rate, velocities
+    rsd = lib.pyl_ma_overdensity_rsd
+    assert rsd(buf, buf, None, 10, buf, None, 16, 1.0, 2, 0, 100.0, 0.0, 3, None, 0, None) == 1
+    assert 'axis' in lib.pyl_last_error().decode()
+    assert rsd(buf, buf, None, 10, buf, None, 16, 1.0, 2, 0, 0.0, 0.0, 0, None, 0, None) == 1
+    assert 'Hubble' in lib.pyl_last_error().decode()
+    assert rsd(buf, None, None, 10, buf, None, 16, 1.0, 2, 0, 100.0, 0.0, 0, None, 0, None) == 1
+    assert 'null' in lib.pyl_last_error().decode()
+
+
+def test_noalloc_limits_are_checked_on_the_host(lib):
+    buf = ctypes.c_void_p(16)
+    assert lib.pyl_ma_noalloc(buf, None, 524289, buf, None, 64, 1.0, 2, None) == 1
+    assert 'at most 524288 particles' in lib.pyl_last_error().decode()
+    assert lib.pyl_ma_noalloc(buf, None, 1000, buf, None, 513, 1.0, 2, None) == 1
+    assert 'dims <= 512' in lib.pyl_last_error().decode()
+    assert lib.pyl_ma_noalloc(buf, None, 1000, buf, None, 64, 1.0, 0, None) == 1
+    assert 'MAS' in lib.pyl_last_error().decode()
+
+
+def test_interp_and_shift_reject_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)
+    assert lib.pyl_cic_interp(buf, 16, -1.0, buf, 10, buf, None) == 1
+    assert 'BoxSize' in lib.pyl_last_error().decode()
+    assert lib.pyl_cic_interp(buf, 16, 1.0, None, 10, buf, None) == 1
+    assert 'null' in lib.pyl_last_error().decode()
+    assert lib.pyl_pos_redshift_space(buf, buf, 10, 1.0, 100.0, 0.0, 5, None) == 1
+    assert 'axis' in lib.pyl_last_error().decode()
+    assert lib.pyl_pos_redshift_space(buf, buf, -1, 1.0, 100.0, 0.0, 0, None) == 1
+    assert 'negative' in lib.pyl_last_error().decode()
