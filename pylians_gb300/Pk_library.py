@@ -15,7 +15,7 @@ Mirrors library/Pk_library/Pk_library.pyx and bispectrum_library.pyx:
 The mode loops run in libpylgpu.so (one read of each half-complex field, no
 k-grid materialised); only the O(bins) finalisation below runs on the host,
 in float64, with the reference's formulas.  `threads` is accepted and ignored.
-Differences: check_number_modes raises RuntimeError instead of sys.exit();
+Differences: check_number_modes(_2D) raise RuntimeError instead of sys.exit();
 keyword-only `interlaced=` takes the half-cell-shifted grid(s) produced by
 MAS_library.MA(..., interlaced=...).  Inputs may be numpy arrays or CUDA tensors.
 """
@@ -238,11 +238,12 @@ def frequencies_2D(BoxSize, dims):
 
 
 def check_number_modes_2D(Nmodes, dims):
-    """Pk_library.check_number_modes_2D (:105-117); raises instead of exiting."""
+    """Pk_library.check_number_modes_2D (:105-117); raises RuntimeError, like
+    check_number_modes, instead of exiting."""
     own = 1 if dims % 2 == 1 else 4
     indep = (dims ** 2 - own) // 2 + own
     if int(np.sum(Nmodes)) != indep:
-        raise ValueError('Not all modes counted: counted %d independent modes, expected %d'
+        raise RuntimeError('Not all modes counted: counted %d independent modes, expected %d'
                          % (int(np.sum(Nmodes)), indep))
 
 
