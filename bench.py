@@ -42,7 +42,6 @@ def parse():
     ap.add_argument('--grid', type=int, default=1024)
     ap.add_argument('--particles-side', type=int, default=1024)
     ap.add_argument('--cpu-side', type=int, default=512, help='side of the CPU baseline sample')
-    ap.add_argument('--ref-side', type=int, default=256, help='side of each reference-arm step')
     ap.add_argument('--no-secondary', action='store_true')
     ap.add_argument('--batch-size', type=int, default=512)
     ap.add_argument('--no-cpu', action='store_true')
@@ -114,6 +113,13 @@ def run_cpu_baseline(side):
 
 
 def reference_arm(a):
+    """The reference's CPU path (the oracle port: MAS_c.c-style OpenMP CIC, float32 FFTs,
+    the Pk mode loop) on the GPU arm's own workload.  The K timed steps together process
+    exactly one headline workload: step i deposits the i-th of K equal slices of the
+    particles (uniform, seeded per slice) onto the two dims^3 grids, and the last step
+    also runs the overdensity, both FFTs and the mode loop.  value = particles of the
+    workload / total time of the K steps.  Warm-up steps deposit slices into scratch
+    grids of the same size (not timed)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -121,25 +127,57 @@ def reference_arm(a):
     import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    side = a.ref_side
-    pos = cpu_sample(side)
-    for _ in range(a.warmup):
-        cpu_chain(pos, side, threads)
+    dims, side = a.grid, a.particles_side
+    n = side ** 3
+    K = max(1, a.steps)
+    slice_n = -(-n // K)
+    half = np.float32(0.5 * BOX / dims)
+
+    def deposit(g1, g2, count, seed):
+        rng = np.random.default_rng(seed)
+        pos = (rng.random((count, 3), dtype=np.float32) * np.float32(BOX)).astype(np.float32)
+        O.ma_kernel(pos, g1, BOX, 'CIC', None, threads=threads, flavor=1)
+        pos += half
+        O.ma_kernel(pos, g2, BOX, 'CIC', None, threads=threads, flavor=1)
+
+    g1 = np.zeros((dims,) * 3, np.float32)
+    g2 = np.zeros((dims,) * 3, np.float32)
+    for i in range(a.warmup):
+        deposit(g1, g2, slice_n, 1000 + i)
+    g1[...] = 0.0
+    g2[...] = 0.0
     t0 = time.perf_counter()
-    for _ in range(a.steps):
-        cpu_chain(pos, side, threads)
+    done = 0
+    for i in range(K):
+        cnt = min(slice_n, n - done)
+        deposit(g1, g2, cnt, 1 + i)
+        done += cnt
+        if i == K - 1:
+            m = np.float32(n / dims ** 3)
+            for g in (g1, g2):
+                g /= m
+                g -= np.float32(1)
+            O.Pk(g1, BOX, 0, 'CIC', threads, interlaced=g2)
     dt = time.perf_counter() - t0
-    v = pos.shape[0] * a.steps / dt
+    v = n / dt
     line = dict(metric=METRIC, value=v, unit=UNIT, n_gpus=world, steps=a.steps, warmup=a.warmup,
-                ms_per_step=dt / a.steps * 1e3, higher_is_better=True, scaling='weak',
+                ms_per_step=dt / K * 1e3, higher_is_better=True, scaling='weak',
                 vs_baseline=None, dtype='f32', data='synthetic',
-                config=dict(workload='cic_interlaced_pk_cpu_sample_%d^3_particles_%d^3_grid' % (side, side),
-                            box_mpc_h=BOX, axis=0, MAS='CIC', interlaced=True),
+                config=headline_config(side, dims, a.strategy),
                 impl='reference',
                 cpu_baseline=dict(value=v, unit=UNIT, cores=threads, kind='port',
-                                  sample='%d^3 particles onto %d^3 grids per step' % (side, side)),
+                                  sample='the whole workload: %d^3 particles in %d slices onto two %d^3 grids, '
+                                         'then overdensity, two FFTs and the P(k) mode loop (%.1f s)'
+                                         % (side, K, dims, dt)),
                 e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line))
+
+
+def headline_config(side, dims, strategy):
+    return dict(workload='cic_interlaced_pk_np%d^3_grid%d^3' % (side, dims),
+                particles=side ** 3, grid=dims, box_mpc_h=BOX, axis=0, MAS='CIC',
+                interlaced=True, strategy=strategy, parallelism='replicas',
+                l2_flush='inputs larger than L2 (%.1f GB positions)' % (12.0 * side ** 3 / 1e9))
 
 
 # ----------------------------------------------------------------------- clocks
@@ -245,6 +283,7 @@ def main():
 
     # ---- per-stage durations (events between C-ABI calls on the launching stream)
     stages = stage_times(pp, pos, reps=max(2, min(a.steps, 5)))
+    grids = grids_per_s(pp, reps=max(3, min(a.steps, 10)))
 
     # ---- end to end: pinned host positions -> device -> chain -> sums to host.
     # Two device position buffers: the copy of step i+1 runs on a copy stream
@@ -261,11 +300,21 @@ def main():
         cps = torch.cuda.Stream()
         copied = [torch.cuda.Event() for _ in range(2)]
         free = [torch.cuda.Event() for _ in range(2)]
+        # copy-stream events around every H2D copy: the link bandwidth each step saw
+        cpy = []
+
+        def copy_into(b):
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record(cps)
+            bufs[b].copy_(host, non_blocking=True)
+            c1.record(cps)
+            copied[b].record(cps)
+            cpy.append((c0, c1))
 
         def run(k2):
             with torch.cuda.stream(cps):
-                bufs[0].copy_(host, non_blocking=True)
-                copied[0].record(cps)
+                copy_into(0)
             for i in range(k2):
                 b = i % 2
                 comp.wait_event(copied[b])
@@ -277,10 +326,10 @@ def main():
                     with torch.cuda.stream(cps):
                         if i >= 1:
                             cps.wait_event(free[nb])
-                        bufs[nb].copy_(host, non_blocking=True)
-                        copied[nb].record(cps)
+                        copy_into(nb)
         run(2)
         torch.cuda.synchronize(); barrier()
+        cpy.clear()
         k2 = a.steps
         t0 = time.perf_counter()
         e0.record()
@@ -289,10 +338,15 @@ def main():
         torch.cuda.synchronize(); barrier()
         ms2 = max_over_ranks(e0.elapsed_time(e1), world, dev)
         wall = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+        hbytes = host.numel() * 4
+        h2d_ms = [c0.elapsed_time(c1) for c0, c1 in cpy]
         e2e = dict(value=whole_job_rate(n, k2, world, ms2), unit=UNIT,
-                   h2d_bytes_per_step=int(host.numel() * 4),
+                   h2d_bytes_per_step=int(hbytes),
                    d2h_bytes_per_step=int(sums_host.numel() * 8), ms_per_step=ms2 / k2,
-                   host_wall_ms_per_step=wall / k2, overlap='h2d of step i+1 under compute of step i')
+                   host_wall_ms_per_step=wall / k2, overlap='h2d of step i+1 under compute of step i',
+                   h2d_ms_per_step=[round(x, 2) for x in h2d_ms],
+                   h2d_gbs_median=float(np.median([hbytes / (x / 1e3) / 1e9 for x in h2d_ms])),
+                   device_ms_per_step=ms / a.steps)
         del host, bufs
         torch.cuda.empty_cache()
 
@@ -311,7 +365,7 @@ def main():
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
     hbm = peaks.get('hbm_gbs', 6800.0)
-    roof = roofline(stages, n, dims, hbm, 'measured' if 'hbm_gbs' in peaks else 'fallback')
+    roof = roofline(stages, n, dims, hbm, 'measured' if 'hbm_gbs' in peaks else 'fallback', ms / a.steps)
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
@@ -321,12 +375,9 @@ def main():
         line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=a.steps,
                     warmup=a.warmup, ms_per_step=ms / a.steps, higher_is_better=True,
                     scaling='weak', vs_baseline=None, dtype='f32', data='synthetic',
-                    config=dict(workload='cic_interlaced_pk_np%d^3_grid%d^3' % (side, dims),
-                                particles=n, grid=dims, box_mpc_h=BOX, axis=0, MAS='CIC',
-                                interlaced=True, strategy=a.strategy, parallelism='replicas',
-                                l2_flush='inputs larger than L2 (%.1f GB positions)' % (12.0 * n / 1e9)),
+                    config=headline_config(side, dims, a.strategy),
                     e2e=e2e, roofline=roof, cpu_baseline=cpu, clocks=clk,
-                    gpu_launches=kernels_per_step(dims) * a.steps, stages_ms=stages,
+                    gpu_launches=kernels_per_step(dims) * a.steps, stages_ms=stages, grids_per_s=grids,
                     secondary=secondary)
         print(json.dumps(line))
 
@@ -485,8 +536,7 @@ STAGES = ('fill', 'hist', 'place', 'place_b', 'deposit', 'sort', 'halo')
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, one pass of
 # counters) of each kernel of the CIC-interlaced step measured by ncu, keyed by
-# (particles, grid); summaries and commands in profiles/cic_interlaced_pk_1024_launches.md
-# and profiles/bin_deposit_fx_cic_interlaced_512.md.
+# (particles, grid), from an ncu capture of the bench step (not measured live).
 KERNEL_TRAFFIC = {
     (1024 ** 3, 1024): dict(hist=12.8850e9 + 0.0053e9, place=13.2252e9 + 17.3872e9,
                             place_b=17.3480e9 + 17.2813e9, deposit=29.0944e9 + 10.2683e9,
@@ -534,7 +584,36 @@ def stage_times(pp, pos, reps):
     return out
 
 
-def roofline(stages, n, dims, hbm, src):
+def grids_per_s(pp, reps):
+    """P(k) of grids already resident in HBM (no deposit): R2C + the fused interlace /
+    deconvolve / bin kernel, for the interlaced pair of the step and for one grid alone
+    (pyl_pk_bin with one field), CUDA events on the launching stream."""
+    import torch
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr, stream_ptr
+    d, st = pp.dims, stream_ptr()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, ng in (('interlaced_pair', 2), ('single_grid', 1)):
+        def once():
+            _lib.call('pyl_fft_r2c', ptr(pp.grids), ptr(pp.dk), d, ng, st)
+            _lib.call('pyl_pk_bin', ptr(pp.dk[0]), ptr(pp.dk[1]) if ng == 2 else None, 1, pp.dk[0].numel(), d,
+                      pp.axis, pp.mas_p, ptr(pp.sums), ptr(pp.pk_ws), pp.pk_ws_bytes, st)
+        once()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            once()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = dict(value=1e3 / ms, unit='grids/s', ms=ms, grid=d)
+    out['metric'] = 'P(k) of a resident %d^3 grid (R2C + fused bin), grids/s' % d
+    return out
+
+
+def roofline(stages, n, dims, hbm, src, ms_step):
     """Algorithmic HBM bytes per launch of each kernel or phase of the step:
       fill (two grids of -1): 2 x 4 B/cell written;
       hist: 12 B/particle read;  place (level A): 12 B read + 16 B written per particle;
@@ -558,9 +637,20 @@ def roofline(stages, n, dims, hbm, src):
     top = max(ms, key=lambda k: ms[k])
     achieved = alg[top] / (ms[top] / 1e3) / 1e9
     measured = KERNEL_TRAFFIC.get((n, dims), {})
+    # the whole step and the mass-assignment stage against the path's own algorithmic
+    # bytes (positions read once, both grids written once, two R2C, the binning read):
+    #   MA: 12 N_p + 2 x 4 N_g;  step: that + 2 (4 N_g + 8 N_h) + 2 x 8 N_h
+    ma_bytes = 12.0 * n + 2 * 4.0 * cells
+    step_bytes = ma_bytes + 2 * (4.0 * cells + 8.0 * modes) + 2 * 8.0 * modes
+    step_gbs = step_bytes / (ms_step / 1e3) / 1e9
+    ma_gbs = ma_bytes / (stages['density'] / 1e3) / 1e9
     return dict(bound='hbm', kernel=top, achieved=achieved, peak=hbm, unit='GB/s',
                 frac=achieved / hbm, traffic=measured.get(top), peak_source=src,
+                traffic_source='ncu capture of the bench step (dram__bytes_read.sum + dram__bytes_write.sum), '
+                               'not measured in this run',
                 alg_bytes=alg[top], ms=ms[top],
+                step=dict(alg_bytes=step_bytes, ms=ms_step, achieved=step_gbs, frac=step_gbs / hbm),
+                ma_stage=dict(alg_bytes=ma_bytes, ms=stages['density'], achieved=ma_gbs, frac=ma_gbs / hbm),
                 all_kernels={k: dict(ms=ms[k], gbs=alg[k] / (ms[k] / 1e3) / 1e9,
                                      frac=alg[k] / (ms[k] / 1e3) / 1e9 / hbm, traffic=measured.get(k))
                              for k in ms})

@@ -93,19 +93,36 @@ int pyl_ma_overdensity_rsd(float *pos, const float *vel, const float *weights, i
                            float *grid_interlaced, int dims, float box_size, int mas, int strategy, float hubble,
                            float redshift, int axis, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Float64 grids: replaces MAS_library.CICW_d (library/MAS_library/MAS_library.pyx:229-266)
+ * and NGPW_d (:338-358); TSC and PCS run the same way.
+ * grid     float64 [dims][dims][depth], ACCUMULATED into (+=); depth == dims for
+ *          ndim 3.  With ndim 2 the third index is 0 and the third-axis weight
+ *          1, as in the reference's 2D use of these kernels (CIC adds each
+ *          (x, y) term twice into plane 0).
+ * weights  float32 [n_particles], or NULL for unit weights.
+ * Each contribution is the reference's float32 product ((C0 C1) C2) W, added
+ * to its float64 cell with a float64 atomic: the sums differ from the
+ * reference's serial loop by float64 rounding at most (NGP sums of float32
+ * weights are exact while they fit 53 bits). */
+int pyl_ma_f64(const float *pos, const float *weights, int64_t n_particles, int ndim, double *grid, int dims,
+               int depth, float box_size, int mas, void *stream);
+
 /* Allocation-free mass assignment.  No counterpart in the reference: it exists
- * for callers that cannot allocate device memory around the call (code running
- * during CUDA-graph capture, plugins inside a host framework that owns the
- * device allocator, real-time loops that allocate nothing after start-up).
+ * for callers that cannot allocate device memory around the call, such as
+ * plugins inside a host framework whose own allocator owns all device memory,
+ * and real-time loops that allocate nothing after start-up.
  * Same deposit as pyl_ma with the tiled strategy (3D grids only, grid +=,
  * optional interlaced grid), but the binning scratch lives in a fixed 24 MiB
  * array compiled into the library, held by every GPU that loads it until the
  * process exits.  Limits: n_particles <= 524288 and dims <= 512; larger
  * requests return PYL_ERR_INVALID.  The first call on a device looks up the
- * array's device address and sets kernel attributes; make that first call
- * before any stream capture.  All calls share the one array, so calls that
- * overlap on the GPU (different streams, or different host threads) race and
- * must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
+ * array's device address, and the first call with each combination of MAS,
+ * weights and interlacing raises the shared-memory limits of its kernels; make
+ * those first calls before any stream capture.  All calls share the one array
+ * and each keeps the previous call's contents (the call clears what must start
+ * at zero), so calls that overlap on the GPU (different streams, or different
+ * host threads) race and must be serialised by the caller.  Calls no
+ * cudaMalloc/cudaFree. */
 int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n_particles, float *grid,
                    float *grid_interlaced, int dims, float box_size, int mas, void *stream);
 
@@ -317,10 +334,27 @@ int pyl_xi_bin(const float *xi_grid, int dims, int axis, double *sums, void *str
 int pyl_stage_timing(int enable);
 int pyl_stage_times(double *ms_out, int n);
 
+/* Thresholds of the tiled deposit's code paths (no counterpart in the reference),
+ * process-wide, for tests and tuning: grids from owned_min_dims per side up
+ * (multiples of 32) take the owned-cell write-out (default 1024), and unweighted
+ * CIC/TSC/PCS deposits of at least tot_min_per_cell particles per bin cell on
+ * average find fixed-point wraps from each bin's total (default 2.0).  A negative
+ * value restores that default.  Change them only between calls (the workspace
+ * size depends on the first). */
+int pyl_ma_set_thresholds(int owned_min_dims, double tot_min_per_cell);
+
 /* Device-side error word (no counterpart in the reference): nonzero when a kernel's
  * bounded wait for its own bulk copies ran out and the kernel left early (its
  * output is then incomplete).  Synchronous; reset = 1 clears it. */
 int pyl_device_error(int reset, unsigned *out);
+
+/* Exercises that bounded wait (no counterpart in the reference; for tests): one
+ * thread arms a shared-memory mbarrier for arm_bytes (a multiple of 16) of
+ * bulk-copy data, issues no copy and waits at most `cycles` SM clock cycles
+ * (0 < cycles <= 2e8).  *completed (device) becomes 1 if the phase completed
+ * (arm_bytes == 0) and 0 if the wait ran out, which also sets the device error
+ * word read by pyl_device_error.  Nothing is left in flight. */
+int pyl_wait_probe(unsigned arm_bytes, long long cycles, unsigned *completed, void *stream);
 
 /* ---- particle-side neighbours of the mass assignment --------------------------
  * pyl_cic_interp replaces MAS_library.CIC_interp (library/MAS_library/MAS_library.pyx:558-599):

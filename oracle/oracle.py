@@ -9,6 +9,7 @@ P(k) mode loop); this file restates the rest in numpy, each part citing the
 reference lines it follows:
 
   MA()                MAS_library.pyx:57-112 (dispatch, 2D renormalisation)
+  ma_f64()            CICW_d MAS_library.pyx:229-266, NGPW_d :338-358 (float64 grids)
   frequencies()       Pk_library.pyx:59-64
   MAS_function()      Pk_library.pyx:75-81
   check_number_modes  Pk_library.pyx:90-102
@@ -97,6 +98,49 @@ def ma_kernel(pos, number, BoxSize, MAS, W=None, threads=1, flavor=0):
         raise ValueError('oracle_ma failed (%d)' % rc)
 
 
+def ma_f64(pos, number, BoxSize, MAS, W):
+    """CICW_d / NGPW_d (MAS_library.pyx:229-266, :338-358) in numpy: float32 weights and
+    products as the compiled reference evaluates them, added to the float64 grid number[dims][dims][depth]
+    in the reference's serial order (particle by particle, corners in its order).  2D positions
+    keep the third index at 0 with weight 1.0 on both CIC sides."""
+    assert pos.dtype == np.float32 and number.dtype == np.float64 and number.ndim == 3
+    n, coord = pos.shape
+    dims, depth = number.shape[0], number.shape[2]
+    inv = np.float32(dims) / np.float32(BoxSize)
+    W = np.asarray(W, dtype=np.float32)
+    flat = number.reshape(-1)
+    if MAS == 'NGP':
+        idx = np.zeros((n, 3), np.int64)
+        for a in range(coord):
+            k = np.trunc((pos[:, a] * inv).astype(np.float64) + 0.5).astype(np.int64)
+            idx[:, a] = np.mod(k, dims)
+        np.add.at(flat, (idx[:, 0] * dims + idx[:, 1]) * depth + idx[:, 2], W.astype(np.float64))
+        return
+    if MAS != 'CIC':
+        raise ValueError('the reference has CICW_d and NGPW_d only')
+    lo = np.zeros((n, 3), np.int64)
+    hi = np.zeros((n, 3), np.int64)
+    d = np.ones((n, 3), np.float32)
+    u = np.ones((n, 3), np.float32)
+    for a in range(coord):
+        dist = (pos[:, a] * inv).astype(np.float32)
+        k = np.trunc(dist).astype(np.int64)
+        u[:, a] = (dist - k.astype(np.float32)).astype(np.float32)
+        d[:, a] = (np.float32(1.0) - u[:, a]).astype(np.float32)
+        lo[:, a] = np.mod(k, dims)
+        hi[:, a] = np.mod(lo[:, a] + 1, dims)
+    idxs, vals = [], []
+    for cx, ix in ((d[:, 0], lo[:, 0]), (u[:, 0], hi[:, 0])):
+        for cy, iy in ((d[:, 1], lo[:, 1]), (u[:, 1], hi[:, 1])):
+            for cz, iz in ((d[:, 2], lo[:, 2]), (u[:, 2], hi[:, 2])):
+                idxs.append((ix * dims + iy) * depth + iz)
+                # (d0 d1)(d2 W): the association the reference's -ffast-math build evaluates
+                # (its source reads left to right; the compiled golden grids pin this order)
+                vals.append(((cx * cy).astype(np.float32) * (cz * W).astype(np.float32)).astype(np.float32))
+    order = np.stack(idxs, axis=1).reshape(-1)       # particle-major, corners in the reference's order
+    np.add.at(flat, order, np.stack(vals, axis=1).reshape(-1).astype(np.float64))
+
+
 def MA(pos, number, BoxSize, MAS='CIC', W=None, renormalize_2D=True, threads=1):
     """MAS_library.MA (MAS_library.pyx:57-112): accumulate into ``number`` in place."""
     if pos.shape[1] != number.ndim:
@@ -164,9 +208,13 @@ def interlace_combine(dk1, dk2):
     k = np.arange(dims)
     k = np.where(k > middle, k - dims, k)      # the reference's signed frequency (Pk_library.pyx:315)
     kz = np.arange(dims // 2 + 1)
-    ph = np.pi / dims * (k[:, None, None] + k[None, :, None] + kz[None, None, :])
-    out = 0.5 * (dk1.astype(np.complex128) + dk2.astype(np.complex128) * np.exp(1j * ph))
-    return out.astype(np.complex64)
+    out = np.empty(dk1.shape, np.complex64)
+    step = max(1, (1 << 24) // (dims * (dims // 2 + 1)))      # x slabs of ~16M modes (bounded memory)
+    for x0 in range(0, dims, step):
+        x1 = min(dims, x0 + step)
+        ph = np.pi / dims * (k[x0:x1, None, None] + k[None, :, None] + kz[None, None, :])
+        out[x0:x1] = 0.5 * (dk1[x0:x1].astype(np.complex128) + dk2[x0:x1].astype(np.complex128) * np.exp(1j * ph))
+    return out
 
 
 def pk_mode_sums(dk_fields, axis, mas_p, threads=1):
@@ -176,7 +224,10 @@ def pk_mode_sums(dk_fields, axis, mas_p, threads=1):
     kF, kN, kmax_par, kmax_per, kmax = frequencies(1.0, dims)
     nb1, nb2, nb3 = kmax_par + 1, (kmax_par + 1) * (kmax_per + 1), kmax + 1
     X = F * (F - 1) // 2
-    dk = np.ascontiguousarray(np.stack(dk_fields).astype(np.complex64))
+    if F == 1 and dk_fields[0].dtype == np.complex64 and dk_fields[0].flags.c_contiguous:
+        dk = dk_fields[0][None]                        # no copy of a large single field
+    else:
+        dk = np.ascontiguousarray(np.stack(dk_fields).astype(np.complex64))
     z = lambda *s: np.zeros(s, np.float64)
     out = dict(k1D=z(nb1), Nmodes1D=z(nb1), Pk1D=z(nb1, F), PkX1D=z(nb1, max(X, 1)),
                Nmodes2D=z(nb2), Pk2D=z(nb2, F), PkX2D=z(nb2, max(X, 1)),

@@ -3,6 +3,7 @@
 Mirrors library/MAS_library/MAS_library.pyx:
   MA(pos, number, BoxSize, MAS='CIC', W=None, verbose=False, renormalize_2D=True)  (:57-112)
   NGP/CIC/TSC/PCS(pos, number, BoxSize) and NGPW/CICW/TSCW/PCSW(..., W)          (:123-545)
+  CICW_d(pos, number, BoxSize, W), NGPW_d(pos, number, BoxSize, W): float64 grids (:229-266, :338-358)
   NGPc3D/CICc3D/... (pos, number, BoxSize, threads), *Wc3D(pos, number, W, BoxSize, threads),
   *c2D                                                                            (:1136-1221)
   FLOAT_type()                                                                     (:11-13)
@@ -25,9 +26,9 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import as_device_f32, is_torch, ptr, require_cuda, stream_ptr, workspace
+from ._device import as_device_f32, as_device_f64, is_torch, ptr, require_cuda, stream_ptr, workspace
 
-__all__ = ['MA', 'NGP', 'CIC', 'TSC', 'PCS', 'NGPW', 'CICW', 'TSCW', 'PCSW', 'FLOAT_type',
+__all__ = ['MA', 'NGP', 'CIC', 'TSC', 'PCS', 'NGPW', 'CICW', 'TSCW', 'PCSW', 'CICW_d', 'NGPW_d', 'FLOAT_type',
            'NGPc3D', 'CICc3D', 'TSCc3D', 'PCSc3D', 'NGPWc3D', 'CICWc3D', 'TSCWc3D', 'PCSWc3D',
            'NGPc2D', 'CICc2D', 'TSCc2D', 'PCSc2D', 'NGPWc2D', 'CICWc2D', 'TSCWc2D', 'PCSWc2D',
            'CIC_interp', 'ma_device', 'overdensity_device']
@@ -146,6 +147,44 @@ def _single(mas, weighted):
 
 NGP, CIC, TSC, PCS = (_single(m, False) for m in ('NGP', 'CIC', 'TSC', 'PCS'))
 NGPW, CICW, TSCW, PCSW = (_single(m, True) for m in ('NGP', 'CIC', 'TSC', 'PCS'))
+
+
+def _ma_f64(pos, number, BoxSize, mas, W):
+    """Deposit into a float64 grid (number[dims][dims][depth], += in place; numpy
+    arrays are copied to the device and written back)."""
+    require_cuda()
+    dpos = as_device_f32(pos, 'pos')
+    dW = as_device_f32(W, 'W') if W is not None else None
+    dgrid = as_device_f64(number, 'number')
+    if dpos.dim() != 2 or dpos.shape[1] not in (2, 3):
+        raise ValueError('pos must be (N,2) or (N,3)')
+    if dgrid.dim() != 3:
+        raise ValueError('number must be a 3D float64 array')
+    n, ndim = dpos.shape
+    if dW is not None and (dW.dim() != 1 or dW.shape[0] != n):
+        raise ValueError('W must have one weight per particle')
+    dims, depth = dgrid.shape[0], dgrid.shape[2]
+    if ndim == 3 and tuple(dgrid.shape) != (dims, dims, dims):
+        raise ValueError('number must be (dims, dims, dims) for 3D positions')
+    if ndim == 2 and dgrid.shape[1] != dims:
+        raise ValueError('number must be (dims, dims, depth) for 2D positions')
+    _lib.call('pyl_ma_f64', ptr(dpos), ptr(dW), n, ndim, ptr(dgrid), dims, depth, float(BoxSize),
+              _lib.MAS_INDEX[mas], stream_ptr())
+    if is_torch(number):
+        if not number.is_cuda:
+            number.copy_(dgrid.cpu())
+    else:
+        np.copyto(number, dgrid.cpu().numpy())
+
+
+def CICW_d(pos, number, BoxSize, W):
+    """MAS_library.CICW_d: weighted CIC into a float64 grid (MAS_library.pyx:229-266)."""
+    _ma_f64(pos, number, BoxSize, 'CIC', W)
+
+
+def NGPW_d(pos, number, BoxSize, W):
+    """MAS_library.NGPW_d: weighted NGP into a float64 grid (MAS_library.pyx:338-358)."""
+    _ma_f64(pos, number, BoxSize, 'NGP', W)
 
 
 def _cpath(mas, weighted, ndim):

@@ -50,6 +50,24 @@ def as_device_f32(a, name, device=None):
     return torch.from_numpy(np.ascontiguousarray(arr)).to(device)
 
 
+def as_device_f64(a, name, device=None):
+    """float64 C-contiguous CUDA tensor viewing (or copying) `a` (the reference's
+    np.float64_t[:,:,:] grids of the *_d kernels)."""
+    device = device or torch.device('cuda', torch.cuda.current_device())
+    if is_torch(a):
+        if a.dtype != torch.float64:
+            raise ValueError('%s must be float64, got %s' % (name, a.dtype))
+        if a.is_cuda:
+            if not a.is_contiguous():
+                raise ValueError('%s must be C-contiguous' % name)
+            return a
+        return a.contiguous().to(device)
+    arr = np.asarray(a)
+    if arr.dtype != np.float64:
+        raise ValueError('Buffer dtype mismatch: %s must be float64, got %s' % (name, arr.dtype))
+    return torch.from_numpy(np.ascontiguousarray(arr)).to(device)
+
+
 def as_device_c64(a, name, device=None):
     device = device or torch.device('cuda', torch.cuda.current_device())
     if is_torch(a):

@@ -29,6 +29,7 @@ SIGNATURES = {
     'pyl_ma_workspace_size': (_SZ, [_I64, _I, _I, _I, _I, _I]),
     'pyl_ma': (_I, [_P, _P, _I64, _I, _P, _P, _I, _F, _I, _I, _I, _P, _SZ, _P]),
     'pyl_ma_noalloc': (_I, [_P, _P, _I64, _P, _P, _I, _F, _I, _P]),
+    'pyl_ma_f64': (_I, [_P, _P, _I64, _I, _P, _I, _I, _F, _I, _P]),
     'pyl_ma_overdensity': (_I, [_P, _P, _I64, _P, _P, _I, _F, _I, _I, _P, _SZ, _P]),
     'pyl_ma_overdensity_rsd': (_I, [_P, _P, _P, _I64, _P, _P, _I, _F, _I, _I, _F, _F, _I, _P, _SZ, _P]),
     'pyl_ma_batch': (_I, [_P, _I, _P, _I, _P, _I, _P]),
@@ -65,6 +66,8 @@ SIGNATURES = {
     'pyl_stage_timing': (_I, [_I]),
     'pyl_stage_times': (_I, [_P, _I]),
     'pyl_device_error': (_I, [_I, _P]),
+    'pyl_ma_set_thresholds': (_I, [_I, _D]),
+    'pyl_wait_probe': (_I, [ctypes.c_uint, ctypes.c_longlong, _P, _P]),
     'pyl_cic_interp': (_I, [_P, _I, _F, _P, _I64, _P, _P]),
     'pyl_pos_redshift_space': (_I, [_P, _P, _I64, _F, _F, _F, _I, _P]),
 }

@@ -86,7 +86,25 @@ namespace pyl {
 namespace {
 std::mutex g_smem_mu;
 std::map<std::pair<int, const void *>, size_t> g_smem_limits;
+std::mutex g_sm_mu;
+std::map<int, int> g_sm_count;
 }  // namespace
+
+int num_sms()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_sm_mu);
+    auto it = g_sm_count.find(dev);
+    if (it != g_sm_count.end()) return it->second;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();     // no device (host-side size queries): the GB300's count
+        n = 152;
+    }
+    g_sm_count[dev] = n;
+    return n;
+}
 
 size_t smem_limit_raise(const void *kernel, size_t bytes, cudaError_t *err)
 {

@@ -33,17 +33,9 @@ void stage_mark(int phase, bool begin, cudaStream_t st);
 
 #define PYL_LAUNCH_CHECK() PYL_CUDA(cudaGetLastError())
 
-static inline int num_sms()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 152;
-    }
-    return n;
-}
+// Multiprocessor count of the current device, looked up once per device under a
+// lock (workspace layouts and grid sizes follow the device a call runs on).
+int num_sms();
 
 // Non-negative modulo: the cell index of any integer on a periodic axis.  The
 // 64-bit division only runs for indices more than one period outside [0, n).

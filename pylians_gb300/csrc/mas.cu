@@ -27,6 +27,7 @@
 
 #include <stdlib.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -1058,7 +1059,14 @@ TiledWs tiled_layout(void *base, long long n, int dims, size_t halo_floats = 0)
 // below that the fill pass plus atomic write-out measures as fast or faster (the
 // four-bin CTAs of the owned deposit leave too few CTAs to balance 152 SMs).
 constexpr int OWNED_MIN_DIMS = 1024;
-inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= OWNED_MIN_DIMS; }
+// Unweighted CIC/TSC/PCS deposits with at least this many particles per bin cell on
+// average find fixed-point wraps from each bin's total (see fx_accumulate).
+constexpr double TOT_MIN_PER_CELL = 2.0;
+// Both thresholds can be moved process-wide by pyl_ma_set_thresholds (tests reach
+// the large-grid code paths on small grids with it).
+std::atomic<int> g_owned_min_dims{OWNED_MIN_DIMS};
+std::atomic<double> g_tot_min_per_cell{TOT_MIN_PER_CELL};
+inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= g_owned_min_dims.load(); }
 
 // Floats of the owned-cell halo buffers of both grids (0 when the grid does not
 // take the owned-cell write-out, or a non-interlaced NGP deposit has no halo).
@@ -1595,7 +1603,7 @@ int launch_deposit_fx(const TiledWs &ws, TileGeom g, float inv, float halfcell, 
         // bin-total wrap detection: unweighted non-NGP deposits of two or more
         // particles per bin cell on average
         const bool tot = MAS != PYL_MAS_NGP && !inv_w &&
-                         (double)ws.n >= 2.0 * (double)g.nt * g.nt * g.nt * (double)FS::CELLS;
+                         (double)ws.n >= g_tot_min_per_cell.load() * (double)g.nt * g.nt * g.nt * (double)FS::CELLS;
         // owned-cell launches: no block barriers per batch
         auto kern = ow.on ? (p2 ? (tot ? bin_deposit_fx_tma_kernel<MAS, I, RR, true, true, true>
                                        : bin_deposit_fx_tma_kernel<MAS, I, RR, true, false, true>)
@@ -2025,11 +2033,81 @@ extern "C" int pyl_ma_overdensity_rsd(float *pos, const float *vel, const float 
                                workspace_bytes, stream, &r);
 }
 
+// ------------------------------------------------------------- float64 grids
+// MAS_library.CICW_d (MAS_library.pyx:229-266) and NGPW_d (:338-358): float32
+// positions, weights and per-cell products exactly as the float32 kernels
+// ((C0*C1)*C2)*W, no FMA), each product added to a float64 cell.  The grid is
+// [dims][dims][depth]; with 2D positions the third index stays 0 and the third
+// axis weight 1, so CIC adds each (x, y) term twice into plane 0, as the
+// reference's loop over index_d[2] = index_u[2] = 0 does.
+namespace pyl {
+namespace {
+template <int MAS>
+__global__ void __launch_bounds__(256) ma_f64_kernel(const float *__restrict__ pos, const float *__restrict__ w,
+                                                     long long n, int ndim, double *__restrict__ grid, int dims,
+                                                     long long depth, float inv)
+{
+    constexpr int S = Support<MAS>::S;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float C[3][S];
+        int idx[3][S];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (a < ndim) {
+                const int f = axis_weights<MAS>(__ldg(pos + i * ndim + a), inv, C[a]);
+#pragma unroll
+                for (int j = 0; j < S; j++) idx[a][j] = wrap_index((long long)f + j, dims);
+            } else {
+#pragma unroll
+                for (int j = 0; j < S; j++) { C[a][j] = 1.0f; idx[a][j] = 0; }
+            }
+        }
+        const float wi = w ? __ldg(w + i) : 1.0f;
+#pragma unroll
+        for (int l = 0; l < S; l++)
+#pragma unroll
+            for (int m = 0; m < S; m++) {
+                const float c01 = __fmul_rn(C[0][l], C[1][m]);
+                double *row = grid + ((long long)idx[0][l] * dims + idx[1][m]) * depth;
+#pragma unroll
+                for (int q = 0; q < S; q++)
+                    atomicAdd(row + idx[2][q], (double)__fmul_rn(__fmul_rn(c01, C[2][q]), wi));
+            }
+    }
+}
+}  // namespace
+}  // namespace pyl
+
+extern "C" int pyl_ma_f64(const float *pos, const float *weights, int64_t n, int ndim, double *grid, int dims,
+                          int depth, float box_size, int mas, void *stream)
+{
+    PYL_CHECK_ARG(ndim == 2 || ndim == 3, "ndim must be 2 or 3");
+    PYL_CHECK_ARG(mas >= PYL_MAS_NGP && mas <= PYL_MAS_PCS, "MAS must be NGP, CIC, TSC or PCS");
+    PYL_CHECK_ARG(dims > 0 && dims <= 65536, "dims out of range");
+    PYL_CHECK_ARG(depth > 0 && (ndim == 2 || depth == dims), "depth must equal dims for 3D positions");
+    PYL_CHECK_ARG(n >= 0, "negative particle count");
+    PYL_CHECK_ARG(grid != nullptr, "grid is NULL");
+    PYL_CHECK_ARG(n == 0 || pos != nullptr, "pos is NULL");
+    PYL_CHECK_ARG(box_size > 0.0f && isfinite(box_size), "BoxSize must be positive and finite");
+    if (n == 0) return PYL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float inv = (float)dims / box_size;                 // MAS_library.pyx:245,352
+    const int blocks = grid_blocks(n, 256, 16);
+    switch (mas) {
+        case PYL_MAS_NGP: ma_f64_kernel<PYL_MAS_NGP><<<blocks, 256, 0, st>>>(pos, weights, n, ndim, grid, dims, depth, inv); break;
+        case PYL_MAS_CIC: ma_f64_kernel<PYL_MAS_CIC><<<blocks, 256, 0, st>>>(pos, weights, n, ndim, grid, dims, depth, inv); break;
+        case PYL_MAS_TSC: ma_f64_kernel<PYL_MAS_TSC><<<blocks, 256, 0, st>>>(pos, weights, n, ndim, grid, dims, depth, inv); break;
+        default:          ma_f64_kernel<PYL_MAS_PCS><<<blocks, 256, 0, st>>>(pos, weights, n, ndim, grid, dims, depth, inv); break;
+    }
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
 // ------------------------------------------------------- allocation-free variant
-// Some callers cannot allocate device memory around a call: code that runs
-// while a CUDA graph is being captured (cudaMalloc is not a capturable
-// operation), plugins hosted by a framework whose allocator owns all device
-// memory, and real-time loops that forbid allocation after start-up.  For them,
+// Some callers cannot allocate device memory around a call: plugins hosted by
+// a framework whose allocator owns all device memory, and real-time loops that
+// forbid allocation after start-up.  For them,
 // pyl_ma_noalloc deposits through the same tiled kernels as pyl_ma but keeps
 // the binning scratch in a fixed array compiled into this library.
 namespace pyl {
@@ -2100,6 +2178,46 @@ extern "C" int pyl_ma_noalloc(const float *pos, const float *weights, int64_t n,
         case PYL_MAS_TSC: return launch_tiled<PYL_MAS_TSC>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
         default:          return launch_tiled<PYL_MAS_PCS>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, scratch, OutScale{1.0f, nullptr}, st);
     }
+}
+
+// ------------------------------------------------------- bounded-wait probe
+// One thread arms an mbarrier for arm_bytes of bulk-copy data and issues no copy,
+// then waits on it with the staged kernels' bounded wait and the given cycle
+// limit: with arm_bytes > 0 the phase never completes, the wait runs out, sets
+// the device error word (pyl_device_error) and the kernel returns; with 0 the
+// phase completes at the arrive and the word is left alone.  Nothing is in
+// flight when the CTA leaves.
+namespace pyl {
+namespace {
+__global__ void wait_probe_kernel(unsigned arm_bytes, long long cycles, unsigned *out)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+    mbar_arrive_expect_tx(&bar, arm_bytes);
+    *out = mbar_wait_bounded(&bar, 0u, &g_tma_error, cycles) ? 1u : 0u;
+}
+}  // namespace
+}  // namespace pyl
+
+extern "C" int pyl_wait_probe(unsigned arm_bytes, long long cycles, unsigned *completed, void *stream)
+{
+    PYL_CHECK_ARG(completed != nullptr, "completed is NULL");
+    PYL_CHECK_ARG(cycles > 0 && cycles <= pyl::MBAR_WAIT_CYCLES, "cycles must be in (0, 2e8]");
+    PYL_CHECK_ARG(arm_bytes % 16 == 0 && arm_bytes < (1u << 20), "arm_bytes must be a multiple of 16 below 2^20");
+    pyl::wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(arm_bytes, cycles, completed);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
+extern "C" int pyl_ma_set_thresholds(int owned_min_dims, double tot_min_per_cell)
+{
+    PYL_CHECK_ARG(owned_min_dims != 0, "owned_min_dims must be positive (or negative for the default)");
+    PYL_CHECK_ARG(!(tot_min_per_cell != tot_min_per_cell), "tot_min_per_cell is NaN");
+    pyl::g_owned_min_dims.store(owned_min_dims < 0 ? pyl::OWNED_MIN_DIMS : owned_min_dims);
+    pyl::g_tot_min_per_cell.store(tot_min_per_cell < 0.0 ? pyl::TOT_MIN_PER_CELL : tot_min_per_cell);
+    return PYL_OK;
 }
 
 extern "C" int pyl_device_error(int reset, unsigned *out)

@@ -62,12 +62,13 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
 
 // Bounded wait for phase `parity` of `bar`; false (and *err set) when the time
 // limit runs out or *err is already set.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, unsigned *err)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, unsigned *err,
+                                                  long long limit = MBAR_WAIT_CYCLES)
 {
     const long long t0 = clock64();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > MBAR_WAIT_CYCLES || *(volatile unsigned *)err) break;
+        if (clock64() - t0 > limit || *(volatile unsigned *)err) break;
     }
     atomicOr(err, 1u);
     return false;

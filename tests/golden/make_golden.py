@@ -85,6 +85,33 @@ def make_ma(MASL):
     return out
 
 
+def make_ma_d(MASL):
+    """CICW_d / NGPW_d (float64 grids): 3D on the per-cell mesh of make_ma, 2D
+    positions into a (N, N, 1) grid, and accumulation onto a non-zero base."""
+    out = {}
+    rng = np.random.default_rng(20240602)
+    N, L = 24, 1000.0
+    pos = np.concatenate([(rng.random((3000, 3)) * L).astype(np.float32), edge_positions(L, N)])
+    W = (rng.random(pos.shape[0]) * 3.0).astype(np.float32)
+    out['pos'] = pos
+    out['W'] = W
+    out['meta'] = np.array([N, L])
+    base = rng.random((N, N, N))
+    out['base'] = base
+    for name in ('CICW_d', 'NGPW_d'):
+        fn = getattr(MASL, name)
+        d = np.zeros((N, N, N), np.float64)
+        fn(pos, d, L, W)
+        out['%s_3D' % name] = d
+        d = base.copy()
+        fn(pos, d, L, W)
+        out['%s_3D_accum' % name] = d
+        d = np.zeros((N, N, 1), np.float64)
+        fn(np.ascontiguousarray(pos[:, :2]), d, L, W)
+        out['%s_2D' % name] = d
+    return out
+
+
 def cic_overdensity(MASL, pos, N, L):
     d = np.zeros((N, N, N), np.float32)
     MASL.MA(pos, d, L, 'CIC')
@@ -240,12 +267,14 @@ def make_smoothing(MASL):
     return out
 
 
-def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing')):
+def main(which=('ma', 'ma_d', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing')):
     if not build_ref.built():
         build_ref.build()
     MASL, PKL, BKL = build_ref.load_reference()
     if 'ma' in which:
         np.savez_compressed(os.path.join(HERE, 'ma_golden.npz'), **make_ma(MASL))
+    if 'ma_d' in which:
+        np.savez_compressed(os.path.join(HERE, 'ma_d_golden.npz'), **make_ma_d(MASL))
     if 'pk' in which:
         np.savez_compressed(os.path.join(HERE, 'pk_golden.npz'), **make_pk(MASL, PKL))
     if 'bk' in which:
@@ -265,4 +294,4 @@ def main(which=('ma', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing')):
 
 
 if __name__ == '__main__':
-    main(tuple(sys.argv[1:]) or ('ma', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing'))
+    main(tuple(sys.argv[1:]) or ('ma', 'ma_d', 'pk', 'bk', 'interp', 'xi', 'plane', 'smoothing'))

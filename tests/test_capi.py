@@ -134,3 +134,32 @@ def test_interp_and_shift_reject_bad_arguments(lib):
     assert 'axis' in lib.pyl_last_error().decode()
     assert lib.pyl_pos_redshift_space(buf, buf, -1, 1.0, 100.0, 0.0, 0, None) == 1
     assert 'negative' in lib.pyl_last_error().decode()
+
+
+def test_f64_grid_rejects_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)
+    f64 = lib.pyl_ma_f64
+    assert f64(buf, buf, 10, 3, buf, 16, 8, 1.0, 2, None) == 1
+    assert 'depth' in lib.pyl_last_error().decode()
+    assert f64(buf, buf, 10, 4, buf, 16, 16, 1.0, 2, None) == 1
+    assert 'ndim' in lib.pyl_last_error().decode()
+    assert f64(buf, buf, 10, 3, None, 16, 16, 1.0, 2, None) == 1
+    assert 'grid' in lib.pyl_last_error().decode()
+    assert f64(buf, buf, 10, 3, buf, 16, 16, 0.0, 2, None) == 1
+    assert 'BoxSize' in lib.pyl_last_error().decode()
+    assert f64(buf, buf, 10, 3, buf, 16, 16, 1.0, 9, None) == 1
+    assert 'MAS' in lib.pyl_last_error().decode()
+    assert f64(buf, buf, 0, 3, buf, 16, 16, 1.0, 2, None) == 0     # nothing to deposit, nothing launched
+
+
+def test_wait_probe_and_thresholds_reject_bad_arguments(lib):
+    buf = ctypes.c_void_p(16)
+    assert lib.pyl_wait_probe(16, 0, buf, None) == 1
+    assert 'cycles' in lib.pyl_last_error().decode()
+    assert lib.pyl_wait_probe(16, 10 ** 9, buf, None) == 1
+    assert lib.pyl_wait_probe(12, 1000, buf, None) == 1
+    assert 'arm_bytes' in lib.pyl_last_error().decode()
+    assert lib.pyl_wait_probe(16, 1000, None, None) == 1
+    assert lib.pyl_ma_set_thresholds(0, 1.0) == 1
+    assert lib.pyl_ma_set_thresholds(-1, float('nan')) == 1
+    assert lib.pyl_ma_set_thresholds(-1, -1.0) == 0

@@ -438,3 +438,30 @@ def test_staged_placement_reports_no_device_error(MASL):
     _lib.call('pyl_device_error', 0, ctypes.byref(word))
     assert word.value == 0
     assert (a - b).abs().max().item() <= 2e-6 * a.abs().max().item()
+
+
+@pytest.mark.parametrize('name', ['CICW_d', 'NGPW_d'])
+def test_ma_f64_golden(MASL, name):
+    """CICW_d / NGPW_d into float64 grids against the compiled reference: NGPW_d bit-exact
+    (float32 weights summed in float64 are exact here, whatever the order); CICW_d within
+    1e-6 of the grid maximum (the reference's -ffast-math build multiplies the four float32
+    factors in another association, an ulp apart).  3D onto zeros and onto a non-zero base
+    (+=), 2D positions into a (N, N, 1) grid, numpy in and a CUDA tensor in place."""
+    g = np.load(os.path.join(GOLDEN, 'ma_d_golden.npz'))
+    pos, W = g['pos'], g['W']
+    N, L = int(g['meta'][0]), float(g['meta'][1])
+    fn = getattr(MASL, name)
+    exact = name == 'NGPW_d'
+    tol = 1e-6
+    d = np.zeros((N, N, N))
+    fn(pos, d, L, W)
+    close(d, g['%s_3D' % name], exact, tol)
+    d = g['base'].copy()
+    fn(pos, d, L, W)
+    close(d, g['%s_3D_accum' % name], exact, tol)
+    d = np.zeros((N, N, 1))
+    fn(np.ascontiguousarray(pos[:, :2]), d, L, W)
+    close(d, g['%s_2D' % name], exact, tol)
+    t = torch.zeros((N, N, N), dtype=torch.float64, device='cuda')
+    fn(torch.from_numpy(pos).cuda(), t, L, torch.from_numpy(W).cuda())
+    close(t.cpu().numpy(), g['%s_3D' % name], exact, tol)

@@ -239,3 +239,22 @@ def test_oracle_smoothing_golden(sg, N, filt, R):
     sm = O.field_smoothing(sg['field_%d' % N], gf)
     ref = sg['smoothed_%s_%d' % (t, N)]
     assert np.abs(sm - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize('name,mas', [('CICW_d', 'CIC'), ('NGPW_d', 'NGP')])
+def test_ma_f64_golden(name, mas):
+    """CICW_d / NGPW_d (MAS_library.pyx:229-266, :338-358): float64 grids.  The oracle adds the
+    same float32 products in the reference's serial order, so every case is bit-exact: 3D onto
+    zeros and onto a non-zero base, and 2D positions into a (N, N, 1) grid."""
+    g = np.load(os.path.join(GOLDEN, 'ma_d_golden.npz'))
+    pos, W = g['pos'], g['W']
+    N, L = int(g['meta'][0]), float(g['meta'][1])
+    d = np.zeros((N, N, N))
+    O.ma_f64(pos, d, L, mas, W)
+    np.testing.assert_array_equal(d, g['%s_3D' % name])
+    d = g['base'].copy()
+    O.ma_f64(pos, d, L, mas, W)
+    np.testing.assert_array_equal(d, g['%s_3D_accum' % name])
+    d = np.zeros((N, N, 1))
+    O.ma_f64(np.ascontiguousarray(pos[:, :2]), d, L, mas, W)
+    np.testing.assert_array_equal(d, g['%s_2D' % name])

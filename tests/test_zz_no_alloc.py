@@ -1,8 +1,8 @@
 """Allocation-free mass assignment: pyl_ma_noalloc through the C-ABI.
 
-Some callers of this library cannot allocate device memory around a call: code
-that runs while a CUDA graph is being captured, plugins hosted by a framework
-that owns the device allocator, loops that allocate nothing after start-up.
+Some callers of this library cannot allocate device memory around a call:
+plugins hosted by a framework whose allocator owns all device memory, and loops
+that allocate nothing after start-up.
 pyl_ma_noalloc serves them with binning scratch compiled into the library
 (24 MiB per device; at most 524288 particles and dims <= 512).
 
