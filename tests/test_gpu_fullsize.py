@@ -261,4 +261,9 @@ def test_batch_sample_vs_oracle(tmp_path):
         a = oracle_overdensity(host, N, L, mas)
         b = oracle_overdensity(host, N, L, mas, shift=True) if s['interlaced'] else None
         o = O.Pk(a, L, 0, mas, T, interlaced=b)
-        check_pk(r, lambda k: getattr(o, k), [k for k in PK_NAMES if k != 'Pkphase'])
+        # 1e5 particles on 256^3 cells are pure shot noise, and near the grid's corner the
+        # TSC/PCS window leaves (2/pi)^(6p) of that power, so after deconvolution the
+        # float32 rounding of either grid (white in k) is a 1e-4 effect in those Pk2D
+        # bins, and one-mode bins can hold 1e-4 of the typical power: a floor of 5e-4
+        # of the median bin for Pk2D
+        check_pk(r, lambda k: getattr(o, k), [k for k in PK_NAMES if k != 'Pkphase'], floor2d=5e-4)

@@ -43,7 +43,7 @@ def cross_scale(auto, nfields):
     return np.stack(cols, axis=-1)
 
 
-def check_pk(r, get, names, cross=False, floor=1e-8):
+def check_pk(r, get, names, cross=False, floor=1e-8, floor2d=0.0):
     for n in names:
         x, y = np.asarray(getattr(r, n)), np.asarray(get(n))
         assert x.shape == y.shape, (n, x.shape, y.shape)
@@ -70,10 +70,19 @@ def check_pk(r, get, names, cross=False, floor=1e-8):
         else:
             ok = np.isfinite(y)
             assert np.array_equal(ok, np.isfinite(x)), n
-            # floor: the DC bin of Pk2D holds |delta(k=0)|^2, pure float round-off of a
-            # zero-mean field (cross spectra also pass through zero), so the absolute floor is 1e-6 of the
-            # array's largest value
+            if n in ('Pk2D', 'PkX2D'):
+                # the DC bin (k_par = k_per = 0) holds |delta(k=0)|^2, pure float round-off of
+                # a zero-mean field whatever its size: compared on the array's scale
+                big = np.abs(y[ok]).max()
+                assert np.all(np.abs(x[0] - y[0]) <= 1e-4 * big), (n, 'DC', x[0], y[0])
+                ok = ok.copy()
+                ok[0] = False
+            # floor: cross spectra pass through zero, so the absolute floor is 1e-6 of
+            # the array's largest value; floor2d adds floor2d x the median |bin| for 2D
+            # spectra of shot-noise fields (see the batched-realization test)
             atol = 1e-6 * np.abs(y[ok]).max()
+            if floor2d and n in ('Pk2D', 'PkX2D'):
+                atol = max(atol, floor2d * np.median(np.abs(y[ok])))
             err = np.abs(x[ok] - y[ok])
             assert np.all(err <= RTOL * np.abs(y[ok]) + atol), (n, np.max(err / (np.abs(y[ok]) + atol / RTOL)))
 
