@@ -47,6 +47,9 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--strategy', default='auto', choices=['auto', 'atomic', 'tiled', 'sorted'])
+    ap.add_argument('--owned-min-dims', type=int, default=-1,
+                    help='grids from this side up take the owned-cell write-out (profiling the 1024^3 '
+                         'deposit path on a smaller case; default: the library\'s own threshold)')
     return ap.parse_args()
 
 
@@ -248,6 +251,8 @@ def main():
     pb.build()
     from pylians_gb300.pipeline import ParticlePk
     from pylians_gb300 import _lib
+    if a.owned_min_dims > 0:
+        _lib.call('pyl_ma_set_thresholds', a.owned_min_dims, -1.0)
 
     dims, side = a.grid, a.particles_side
     n = side ** 3

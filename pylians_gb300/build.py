@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libpylgpu.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-SOURCES = ['capi.cu', 'mas.cu', 'pk.cu', 'pkbin.cu', 'fft.cu', 'bk.cu', 'batch.cu', 'mlp.cu', 'sorted.cu', 'interp.cu', 'xi.cu', 'plane.cu', 'smooth.cu']
+SOURCES = ['capi.cu', 'mas.cu', 'tiled_ngp.cu', 'tiled_cic.cu', 'tiled_tsc.cu', 'tiled_pcs.cu', 'pk.cu', 'pkbin.cu', 'fft.cu', 'bk.cu', 'batch.cu', 'mlp.cu', 'sorted.cu', 'interp.cu', 'xi.cu', 'plane.cu', 'smooth.cu']
 
 
 def nvcc():

@@ -150,9 +150,19 @@ __device__ __forceinline__ void float_scatter(float *acc, int base, const float 
         }
 }
 
+// Fixed-point value of one corner: the product c01 * c2 as a 10.22 number.  PRE:
+// c2 already carries the factor 2^22 (one FFMA, one rounding of the exact
+// product); otherwise the float product is rounded first, then scaled.
+template <bool PRE>
+__device__ __forceinline__ unsigned fx_corner(float c01, float c2)
+{
+    const float x = PRE ? __fmaf_rn(c01, c2, FX_MAGIC) : __fmaf_rn(__fmul_rn(c01, c2), FX_SCALE, FX_MAGIC);
+    return __float_as_uint(x) - FX_MAGIC_BITS;
+}
+
 // Adds the S^3 fixed-point corner weights without reading the old values back
 // (wraps are then found from the bin's total, see fx_accumulate).
-template <int MAS, int E>
+template <int MAS, int E, bool PRE = false>
 __device__ __forceinline__ void fx_scatter_add(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
 {
     constexpr int S = Support<MAS>::S;
@@ -163,16 +173,14 @@ __device__ __forceinline__ void fx_scatter_add(unsigned *acc, int base, const fl
             const float c01 = __fmul_rn(C[0][l], C[1][m]);
             const int row = base + (l * E + m) * E;
 #pragma unroll
-            for (int q = 0; q < S; q++) {
-                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
-                atomicAdd(acc + row + q, __float_as_uint(x) - FX_MAGIC_BITS);
-            }
+            for (int q = 0; q < S; q++) atomicAdd(acc + row + q, fx_corner<PRE>(c01, C[2][q]));
         }
 }
 
 // COUNT: unweighted NGP adds one integer count per particle; otherwise every
 // corner adds its fixed-point weight (weighted NGP: C holds the scaled weight).
-template <int MAS, int E, bool COUNT = (MAS == PYL_MAS_NGP)>
+// PRE: C[2] carries the factor 2^22 (see fx_corner).
+template <int MAS, int E, bool COUNT = (MAS == PYL_MAS_NGP), bool PRE = false>
 __device__ __forceinline__ unsigned fx_scatter_or(unsigned *acc, int base, const float (*C)[Support<MAS>::S])
 {
     constexpr int S = Support<MAS>::S;
@@ -188,10 +196,7 @@ __device__ __forceinline__ unsigned fx_scatter_or(unsigned *acc, int base, const
             const float c01 = __fmul_rn(C[0][l], C[1][m]);
             const int row = base + (l * E + m) * E;
 #pragma unroll
-            for (int q = 0; q < S; q++) {
-                const float x = __fmaf_rn(__fmul_rn(c01, C[2][q]), FX_SCALE, FX_MAGIC);
-                seen |= atomicAdd(acc + row + q, __float_as_uint(x) - FX_MAGIC_BITS);
-            }
+            for (int q = 0; q < S; q++) seen |= atomicAdd(acc + row + q, fx_corner<PRE>(c01, C[2][q]));
         }
     return seen;
 }
