@@ -464,33 +464,95 @@ def bench_zeldovich(reps=3):
     return out
 
 
-def bench_bispectrum(reps=3):
+def bench_bispectrum(reps=5):
     """Bispectra of a 256^3 CIC overdensity (1000 Mpc/h, 256^3 uniform particles): k1=0.1,
     k2=0.2 h/Mpc with 32 theta bins, plus 20 equilateral triangles k=0.02..0.4 h/Mpc, all 52
-    triangles in one shell fill, one batched C2R and one reduction."""
+    triangles through one BkPlan (one R2C, one shell fill, one batched C2R per field kind,
+    one grouped reduction).  Device time by CUDA events on the launching stream, per stage
+    and for the whole chain; the call time adds the read-back and finalisation.
+
+    Algorithmic bytes (N_g = N^3, N_h = N^2 (N/2+1) on the input grid; M_g, M_h the same on
+    the reduced side M of the shell fields; S shells, T triangles, G (a, b) groups of at
+    most 8 triangles):
+      R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill 2 S x 8 M_h (both fields
+      written); C2R 2 S (8 M_h + 4 M_g); reduction 4 G x 4 M_g + 2 T x 4 M_g."""
+    import ctypes
     import torch
     import pylians_gb300.MAS_library as MASL
     import pylians_gb300.Pk_library as PKL
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr, stream_ptr
     N = 256
     gen = torch.Generator(device='cuda')
     gen.manual_seed(3)
     pos = torch.rand((N ** 3, 3), generator=gen, device='cuda') * BOX
     d = torch.empty((N, N, N), device='cuda')
     MASL.overdensity_device(pos, d, BOX, 'CIC')
+    del pos
     theta = np.linspace(0, np.pi, 32)
     k3 = np.sqrt((0.2 * np.sin(theta)) ** 2 + (0.2 * np.cos(theta) + 0.1) ** 2)
     tris = [(0.1, 0.2, float(x)) for x in k3] + [(float(k), float(k), float(k)) for k in np.linspace(0.02, 0.4, 20)]
-    PKL.Bk_triangles(d, BOX, tris, 'CIC')
+    plan = PKL.BkPlan(N, BOX, tris, 'CIC')
+    plan.run(d)
     torch.cuda.synchronize()
-    ts = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
     for _ in range(reps):
-        t0 = time.perf_counter()
-        PKL.Bk_triangles(d, BOX, tris, 'CIC')
+        plan.run(d)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / reps
+    # stages: the launches of BkPlan.run with events between them (S <= 96: one fill call)
+    st = stream_ptr()
+    S, T, m = len(plan.bounds), len(plan.tri), plan.side
+    se = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    acc = np.zeros(5)
+    for _ in range(reps):
+        se[0].record()
+        _lib.call('pyl_fft_r2c', ptr(d), ptr(plan.dk), N, 1, st)
+        se[1].record()
+        _lib.call('pyl_mas_deconvolve', ptr(plan.dk), None, N, plan.mas_p, st)
+        se[2].record()
+        _lib.call('pyl_bk_shell_fill', ptr(plan.dk), N, m, ctypes.cast(plan._lo[0], ctypes.c_void_p),
+                  ctypes.cast(plan._hi[0], ctypes.c_void_p), S, ptr(plan.cd), ptr(plan.ci), ptr(plan.power), st)
+        se[3].record()
+        _lib.call('pyl_fft_c2r', ptr(plan.cd), ptr(plan.d_real), m, S, st)
+        _lib.call('pyl_fft_c2r', ptr(plan.ci), ptr(plan.i_real), m, S, st)
+        se[4].record()
+        _lib.call('pyl_bk_triangles', ptr(plan.d_real), ptr(plan.i_real), m, plan.stride, S,
+                  ctypes.cast(plan._tri, ctypes.c_void_p), T, ptr(plan.num), ptr(plan.den), st)
+        se[5].record()
         torch.cuda.synchronize()
-        ts.append(time.perf_counter() - t0)
-    t = float(np.median(ts))
-    return dict(metric='bispectra/s', value=len(tris) / t, triangles=len(tris), ms_per_call=t * 1e3,
-                workload='Bk 256^3 CIC, 32-theta sweep + 20 equilateral', timing='host wall incl. sync')
+        acc += [se[k].elapsed_time(se[k + 1]) for k in range(5)]
+    acc /= reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plan.run(d)
+        plan.result()
+    t_call = (time.perf_counter() - t0) / reps * 1e3
+    Ng, Nh = N ** 3, N * N * (N // 2 + 1)
+    Mg, Mh = m ** 3, m * m * (m // 2 + 1)
+    pairs = {}
+    for a, b, _ in plan.tri:
+        pairs[(int(a), int(b))] = pairs.get((int(a), int(b)), 0) + 1
+    G = sum(-(-c // 8) for c in pairs.values())
+    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=2 * S * 8.0 * Mh,
+               fft_c2r=2 * S * (8.0 * Mh + 4.0 * Mg), triangles=4 * G * 4.0 * Mg + 2 * T * 4.0 * Mg)
+    names = ['fft_r2c', 'deconvolve', 'shell_fill', 'fft_c2r', 'triangles']
+    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
+        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    stages = {nm: dict(ms=float(acc[k]), gbs=alg[nm] / (acc[k] / 1e3) / 1e9,
+                       frac=alg[nm] / (acc[k] / 1e3) / 1e9 / hbm) for k, nm in enumerate(names)}
+    del plan, d
+    torch.cuda.empty_cache()
+    return dict(metric='bispectra/s', value=len(tris) / (ms / 1e3), triangles=len(tris), shells=S, groups=G,
+                reduced_side=m, ms_per_call_device=ms, ms_per_call_host=t_call,
+                value_host=len(tris) / (t_call / 1e3), stages=stages,
+                roofline=dict(kernel='triangles', bound='hbm', achieved=stages['triangles']['gbs'], peak=hbm,
+                              unit='GB/s', frac=stages['triangles']['frac']),
+                workload='Bk 256^3 CIC, 32-theta sweep + 20 equilateral',
+                timing='device: CUDA events around BkPlan.run; host: run + read-back + finalisation')
 
 
 def bench_batch(count, steps=3):

@@ -241,21 +241,28 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  * Replaces Bk (library/Pk_library/bispectrum_library.pyx:32-196).
  * Shell s holds the modes with host_k2_lo[s] <= kx^2+ky^2+kz^2 < host_k2_hi[s]
  * (the integer form of  k_min <= |k| < k_max  in units of kF, :73-77,116-118).
- * pyl_bk_shell_fill reads the deconvolved half-complex field once and writes,
- * for each shell, delta_s (complex64) and the indicator I_s (1+0i) half grids at
- * out_delta + s*half, out_ind + s*half (half = dims*dims*(dims/2+1)), and
- * power[2*s] = sum_x delta_s(x)^2 / dims^3, power[2*s+1] = sum_x I_s(x)^2 / dims^3
- * (float64, via Parseval on the Hermitian half grid; zeroed by the call).
- * At most PYL_BK_MAX_SHELLS shells per call.
+ * pyl_bk_shell_fill reads the deconvolved half-complex dims^3 field and writes,
+ * for each shell, delta_s (complex64) and the indicator I_s (1+0i) as half grids
+ * of side out_dims at out_delta + s*half, out_ind + s*half (half =
+ * out_dims*out_dims*(out_dims/2+1), mode (kx, ky, kz) at (kx mod out_dims,
+ * ky mod out_dims, kz)), and power[2*s] = sum_x delta_s(x)^2 / dims^3,
+ * power[2*s+1] = sum_x I_s(x)^2 / dims^3 on the dims^3 grid (float64, via
+ * Parseval on the Hermitian half grid; zeroed by the call).  out_dims is dims,
+ * or any side above 3 K with K the largest wave number of the call's shells:
+ * the shell fields are band-limited, so the triple-product sums over out_dims^3
+ * cells are (out_dims/dims)^3 times those over dims^3 cells and B, a ratio of
+ * two such sums, is the same.  At most PYL_BK_MAX_SHELLS shells per call.
  *
  * pyl_bk_triangles reduces the C2R'd real fields: for triangle t with shells
  * (a,b,c) = host_tri[3t..3t+2], num[t] = sum_x d_a d_b d_c and
- * den[t] = sum_x I_a I_b I_c (float64, zeroed by the call) over dims^3 cells;
- * d_fields / i_fields are float32, shell s at offset s*field_stride elements
- * (field_stride >= dims^3, a multiple of 4; buffers 16-byte aligned).
+ * den[t] = sum_x I_a I_b I_c (float64, zeroed by the call) over dims^3 cells
+ * (the grid the fields live on); triangles sharing (a, b) are reduced together,
+ * reading d_a d_b and I_a I_b once.  d_fields / i_fields are float32, shell s at
+ * offset s*field_stride elements (field_stride >= dims^3, a multiple of 4;
+ * buffers 16-byte aligned).
  */
 #define PYL_BK_MAX_SHELLS 96
-int pyl_bk_shell_fill(const void *dk, int dims, const int64_t *host_k2_lo,
+int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const int64_t *host_k2_lo,
                       const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
                       double *power, void *stream);
 int pyl_bk_triangles(const float *d_fields, const float *i_fields, int dims, int64_t field_stride,

@@ -435,79 +435,144 @@ def shell_k2_bounds(k_min, k_max):
     return first_at_least(k_min), first_at_least(k_max)
 
 
-def _bk_fields(dk, dims, bounds):
-    """Shell fill + C2R for a list of shells; returns real delta_s, I_s fields and
-    the Parseval sums (sum_x delta_s^2 / N^3, sum_x I_s^2 / N^3)."""
-    S = len(bounds)
-    dev = dk.device
-    half = dims * dims * (dims // 2 + 1)
-    cells = dims ** 3
-    stride = (cells + 3) // 4 * 4
-    d_real = torch.empty(S * stride, dtype=torch.float32, device=dev)
-    i_real = torch.empty(S * stride, dtype=torch.float32, device=dev)
-    power = torch.empty(2 * S, dtype=torch.float64, device=dev)
-    import ctypes
-    maxs = 96
-    for s0 in range(0, S, maxs):
-        ns = min(maxs, S - s0)
-        lo = (ctypes.c_int64 * ns)(*[b[0] for b in bounds[s0:s0 + ns]])
-        hi = (ctypes.c_int64 * ns)(*[b[1] for b in bounds[s0:s0 + ns]])
-        cd = torch.empty((ns, half), dtype=torch.complex64, device=dev)
-        ci = torch.empty((ns, half), dtype=torch.complex64, device=dev)
-        pw = torch.empty(2 * ns, dtype=torch.float64, device=dev)
-        _lib.call('pyl_bk_shell_fill', ptr(dk), dims, ctypes.cast(lo, ctypes.c_void_p),
-                  ctypes.cast(hi, ctypes.c_void_p), ns, ptr(cd), ptr(ci), ptr(pw), stream_ptr())
-        power[2 * s0:2 * (s0 + ns)] = pw
-        if stride == cells:
-            _lib.call('pyl_fft_c2r', ptr(cd), ptr(d_real[s0 * stride:]), dims, ns, stream_ptr())
-            _lib.call('pyl_fft_c2r', ptr(ci), ptr(i_real[s0 * stride:]), dims, ns, stream_ptr())
+def _fast_side(m):
+    """Smallest even side >= m whose prime factors are 2, 3, 5 and 7 (fast cuFFT sizes)."""
+    m = max(2, int(m))
+    while True:
+        if m % 2 == 0:
+            r = m
+            for p in (2, 3, 5, 7):
+                while r % p == 0:
+                    r //= p
+            if r == 1:
+                return m
+        m += 1
+
+
+def bk_side(dims, bounds):
+    """Side M of the grid the shell fields are transformed and reduced on: the smallest
+    fast side above 3 K (K the largest wave number of any shell: k^2 < max hi), or dims
+    when that is not smaller.  The shell fields are band-limited, so their triple-product
+    sums over M^3 cells are (M/dims)^3 those over dims^3 cells (pyl_bk_shell_fill)."""
+    hi = max(b[1] for b in bounds)
+    K = 0
+    while (K + 1) ** 2 < hi:
+        K += 1
+    m = _fast_side(3 * K + 1)
+    return m if m < dims else dims
+
+
+class BkPlan(object):
+    """Bispectra of a fixed triangle set (k1, k2, k3 in h/Mpc) on dims^3 fields: shells,
+    their exact integer bounds, the reduced grid side, triangle index lists and every
+    device buffer are set up once; run(delta) enqueues the whole chain on one stream
+    (R2C, MAS deconvolution, shell fill, batched C2R of the shell fields, grouped
+    triple-product sums) with no host synchronisation, so capture() can record it as a
+    CUDA graph; result() reads the sums back and finalises B, Q and the shell powers
+    (bispectrum_library.pyx:132-190)."""
+
+    MAX_SHELLS = 96
+
+    def __init__(self, dims, BoxSize, triangles, MAS='CIC', device=None, side=None):
+        require_cuda()
+        import ctypes
+        self.dims, self.BoxSize, self.MAS = int(dims), float(BoxSize), MAS
+        self.device = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
+        kF = frequencies(BoxSize, dims)[0]
+        keys, index, tri_idx = [], {}, []
+        for (a, b, c) in triangles:
+            ids = []
+            for k in (a, b, c):
+                kmin, kmax = (k - kF) / kF, (k + kF) / kF       # bispectrum_library.pyx:73-77
+                if (kmin, kmax) not in index:
+                    index[(kmin, kmax)] = len(keys)
+                    keys.append((kmin, kmax))
+                ids.append(index[(kmin, kmax)])
+            tri_idx.append(ids)
+        self.tri = np.asarray(tri_idx, dtype=np.int64)
+        self.bounds = [shell_k2_bounds(lo, hi) for lo, hi in keys]
+        S, T = len(self.bounds), len(tri_idx)
+        # side: the reduced grid (bk_side) unless the caller asks for another valid one
+        self.side = int(side) if side else bk_side(self.dims, self.bounds)
+        m = self.side
+        self.half = m * m * (m // 2 + 1)
+        self.cells = m ** 3
+        self.stride = (self.cells + 3) // 4 * 4
+        dev = self.device
+        self.dk = torch.empty(_half_shape(self.dims), dtype=torch.complex64, device=dev)
+        self.cd = torch.empty((S, self.half), dtype=torch.complex64, device=dev)
+        self.ci = torch.empty((S, self.half), dtype=torch.complex64, device=dev)
+        self.d_real = torch.empty(S * self.stride, dtype=torch.float32, device=dev)
+        self.i_real = torch.empty(S * self.stride, dtype=torch.float32, device=dev)
+        self.power = torch.empty(2 * S, dtype=torch.float64, device=dev)
+        self.num = torch.empty(T, dtype=torch.float64, device=dev)
+        self.den = torch.empty(T, dtype=torch.float64, device=dev)
+        ch = range(0, S, self.MAX_SHELLS)
+        self._lo = [(ctypes.c_int64 * min(self.MAX_SHELLS, S - s0))(*[b[0] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
+                    for s0 in ch]
+        self._hi = [(ctypes.c_int64 * min(self.MAX_SHELLS, S - s0))(*[b[1] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
+                    for s0 in ch]
+        self._tri = (ctypes.c_int * (3 * T))(*[int(i) for t in tri_idx for i in t])
+        self.mas_p = MAS_function(MAS)
+        self.graph = None
+
+    def run(self, delta, stream=None):
+        """Enqueue the chain on `delta` (a dims^3 float32 grid); nothing waits on the host."""
+        import ctypes
+        x = as_device_f32(delta, 'delta')
+        if tuple(x.shape) != (self.dims,) * 3:
+            raise ValueError('delta must be a %d^3 grid' % self.dims)
+        self._x = x
+        st = stream_ptr(stream)
+        d, m, S = self.dims, self.side, len(self.bounds)
+        _lib.call('pyl_fft_r2c', ptr(x), ptr(self.dk), d, 1, st)
+        _lib.call('pyl_mas_deconvolve', ptr(self.dk), None, d, self.mas_p, st)
+        for j, s0 in enumerate(range(0, S, self.MAX_SHELLS)):
+            ns = min(self.MAX_SHELLS, S - s0)
+            _lib.call('pyl_bk_shell_fill', ptr(self.dk), d, m, ctypes.cast(self._lo[j], ctypes.c_void_p),
+                      ctypes.cast(self._hi[j], ctypes.c_void_p), ns, ptr(self.cd[s0]), ptr(self.ci[s0]),
+                      ptr(self.power[2 * s0:]), st)
+        if self.stride == self.cells:
+            _lib.call('pyl_fft_c2r', ptr(self.cd), ptr(self.d_real), m, S, st)
+            _lib.call('pyl_fft_c2r', ptr(self.ci), ptr(self.i_real), m, S, st)
         else:
-            for j in range(ns):
-                o = (s0 + j) * stride
-                _lib.call('pyl_fft_c2r', ptr(cd[j]), ptr(d_real[o:]), dims, 1, stream_ptr())
-                _lib.call('pyl_fft_c2r', ptr(ci[j]), ptr(i_real[o:]), dims, 1, stream_ptr())
-        del cd, ci
-    return d_real, i_real, power, stride
+            for s in range(S):
+                _lib.call('pyl_fft_c2r', ptr(self.cd[s]), ptr(self.d_real[s * self.stride:]), m, 1, st)
+                _lib.call('pyl_fft_c2r', ptr(self.ci[s]), ptr(self.i_real[s * self.stride:]), m, 1, st)
+        _lib.call('pyl_bk_triangles', ptr(self.d_real), ptr(self.i_real), m, self.stride, S,
+                  ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), ptr(self.num), ptr(self.den), st)
+
+    def capture(self, delta):
+        """Record run(delta) (fixed address) as a CUDA graph; replay() relaunches it."""
+        self.run(delta)             # warm-up: plans, function attributes
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(delta)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def result(self):
+        """(B, Q, Pk1, Pk2, Pk3) per triangle, in float64 on the host."""
+        L, d = self.BoxSize, self.dims
+        pw = self.power.cpu().numpy()
+        P = (pw[0::2] / pw[1::2]) * (L / d ** 2) ** 3
+        B = (self.num.cpu().numpy() / self.den.cpu().numpy()) * (L ** 2 / d ** 3) ** 3
+        t = self.tri
+        P1, P2, P3 = P[t[:, 0]], P[t[:, 1]], P[t[:, 2]]
+        Q = B / (P1 * P2 + P1 * P3 + P2 * P3)
+        return B, Q, P1, P2, P3
 
 
 def Bk_triangles(delta, BoxSize, triangles, MAS='CIC', threads=1):
     """Bispectra of many triangles (k1, k2, k3) in h/Mpc sharing one FFT, one shell
-    fill, one batched C2R and one reduction launch.  Returns (B, Q, Pk1, Pk2, Pk3)."""
-    require_cuda()
-    import ctypes
-    dims = delta.shape[0]
-    kF = frequencies(BoxSize, dims)[0]
-    dev = torch.device('cuda', torch.cuda.current_device())
-    x = as_device_f32(delta, 'delta')
-    dk = torch.empty(_half_shape(dims), dtype=torch.complex64, device=dev)
-    _lib.call('pyl_fft_r2c', ptr(x), ptr(dk), dims, 1, stream_ptr())
-    _lib.call('pyl_mas_deconvolve', ptr(dk), None, dims, MAS_function(MAS), stream_ptr())
-    keys, index = [], {}
-    tri_idx = []
-    for (a, b, c) in triangles:
-        ids = []
-        for k in (a, b, c):
-            kmin, kmax = (k - kF) / kF, (k + kF) / kF       # bispectrum_library.pyx:73-77
-            if (kmin, kmax) not in index:
-                index[(kmin, kmax)] = len(keys)
-                keys.append((kmin, kmax))
-            ids.append(index[(kmin, kmax)])
-        tri_idx.append(ids)
-    bounds = [shell_k2_bounds(lo, hi) for lo, hi in keys]
-    d_real, i_real, power, stride = _bk_fields(dk, dims, bounds)
-    T = len(tri_idx)
-    flat = (ctypes.c_int * (3 * T))(*[i for t in tri_idx for i in t])
-    num = torch.empty(T, dtype=torch.float64, device=dev)
-    den = torch.empty(T, dtype=torch.float64, device=dev)
-    _lib.call('pyl_bk_triangles', ptr(d_real), ptr(i_real), dims, stride, len(keys),
-              ctypes.cast(flat, ctypes.c_void_p), T, ptr(num), ptr(den), stream_ptr())
-    pw = power.cpu().numpy()
-    P = (pw[0::2] / pw[1::2]) * (BoxSize / dims ** 2) ** 3
-    B = (num.cpu().numpy() / den.cpu().numpy()) * (BoxSize ** 2 / dims ** 3) ** 3
-    t = np.asarray(tri_idx)
-    P1, P2, P3 = P[t[:, 0]], P[t[:, 1]], P[t[:, 2]]
-    Q = B / (P1 * P2 + P1 * P3 + P2 * P3)
-    return B, Q, P1, P2, P3
+    fill, one batched C2R and one reduction pass.  Returns (B, Q, Pk1, Pk2, Pk3)."""
+    plan = BkPlan(delta.shape[0], BoxSize, triangles, MAS)
+    plan.run(delta)
+    return plan.result()
 
 
 class Bk(object):

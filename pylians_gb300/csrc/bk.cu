@@ -10,7 +10,21 @@
 // the reference's float64 bounds into exact integer bounds.  sum_x delta_s(x)^2
 // and sum_x I_s(x)^2 come from Parseval on the half grid (modes with
 // 0 < kz < N/2 stand for two), so only the triple products need real space.
+//
+// Band-limited evaluation: every mode of a call's shells has |k_a| <= K < N/2 on
+// each axis, so the product of three shell fields has no wave number beyond 3K per
+// axis, and sum_x d_a d_b d_c over an M^3 grid with M > 3K equals (M/N)^3 times
+// the sum over the N^3 grid (a sum over x keeps the k_a + k_b + k_c = 0 terms, and
+// with |k_a + k_b + k_c| <= 3K < M no other sum of three modes aliases to zero).
+// B and P are ratios of such sums, so the shells are written into M^3 half grids
+// (the caller picks M), transformed there and reduced there: (M/N)^3 of the C2R
+// and reduction work.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -22,33 +36,43 @@ struct ShellBounds {
     int n;
 };
 
-__global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restrict__ dk, int dims,
+// One thread per stored mode of the N grid with |kx|, |ky|, kz <= K (no shell
+// reaches past K): kx, ky in [klo, khi] = [-min(K, (N-1)/2), min(K, N/2)], the
+// grid's own signed frequencies, each stored mode once.  The mode's value and
+// indicator go to slot (kx mod M, ky mod M, kz) of every shell that holds it; the
+// Parseval sums use the N grid's weights (1 on the kz = 0 and kz = N/2 planes, 2
+// elsewhere).
+__global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restrict__ dk, int dims, int K, int M,
                                                          ShellBounds sb, float2 *__restrict__ od,
                                                          float2 *__restrict__ oi, double *power)
 {
     __shared__ double acc[2 * PYL_BK_MAX_SHELLS];
     for (int i = threadIdx.x; i < 2 * sb.n; i += blockDim.x) acc[i] = 0.0;
     __syncthreads();
-    const int nz = dims / 2 + 1;
-    const long long half = (long long)dims * dims * nz;
+    const int nz = dims / 2 + 1, mz = M / 2 + 1;
+    const int klo = -min(K, (dims - 1) / 2), khi = min(K, dims / 2), kzhi = min(K, dims / 2);
+    const int side = khi - klo + 1;
+    const long long cube = (long long)side * side * (kzhi + 1);
+    const long long half_m = (long long)M * M * mz;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const bool even = (dims & 1) == 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < half; i += stride) {
-        const int kz = (int)(i % nz);
-        const long long rr = i / nz;
-        const int ky = freq_of((int)(rr % dims), dims), kx = freq_of((int)(rr / dims), dims);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cube; i += stride) {
+        const int kz = (int)(i % (kzhi + 1));
+        const long long rr = i / (kzhi + 1);
+        const int ky = (int)(rr % side) + klo, kx = (int)(rr / side) + klo;
         const long long n2 = (long long)kx * kx + (long long)ky * ky + (long long)kz * kz;
-        // skip quickly when outside every shell
         bool any = false;
         for (int s = 0; s < sb.n; s++) any |= (n2 >= sb.lo[s]) & (n2 < sb.hi[s]);
         if (!any) continue;
-        const float2 v = __ldg(dk + i);
+        const long long src = ((long long)(kx < 0 ? kx + dims : kx) * dims + (ky < 0 ? ky + dims : ky)) * nz + kz;
+        const long long dst = ((long long)(kx < 0 ? kx + M : kx) * M + (ky < 0 ? ky + M : ky)) * mz + kz;
+        const float2 v = __ldg(dk + src);
         const double w = (kz == 0 || (even && kz == dims / 2)) ? 1.0 : 2.0;
         const double p2 = w * ((double)v.x * v.x + (double)v.y * v.y);
         for (int s = 0; s < sb.n; s++) {
             if (n2 >= sb.lo[s] && n2 < sb.hi[s]) {
-                od[s * half + i] = v;
-                oi[s * half + i] = make_float2(1.0f, 0.0f);
+                od[s * half_m + dst] = v;
+                oi[s * half_m + dst] = make_float2(1.0f, 0.0f);
                 atomicAdd(acc + 2 * s, p2);
                 atomicAdd(acc + 2 * s + 1, w);
             }
@@ -59,55 +83,98 @@ __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restric
         if (acc[i] != 0.0) atomicAdd(power + i, acc[i]);
 }
 
-struct TriList {
-    int a[PYL_BK_MAX_SHELLS], b[PYL_BK_MAX_SHELLS], c[PYL_BK_MAX_SHELLS];
+// Triangles grouped by their first two shells: a group reads d_a d_b and I_a I_b
+// once per cell and the third shell of each of its (up to GC) triangles.
+constexpr int GC = 8;
+constexpr int MAX_GROUPS = 64;
+
+struct TriGroups {
+    int a[MAX_GROUPS], b[MAX_GROUPS], n[MAX_GROUPS];
+    int c[MAX_GROUPS][GC], t[MAX_GROUPS][GC];
 };
 
-// blockIdx.y = triangle within this launch; float32 partial sums over 32 cells,
-// float64 above that.
-__global__ void __launch_bounds__(256) triangle_kernel(const float *__restrict__ d, const float *__restrict__ I,
-                                                       long long cells, long long fs, TriList tl, int tri0,
-                                                       double *num, double *den)
+// blockIdx.y = group; float32 partial sums over 8 float4 steps, float64 above.
+// Products (d_a d_b) d_c, as the reference forms d12 * d3 (:183-186).
+template <int NC>
+__device__ __forceinline__ void tri_group(const float *__restrict__ d, const float *__restrict__ I, long long cells,
+                                          long long fs, const TriGroups &tg, int gi, double *num, double *den)
 {
-    const int t = blockIdx.y;
-    const float4 *da = (const float4 *)(d + tl.a[t] * fs);
-    const float4 *db = (const float4 *)(d + tl.b[t] * fs);
-    const float4 *dc = (const float4 *)(d + tl.c[t] * fs);
-    const float4 *ia = (const float4 *)(I + tl.a[t] * fs);
-    const float4 *ib = (const float4 *)(I + tl.b[t] * fs);
-    const float4 *ic = (const float4 *)(I + tl.c[t] * fs);
+    const float4 *da = (const float4 *)(d + tg.a[gi] * fs), *db = (const float4 *)(d + tg.b[gi] * fs);
+    const float4 *ia = (const float4 *)(I + tg.a[gi] * fs), *ib = (const float4 *)(I + tg.b[gi] * fs);
+    const float4 *dc[NC], *ic[NC];
+#pragma unroll
+    for (int j = 0; j < NC; j++) {
+        dc[j] = (const float4 *)(d + tg.c[gi][j] * fs);
+        ic[j] = (const float4 *)(I + tg.c[gi][j] * fs);
+    }
     const long long n4 = cells / 4;
-    double sn = 0.0, sd = 0.0;
-    float fn = 0.0f, fd = 0.0f;
+    double sn[NC], sd[NC];
+    float fn[NC], fd[NC];
+#pragma unroll
+    for (int j = 0; j < NC; j++) { sn[j] = sd[j] = 0.0; fn[j] = fd[j] = 0.0f; }
     int k = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
-        const float4 x = __ldg(da + i), y = __ldg(db + i), z = __ldg(dc + i);
-        const float4 p = __ldg(ia + i), q = __ldg(ib + i), r = __ldg(ic + i);
-        fn += (x.x * y.x) * z.x + (x.y * y.y) * z.y + (x.z * y.z) * z.z + (x.w * y.w) * z.w;
-        fd += (p.x * q.x) * r.x + (p.y * q.y) * r.y + (p.z * q.z) * r.z + (p.w * q.w) * r.w;
-        if (++k == 8) { sn += fn; sd += fd; fn = fd = 0.0f; k = 0; }
+        const float4 x = __ldg(da + i), y = __ldg(db + i), p = __ldg(ia + i), q = __ldg(ib + i);
+        const float4 xy = make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w);
+        const float4 pq = make_float4(p.x * q.x, p.y * q.y, p.z * q.z, p.w * q.w);
+#pragma unroll
+        for (int j = 0; j < NC; j++) {
+            const float4 z = __ldg(dc[j] + i), r = __ldg(ic[j] + i);
+            fn[j] += xy.x * z.x + xy.y * z.y + xy.z * z.z + xy.w * z.w;
+            fd[j] += pq.x * r.x + pq.y * r.y + pq.z * r.z + pq.w * r.w;
+        }
+        if (++k == 8) {
+#pragma unroll
+            for (int j = 0; j < NC; j++) { sn[j] += fn[j]; sd[j] += fd[j]; fn[j] = fd[j] = 0.0f; }
+            k = 0;
+        }
     }
-    sn += fn; sd += fd;
+#pragma unroll
+    for (int j = 0; j < NC; j++) { sn[j] += fn[j]; sd[j] += fd[j]; }
     if (blockIdx.x == 0 && threadIdx.x < (cells & 3)) {   // tail cells (cells % 4)
-        const long long j = n4 * 4 + threadIdx.x;
-        const float *a0 = d + tl.a[t] * fs, *b0 = d + tl.b[t] * fs, *c0 = d + tl.c[t] * fs;
-        const float *a1 = I + tl.a[t] * fs, *b1 = I + tl.b[t] * fs, *c1 = I + tl.c[t] * fs;
-        sn += (a0[j] * b0[j]) * c0[j];
-        sd += (a1[j] * b1[j]) * c1[j];
+        const long long i = n4 * 4 + threadIdx.x;
+        const float *a0 = d + tg.a[gi] * fs, *b0 = d + tg.b[gi] * fs;
+        const float *a1 = I + tg.a[gi] * fs, *b1 = I + tg.b[gi] * fs;
+#pragma unroll
+        for (int j = 0; j < NC; j++) {
+            sn[j] += (a0[i] * b0[i]) * d[tg.c[gi][j] * fs + i];
+            sd[j] += (a1[i] * b1[i]) * I[tg.c[gi][j] * fs + i];
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        sn += __shfl_down_sync(0xffffffffu, sn, o);
-        sd += __shfl_down_sync(0xffffffffu, sd, o);
+    __shared__ double wsn[8][GC], wsd[8][GC];
+#pragma unroll
+    for (int j = 0; j < NC; j++) {
+        double a = sn[j], b = sd[j];
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if ((threadIdx.x & 31) == 0) { wsn[threadIdx.x >> 5][j] = a; wsd[threadIdx.x >> 5][j] = b; }
     }
-    __shared__ double wsn[8], wsd[8];
-    if ((threadIdx.x & 31) == 0) { wsn[threadIdx.x >> 5] = sn; wsd[threadIdx.x >> 5] = sd; }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < NC) {
         double a = 0.0, b = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += wsn[w]; b += wsd[w]; }
-        atomicAdd(num + tri0 + t, a);
-        atomicAdd(den + tri0 + t, b);
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += wsn[w][threadIdx.x]; b += wsd[w][threadIdx.x]; }
+        atomicAdd(num + tg.t[gi][threadIdx.x], a);
+        atomicAdd(den + tg.t[gi][threadIdx.x], b);
+    }
+}
+
+__global__ void __launch_bounds__(256) triangle_group_kernel(const float *__restrict__ d, const float *__restrict__ I,
+                                                             long long cells, long long fs, TriGroups tg,
+                                                             double *num, double *den)
+{
+    const int gi = blockIdx.y;
+    switch (tg.n[gi]) {     // the third-shell count of a group is uniform over its CTAs
+        case 1: tri_group<1>(d, I, cells, fs, tg, gi, num, den); break;
+        case 2: tri_group<2>(d, I, cells, fs, tg, gi, num, den); break;
+        case 3: tri_group<3>(d, I, cells, fs, tg, gi, num, den); break;
+        case 4: tri_group<4>(d, I, cells, fs, tg, gi, num, den); break;
+        case 5: tri_group<5>(d, I, cells, fs, tg, gi, num, den); break;
+        case 6: tri_group<6>(d, I, cells, fs, tg, gi, num, den); break;
+        case 7: tri_group<7>(d, I, cells, fs, tg, gi, num, den); break;
+        default: tri_group<8>(d, I, cells, fs, tg, gi, num, den); break;
     }
 }
 
@@ -116,25 +183,38 @@ __global__ void __launch_bounds__(256) triangle_kernel(const float *__restrict__
 
 using namespace pyl;
 
-extern "C" int pyl_bk_shell_fill(const void *dk, int dims, const int64_t *host_k2_lo,
-                                 const int64_t *host_k2_hi, int n_shells, void *out_delta,
-                                 void *out_ind, double *power, void *stream)
+extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const int64_t *host_k2_lo,
+                                 const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
+                                 double *power, void *stream)
 {
     PYL_CHECK_ARG(dk && out_delta && out_ind && power && host_k2_lo && host_k2_hi, "null pointer");
     PYL_CHECK_ARG(dims >= 2 && dims <= 4096, "dims out of range");
     PYL_CHECK_ARG(n_shells >= 1 && n_shells <= PYL_BK_MAX_SHELLS, "1..96 shells per call");
     ShellBounds sb;
     sb.n = n_shells;
-    for (int s = 0; s < n_shells; s++) { sb.lo[s] = host_k2_lo[s]; sb.hi[s] = host_k2_hi[s]; }
-    const long long half = (long long)dims * dims * (dims / 2 + 1);
+    long long hi_max = 0;
+    for (int s = 0; s < n_shells; s++) {
+        PYL_CHECK_ARG(host_k2_lo[s] >= 0 && host_k2_hi[s] >= host_k2_lo[s], "bad shell bounds");
+        sb.lo[s] = host_k2_lo[s];
+        sb.hi[s] = host_k2_hi[s];
+        hi_max = std::max(hi_max, (long long)host_k2_hi[s]);
+    }
+    // K: the largest |k| component of any shell mode (k^2 < hi_max)
+    int K = 0;
+    while ((long long)(K + 1) * (K + 1) < hi_max) K++;
+    PYL_CHECK_ARG(out_dims == dims || (2 * K < out_dims && 3 * K < out_dims && out_dims <= dims),
+                  "out_dims must equal dims, or exceed 3 K (and 2 K) with K the largest shell wave number");
+    const long long half_m = (long long)out_dims * out_dims * (out_dims / 2 + 1);
     cudaStream_t st = (cudaStream_t)stream;
-    PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half * n_shells, st));
-    PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half * n_shells, st));
+    PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half_m * n_shells, st));
+    PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half_m * n_shells, st));
     PYL_CUDA(cudaMemsetAsync(power, 0, sizeof(double) * 2 * n_shells, st));
-    long long blocks = (half + 255) / 256;
+    const long long side = std::min(K, dims / 2) + std::min(K, (dims - 1) / 2) + 1;
+    const long long cube = side * side * (std::min(K, dims / 2) + 1);
+    long long blocks = (cube + 255) / 256;
     if (blocks > (long long)num_sms() * 8) blocks = (long long)num_sms() * 8;
-    shell_fill_kernel<<<(unsigned)blocks, 256, 0, st>>>((const float2 *)dk, dims, sb, (float2 *)out_delta,
-                                                        (float2 *)out_ind, power);
+    shell_fill_kernel<<<(unsigned)std::max(1LL, blocks), 256, 0, st>>>((const float2 *)dk, dims, K, out_dims, sb,
+                                                                      (float2 *)out_delta, (float2 *)out_ind, power);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
@@ -155,22 +235,35 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
     cudaStream_t st = (cudaStream_t)stream;
     PYL_CUDA(cudaMemsetAsync(num, 0, sizeof(double) * n_tri, st));
     PYL_CUDA(cudaMemsetAsync(den, 0, sizeof(double) * n_tri, st));
-    long long bx = (cells / 4 + 255) / 256;
-    const long long cap = (long long)num_sms() * 4;
-    for (int t0 = 0; t0 < n_tri; t0 += PYL_BK_MAX_SHELLS) {
-        const int nt = n_tri - t0 < PYL_BK_MAX_SHELLS ? n_tri - t0 : PYL_BK_MAX_SHELLS;
-        TriList tl;
-        for (int t = 0; t < nt; t++) {
-            tl.a[t] = host_tri[3 * (t0 + t)];
-            tl.b[t] = host_tri[3 * (t0 + t) + 1];
-            tl.c[t] = host_tri[3 * (t0 + t) + 2];
+    // groups: triangles of equal (a, b), at most GC each
+    std::map<std::pair<int, int>, std::vector<int>> by_ab;
+    for (int t = 0; t < n_tri; t++) by_ab[std::make_pair(host_tri[3 * t], host_tri[3 * t + 1])].push_back(t);
+    std::vector<std::pair<std::pair<int, int>, std::vector<int>>> groups;
+    for (auto &kv : by_ab)
+        for (size_t i = 0; i < kv.second.size(); i += GC)
+            groups.emplace_back(kv.first, std::vector<int>(kv.second.begin() + i,
+                                                           kv.second.begin() + std::min(kv.second.size(), i + GC)));
+    const long long bx = (cells / 4 + 255) / 256;
+    for (size_t g0 = 0; g0 < groups.size(); g0 += MAX_GROUPS) {
+        const int ng = (int)std::min(groups.size() - g0, (size_t)MAX_GROUPS);
+        TriGroups tg;
+        for (int g = 0; g < ng; g++) {
+            const auto &gr = groups[g0 + g];
+            tg.a[g] = gr.first.first;
+            tg.b[g] = gr.first.second;
+            tg.n[g] = (int)gr.second.size();
+            for (int j = 0; j < GC; j++) {
+                const int t = gr.second[std::min(j, tg.n[g] - 1)];
+                tg.c[g][j] = host_tri[3 * t + 2];
+                tg.t[g][j] = t;
+            }
         }
-        long long b = bx;
-        const long long per_tri_cap = cap / nt > 8 ? cap / nt : 8;
-        if (b > per_tri_cap) b = per_tri_cap;
+        // about four resident CTAs per SM over all groups of the launch
+        long long b = std::max(8LL, (long long)num_sms() * 4 / ng);
+        if (b > bx) b = bx;
         if (b < 1) b = 1;
-        dim3 grid((unsigned)b, (unsigned)nt);
-        triangle_kernel<<<grid, 256, 0, st>>>(d_fields, i_fields, cells, field_stride, tl, t0, num, den);
+        triangle_group_kernel<<<dim3((unsigned)b, (unsigned)ng), 256, 0, st>>>(d_fields, i_fields, cells, field_stride,
+                                                                              tg, num, den);
         PYL_LAUNCH_CHECK();
     }
     return PYL_OK;

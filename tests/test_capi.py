@@ -79,7 +79,12 @@ def test_pk_rejects_bad_arguments(lib):
 def test_bk_rejects_bad_arguments(lib):
     buf = ctypes.c_void_p(16)
     lo = (ctypes.c_int64 * 1)(1)
-    assert lib.pyl_bk_shell_fill(buf, 32, lo, lo, 0, buf, buf, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(buf, 32, 32, lo, lo, 0, buf, buf, buf, None) == 1
+    # a reduced side must exceed 3 K (here K = 9 for k^2 < 90): 27 is too small
+    hi = (ctypes.c_int64 * 1)(90)
+    assert lib.pyl_bk_shell_fill(buf, 64, 27, lo, hi, 1, buf, buf, buf, None) == 1
+    assert 'out_dims' in lib.pyl_last_error().decode()
+    assert lib.pyl_bk_shell_fill(buf, 64, 80, lo, hi, 1, buf, buf, buf, None) == 1
     tri = (ctypes.c_int * 3)(0, 0, 5)
     assert lib.pyl_bk_triangles(buf, buf, 16, 4096, 2, tri, 1, buf, buf, None) == 1
 

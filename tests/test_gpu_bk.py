@@ -9,6 +9,7 @@ import os
 
 import numpy as np
 import pytest
+import torch
 
 from conftest import GOLDEN
 import oracle as O
@@ -72,3 +73,44 @@ def test_bk_triangles_batch_equals_single_calls(PKL, bk):
         # k3 of the equilateral triangle rounds to k within 1 ulp: same shell
         assert abs(B[j] - o.B[0]) <= 1e-3 * abs(o.B[0]) + 1e-3 * np.abs(B).max()
         assert abs(P1[j] - o.Pk[0]) <= 1e-4 * o.Pk[0]
+
+
+def test_reduced_side_equals_full_grid(PKL):
+    """The shell fields are band-limited: reduced on the M^3 grid the plan picks (M > 3K)
+    they give the same B as on the full grid (float32 sums over fewer cells: within
+    1e-5 of the largest |B|) and the same shell powers (Parseval on the input grid)."""
+    rng = np.random.default_rng(17)
+    N, L = 96, 1000.0
+    d = rng.standard_normal((N, N, N)).astype(np.float32)
+    d = (d + 0.4 * d * d).astype(np.float32)
+    tris = [(0.05, 0.08, 0.1), (0.05, 0.08, 0.12), (0.1, 0.1, 0.1), (0.06, 0.09, 0.07)]
+    plan = PKL.BkPlan(N, L, tris, 'CIC')
+    assert plan.side < N
+    plan.run(d)
+    B, Q, P1, P2, P3 = plan.result()
+    full = PKL.BkPlan(N, L, tris, 'CIC', side=N)
+    full.run(d)
+    Bf, Qf, P1f, P2f, P3f = full.result()
+    assert np.abs(B - Bf).max() <= 1e-5 * np.abs(Bf).max()
+    np.testing.assert_allclose(P3, P3f, rtol=1e-12)
+    o = O.Bk(d, L, 0.05, 0.08, np.array([np.arccos((0.1 ** 2 - 0.05 ** 2 - 0.08 ** 2) / (2 * 0.05 * 0.08))]),
+             'CIC', 1)
+    assert abs(B[0] - o.B[0]) <= 1e-3 * abs(o.B[0])
+
+
+def test_bk_plan_graph_replay(PKL):
+    """The whole bispectrum chain (R2C, deconvolution, shell fill, C2R, grouped sums)
+    captured as one CUDA graph and replayed gives the eager result."""
+    rng = np.random.default_rng(19)
+    N, L = 64, 1000.0
+    d = torch.from_numpy(rng.standard_normal((N, N, N)).astype(np.float32)).cuda()
+    tris = [(0.05, 0.1, float(k)) for k in np.linspace(0.06, 0.14, 6)] + [(0.08, 0.08, 0.08)]
+    plan = PKL.BkPlan(N, L, tris, 'PCS')
+    plan.run(d)
+    ref = plan.result()
+    plan.capture(d)
+    for _ in range(2):
+        plan.replay()
+    got = plan.result()
+    for a, b in zip(got, ref):
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=0)
