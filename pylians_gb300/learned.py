@@ -16,6 +16,7 @@ nbar, deposited on a coarse grid without interlacing and on a 4x finer grid
 with interlacing (pipeline.ParticlePk).  The plain interlaced fine-grid
 estimate is both the training target and the fallback.
 """
+import json
 import math
 import os
 import time
@@ -100,9 +101,11 @@ class MLP(object):
     def params(self):
         return self.master.cpu().numpy()
 
-    def save(self, path):
+    def save(self, path, provenance=None):
+        """Parameters (and, when given, a JSON string saying how they were trained)."""
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-        np.savez(path, params=self.params())
+        extra = {'provenance': np.array(provenance)} if provenance else {}
+        np.savez(path, params=self.params(), **extra)
 
     @classmethod
     def load(cls, path=DEFAULT_WEIGHTS, device=None):
@@ -179,15 +182,23 @@ def make_pair(N, slope, nbar, MAS='CIC', seed=0, n_target=2_000_000, axis=0, sig
                 Nmodes=rc.Nmodes3D[sel])
 
 
-def training_set(count, seed=0, coarse=(128, 256), mas=('CIC', 'TSC', 'PCS'), density=(0.25, 4.0),
+# Particles of one training pair at most: the 4N = 2048 interlaced fine grid of an N = 512
+# pair (two 2048^3 grids, their transforms and the binning workspace, about 200 GB with
+# 1024^3 particles) leaves no room for more.
+MAX_PAIR_PARTICLES = 1 << 30
+
+
+def training_set(count, seed=0, coarse=(128, 256, 512), mas=('CIC', 'TSC', 'PCS'), density=(0.25, 4.0),
                  sigma=(0.1, 0.6)):
     """Pairs with slope n in [-2.5, -0.5], nbar log-uniform in [1e-4, 1] (h/Mpc)^3, particle
-    count (2N)^3 times a log-uniform factor in `density`, field rms log-uniform in `sigma`."""
+    count (2N)^3 times a log-uniform factor in `density` (at most MAX_PAIR_PARTICLES), field
+    rms log-uniform in `sigma`."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         N = int(rng.choice(coarse))
         n_target = int((2 * N) ** 3 * math.exp(rng.uniform(math.log(density[0]), math.log(density[1]))))
+        n_target = min(n_target, MAX_PAIR_PARTICLES)
         out.append(make_pair(N, float(rng.uniform(-2.5, -0.5)), float(10 ** rng.uniform(-4, 0)),
                              str(rng.choice(mas)), seed=seed * 100003 + i, n_target=n_target,
                              sigma=float(math.exp(rng.uniform(math.log(sigma[0]), math.log(sigma[1]))))))
@@ -256,6 +267,19 @@ def _timed(fn, reps):
     return float(np.median(ts)), out
 
 
+def _device_ms(fn, reps):
+    """Mean CUDA-event time (ms) of fn()'s launches on the current stream."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def evaluate(N=512, side=1024, slope=-1.5, L=1000.0, MAS='CIC', seed=11, oracle_grid=0, reps=3,
              net=None):
     """Learned-corrected N^3 non-interlaced P(k) against the plain interlaced (2N)^3 estimate of
@@ -290,6 +314,8 @@ def evaluate(N=512, side=1024, slope=-1.5, L=1000.0, MAS='CIC', seed=11, oracle_
 
     t_c, (rc, Pcorr, s_est, shot_est) = _timed(coarse, reps)
     t_f, rf = _timed(fine, reps)
+    dev_c = _device_ms(lambda: c.step(pos), reps)
+    dev_f = _device_ms(lambda: f.step(pos), reps)
     nb = len(rc.k3D)
     sel = (rc.k3D <= 0.8 * kN) & (rc.Nmodes3D > 0)
     Pf = rf.Pk[:nb, 0]
@@ -300,6 +326,7 @@ def evaluate(N=512, side=1024, slope=-1.5, L=1000.0, MAS='CIC', seed=11, oracle_
                max_err_learned=float(err_c.max()), mean_err_learned=float(err_c.mean()),
                max_err_plain=float(err_plain.max()), mean_err_plain=float(err_plain.mean()),
                ms_coarse_learned=t_c, ms_fine_interlaced=t_f, speedup=t_f / t_c,
+               device_ms_coarse_step=dev_c, device_ms_fine_step=dev_f,
                k=rc.k3D[sel].tolist(), ratio_learned=(Pcorr[sel] / Pf[sel]).tolist(),
                ratio_plain=(rc.Pk[sel, 0] / Pf[sel]).tolist())
     del c, f
@@ -322,10 +349,11 @@ def main():
     """Train on the device and save DEFAULT_WEIGHTS (python -m pylians_gb300.learned), or
     with --evaluate write the evaluation of the saved weights as JSON."""
     import argparse
-    import json
     ap = argparse.ArgumentParser()
-    ap.add_argument('--pairs', type=int, default=96)
+    # the shipped weights (data/aliasing_mlp.npz) are these defaults' result
+    ap.add_argument('--pairs', type=int, default=160)
     ap.add_argument('--steps', type=int, default=20000)
+    ap.add_argument('--seed', type=int, default=1)
     ap.add_argument('--out', default=DEFAULT_WEIGHTS)
     ap.add_argument('--evaluate', default=None, help='write the evaluation JSON here')
     ap.add_argument('--coarse', type=int, default=512)
@@ -343,7 +371,7 @@ def main():
             json.dump(res, fh)
         print(json.dumps({k: v for k, v in res.items() if not isinstance(v, list)}))
         return
-    pairs = training_set(a.pairs, seed=1)
+    pairs = training_set(a.pairs, seed=a.seed)
     if a.pairs_out:
         np.savez(a.pairs_out, x=np.concatenate([p['x'] for p in pairs]),
                  t=np.concatenate([p['t'] for p in pairs]),
@@ -351,9 +379,13 @@ def main():
                  meta=np.array([(p['N'], p['slope'], p['slope_est'], p['shot'], p['shot_est'], p['n'],
                                  p['nbar'], MAS_P[p['MAS']]) for p in pairs]))
     net, losses = train(pairs, steps=a.steps)
-    net.save(a.out)
-    print('trained on %d pairs (%d bins): loss %.3e -> %.3e, saved %s'
-          % (len(pairs), sum(len(p['t']) for p in pairs), losses[0], losses[-1], a.out))
+    sizes = {int(N): sum(1 for p in pairs if p['N'] == N) for N in sorted({p['N'] for p in pairs})}
+    net.save(a.out, json.dumps(dict(command='python -m pylians_gb300.learned --pairs %d --steps %d --seed %d'
+                                            % (a.pairs, a.steps, a.seed), pairs_by_coarse_side=sizes,
+                                    bins=int(sum(len(p['t']) for p in pairs)), loss_first=float(losses[0]),
+                                    loss_last=float(losses[-1]))))
+    print('trained on %d pairs %s (%d bins): loss %.3e -> %.3e, saved %s'
+          % (len(pairs), sizes, sum(len(p['t']) for p in pairs), losses[0], losses[-1], a.out))
 
 
 if __name__ == '__main__':
