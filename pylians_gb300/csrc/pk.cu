@@ -12,26 +12,43 @@ namespace pyl {
 
 namespace {
 
+// Per-axis float64 tables in shared memory, built once per CTA: the MAS factor
+// C(k) = (x / sin x)^p of each frequency and, for the interlaced combine, the
+// phase e^{i pi k / N}.  Per mode: the float64 product C(kx) C(ky) C(kz) rounded to
+// float32 (Pk_library.pyx:86-87,353-355) and the phase as the product of the three
+// axis phases (equal to e^{i pi (kx+ky+kz)/N} to float64 rounding).
 __global__ void __launch_bounds__(256) deconvolve_kernel(float2 *dk, const float2 *dk2, PkDims d, int p)
 {
+    extern __shared__ double dtab[];
     const int dims = d.dims;
+    double *corr = dtab;                        // [dims]
+    double2 *ph = (double2 *)(dtab + dims);     // [dims] when interlaced
+    for (int i = threadIdx.x; i < dims; i += blockDim.x) {
+        const int k = freq_of(i, dims);
+        corr[i] = mas_corr_d(k, dims, p);
+        if (dk2) {
+            double s, c;
+            sincospi((double)k / dims, &s, &c);
+            ph[i] = make_double2(c, s);
+        }
+    }
+    __syncthreads();
     const long long total = (long long)dims * dims * d.nz;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
         const int kz = (int)(i % d.nz);
         const long long rr = i / d.nz;
         const int kyy = (int)(rr % dims), kxx = (int)(rr / dims);
-        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
         float2 v = dk[i];
         if (dk2) {
-            double s, c;
-            sincospi((double)(kx + ky + kz) / dims, &s, &c);
+            const double2 a = ph[kxx], b = ph[kyy], e = ph[kz];
+            const double2 ab = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+            const float pc = (float)(ab.x * e.x - ab.y * e.y), ps = (float)(ab.x * e.y + ab.y * e.x);
             const float2 w = dk2[i];
-            const float pc = (float)c, ps = (float)s;
             v.x = 0.5f * (v.x + (w.x * pc - w.y * ps));
             v.y = 0.5f * (v.y + (w.x * ps + w.y * pc));
         }
-        const float mf = (float)(mas_corr_d(kx, dims, p) * mas_corr_d(ky, dims, p) * mas_corr_d(kz, dims, p));
+        const float mf = (float)(corr[kxx] * corr[kyy] * corr[kz]);
         dk[i] = make_float2(__fmul_rn(v.x, mf), __fmul_rn(v.y, mf));
     }
 }
@@ -114,7 +131,10 @@ extern "C" int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims,
     PYL_CHECK_ARG(mas_p >= 0 && mas_p <= 4, "MAS exponent must be 0..4");
     const PkDims d = pk_dims(dims);
     const long long total = (long long)dims * dims * d.nz;
-    deconvolve_kernel<<<blocks_for(total, 256), 256, 0, (cudaStream_t)stream>>>(
+    const size_t smem = sizeof(double) * (size_t)dims * (dk_interlaced ? 3 : 1);
+    PYL_CUDA(ensure_smem(deconvolve_kernel, smem));
+    // two CTAs per SM: each builds its tables once and strides over the modes
+    deconvolve_kernel<<<blocks_for(total, 256, 2), 256, smem, (cudaStream_t)stream>>>(
         (float2 *)dk, (const float2 *)dk_interlaced, d, mas_p);
     PYL_LAUNCH_CHECK();
     return PYL_OK;

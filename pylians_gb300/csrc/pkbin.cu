@@ -389,9 +389,6 @@ inline int seq_chunk(int nz)
 inline unsigned seq_chunk_magic(int chunk) { return (unsigned)((0x100000000ull + chunk - 1) / chunk); }
 
 
-// strides of pass 1 whose loads are in flight together
-constexpr int SEQ_U = 4;
-
 template <bool INTER, int AXIS>
 __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
@@ -455,38 +452,23 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
             cur_ring = ring;
             __syncwarp();
         }
-        // pass 1: per-mode power and phase^2, coalesced along kz; the loads of SEQ_U
-        // strides are issued before any of them is used (the binning pass below issues
-        // none, so the warp's loads in flight come from here)
-        for (int kz0 = lane; kz0 < nz; kz0 += 32 * SEQ_U) {
-            float2 vv[SEQ_U], ww[SEQ_U];
-#pragma unroll
-            for (int u = 0; u < SEQ_U; u++) {
-                const int kz = kz0 + 32 * u;
-                if (kz < nz) {
-                    vv[u] = __ldg(a.dk + row + kz);
-                    if (INTER) ww[u] = __ldg(a.dk2 + row + kz);
-                }
+        // pass 1: per-mode power and phase^2, coalesced along kz
+#pragma unroll 2
+        for (int kz = lane; kz < nz; kz += 32) {
+            float2 v = __ldg(a.dk + row + kz);
+            if (INTER) {
+                const float2 w = __ldg(a.dk2 + row + kz);
+                const float2 t = ph[kz];
+                const float2 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
+                v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
+                v.y = 0.5f * (v.y + (w.x * pz.y + w.y * pz.x));
             }
-#pragma unroll
-            for (int u = 0; u < SEQ_U; u++) {
-                const int kz = kz0 + 32 * u;
-                if (kz >= nz) break;
-                float2 v = vv[u];
-                if (INTER) {
-                    const float2 w = ww[u];
-                    const float2 t = ph[kz];
-                    const float2 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
-                    v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
-                    v.y = 0.5f * (v.y + (w.x * pz.y + w.y * pz.x));
-                }
-                const float mf = __fmul_rn(cxy, corr[kz]);
-                const float re = __fmul_rn(v.x, mf), im = __fmul_rn(v.y, mf);
-                float p2 = re * re + im * im;
-                float phase = p2 > 0.0f ? atan_unit(re * rsqrtf(p2)) : 0.0f;
-                if (hermitian_skip(kx, ky, kz, d)) { p2 = 0.0f; phase = 0.0f; }
-                stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(p2, phase * phase);   // kz + kz / chunk
-            }
+            const float mf = __fmul_rn(cxy, corr[kz]);
+            const float re = __fmul_rn(v.x, mf), im = __fmul_rn(v.y, mf);
+            float p2 = re * re + im * im;
+            float phase = p2 > 0.0f ? atan_unit(re * rsqrtf(p2)) : 0.0f;
+            if (hermitian_skip(kx, ky, kz, d)) { p2 = 0.0f; phase = 0.0f; }
+            stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(p2, phase * phase);   // kz + kz / chunk
         }
         __syncwarp();
         // pass 2: this lane's run of kz, sums kept while the bins stay the same
@@ -499,20 +481,18 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
             int kp2 = kperp2 + kz * kz;
             int kper = AXIS == 2 ? ring : isqrt_exact(kp2);
             const int kpar_c = AXIS == 0 ? kx * kx : ky * ky;
-            // per bin: sums of |d|^2, |d|^2 mu^2, |d|^2 mu^4 and phase^2; at a flush the
-            // mu moments become the l = 2, 4 sums, L2 = (3 mu^2 - 1)/2 and
-            // L4 = (35 mu^4 - 30 mu^2 + 3)/8 (Pk_library.pyx:358-362)
-            float s0 = 0.0f, m2 = 0.0f, m4 = 0.0f, sp = 0.0f, sd = 0.0f;
+            float s0 = 0.0f, s2 = 0.0f, s4 = 0.0f, sp = 0.0f, sd = 0.0f;
             const float2 *run = stage + lane * (chunk + 1);
             for (; kz < kz_end; kz++) {
                 const float2 e = run[kz - kz_begin];
                 const float val = e.x;
                 const int kpar2 = AXIS == 2 ? kz * kz : kpar_c;
                 const float mu2 = n2 ? __fdividef((float)kpar2, (float)n2) : 0.0f;
-                const float vm2 = val * mu2;
+                const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
+                const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
                 s0 += val;
-                m2 += vm2;
-                m4 += vm2 * mu2;
+                s2 += val * l2;
+                s4 += val * l4;
                 sp += e.y;
                 if (AXIS == 2) {
                     w2[kz] += val;
@@ -531,8 +511,6 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
                     new2 = (kper + 1) * (kper + 1) <= kp2;
                 }
                 if (new3 || kz + 1 == kz_end) {
-                    const float s2 = 1.5f * m2 - 0.5f * s0;
-                    const float s4 = 4.375f * m4 - 3.75f * m2 + 0.375f * s0;
                     if (part) {                         // one vector reduction in L2
                         atomicAdd(reinterpret_cast<float4 *>(part + ki * 4), make_float4(s0, s2, s4, sp));
                     } else {                            // float shared atomics: compare-and-swap loops
@@ -542,7 +520,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
                         if (s4 != 0.0f) atomicAdd(b3 + 2, s4);
                         if (sp != 0.0f) atomicAdd(b3 + 3, sp);
                     }
-                    s0 = m2 = m4 = sp = 0.0f;
+                    s0 = s2 = s4 = sp = 0.0f;
                     ki += new3 ? 1 : 0;
                 }
                 if (AXIS != 2 && (new2 || kz + 1 == kz_end)) {
