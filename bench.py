@@ -43,6 +43,8 @@ def parse():
     ap.add_argument('--particles-side', type=int, default=1024)
     ap.add_argument('--cpu-side', type=int, default=512, help='side of the CPU baseline sample')
     ap.add_argument('--no-secondary', action='store_true')
+    ap.add_argument('--secondary-only', default=None, choices=['zeldovich', 'bispectrum', 'batch', 'learned'],
+                    help='run only this secondary workload and print its JSON (profiling)')
     ap.add_argument('--batch-size', type=int, default=512)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
@@ -244,6 +246,13 @@ def main():
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if a.secondary_only:
+        import pylians_gb300.build as pb
+        pb.build()
+        fn = dict(zeldovich=bench_zeldovich, bispectrum=bench_bispectrum, learned=bench_learned,
+                  batch=lambda: bench_batch(a.batch_size))[a.secondary_only]
+        print(json.dumps({a.secondary_only: fn()}))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group('nccl')
