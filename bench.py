@@ -481,10 +481,10 @@ def bench_bispectrum(reps=5):
     and for the whole chain; the call time adds the read-back and finalisation.
 
     Algorithmic bytes (N_g = N^3, N_h = N^2 (N/2+1) on the input grid; M_g, M_h the same on
-    the reduced side M of the shell fields; S shells, T triangles, G (a, b) groups of at
-    most 8 triangles):
+    the reduced side M of the shell fields; S shells):
       R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill 2 S x 8 M_h (both fields
-      written); C2R 2 S (8 M_h + 4 M_g); reduction 4 G x 4 M_g + 2 T x 4 M_g."""
+      written); C2R 2 S (8 M_h + 4 M_g); reduction 2 S x 4 M_g (every shell field read
+      once; the kernel re-reads the fields shared by several triangle groups, from L2)."""
     import ctypes
     import torch
     import pylians_gb300.MAS_library as MASL
@@ -544,9 +544,9 @@ def bench_bispectrum(reps=5):
     pairs = {}
     for a, b, _ in plan.tri:
         pairs[(int(a), int(b))] = pairs.get((int(a), int(b)), 0) + 1
-    G = sum(-(-c // 8) for c in pairs.values())
+    G = sum(-(-c // 4) for c in pairs.values())
     alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=2 * S * 8.0 * Mh,
-               fft_c2r=2 * S * (8.0 * Mh + 4.0 * Mg), triangles=4 * G * 4.0 * Mg + 2 * T * 4.0 * Mg)
+               fft_c2r=2 * S * (8.0 * Mh + 4.0 * Mg), triangles=2 * S * 4.0 * Mg)
     names = ['fft_r2c', 'deconvolve', 'shell_fill', 'fft_c2r', 'triangles']
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}

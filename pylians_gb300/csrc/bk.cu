@@ -84,9 +84,12 @@ __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restric
 }
 
 // Triangles grouped by their first two shells: a group reads d_a d_b and I_a I_b
-// once per cell and the third shell of each of its (up to GC) triangles.
-constexpr int GC = 8;
-constexpr int MAX_GROUPS = 64;
+// once per cell and the third shell of each of its (up to GC) triangles.  GC = 4
+// keeps a thread within 85 registers (three resident CTAs per SM: with GC = 8 and
+// 128 registers the reduction was latency bound at 18% of the warp slots); groups
+// sharing (a, b) re-read those two fields, mostly from L2.
+constexpr int GC = 4;
+constexpr int MAX_GROUPS = 96;
 
 struct TriGroups {
     int a[MAX_GROUPS], b[MAX_GROUPS], n[MAX_GROUPS];
@@ -161,20 +164,16 @@ __device__ __forceinline__ void tri_group(const float *__restrict__ d, const flo
     }
 }
 
-__global__ void __launch_bounds__(256) triangle_group_kernel(const float *__restrict__ d, const float *__restrict__ I,
-                                                             long long cells, long long fs, TriGroups tg,
-                                                             double *num, double *den)
+__global__ void __launch_bounds__(256, 3) triangle_group_kernel(const float *__restrict__ d,
+                                                                const float *__restrict__ I, long long cells,
+                                                                long long fs, TriGroups tg, double *num, double *den)
 {
     const int gi = blockIdx.y;
     switch (tg.n[gi]) {     // the third-shell count of a group is uniform over its CTAs
         case 1: tri_group<1>(d, I, cells, fs, tg, gi, num, den); break;
         case 2: tri_group<2>(d, I, cells, fs, tg, gi, num, den); break;
         case 3: tri_group<3>(d, I, cells, fs, tg, gi, num, den); break;
-        case 4: tri_group<4>(d, I, cells, fs, tg, gi, num, den); break;
-        case 5: tri_group<5>(d, I, cells, fs, tg, gi, num, den); break;
-        case 6: tri_group<6>(d, I, cells, fs, tg, gi, num, den); break;
-        case 7: tri_group<7>(d, I, cells, fs, tg, gi, num, den); break;
-        default: tri_group<8>(d, I, cells, fs, tg, gi, num, den); break;
+        default: tri_group<4>(d, I, cells, fs, tg, gi, num, den); break;
     }
 }
 
@@ -258,8 +257,8 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
                 tg.t[g][j] = t;
             }
         }
-        // about four resident CTAs per SM over all groups of the launch
-        long long b = std::max(8LL, (long long)num_sms() * 4 / ng);
+        // about sixteen CTAs per SM over all groups of the launch (three resident)
+        long long b = std::max(8LL, (long long)num_sms() * 16 / ng);
         if (b > bx) b = bx;
         if (b < 1) b = 1;
         triangle_group_kernel<<<dim3((unsigned)b, (unsigned)ng), 256, 0, st>>>(d_fields, i_fields, cells, field_stride,
