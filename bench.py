@@ -476,15 +476,16 @@ def bench_zeldovich(reps=3):
 def bench_bispectrum(reps=5):
     """Bispectra of a 256^3 CIC overdensity (1000 Mpc/h, 256^3 uniform particles): k1=0.1,
     k2=0.2 h/Mpc with 32 theta bins, plus 20 equilateral triangles k=0.02..0.4 h/Mpc, all 52
-    triangles through one BkPlan (one R2C, one shell fill, one batched C2R per field kind,
-    one grouped reduction).  Device time by CUDA events on the launching stream, per stage
-    and for the whole chain; the call time adds the read-back and finalisation.
+    triangles through one BkPlan (one R2C, one shell fill, one batched C2R, one grouped
+    reduction per call; the indicator fields' sums are the plan's, made once).  Device
+    time by CUDA events on the launching stream, per stage and for the whole chain; the
+    call time adds the read-back and finalisation.
 
     Algorithmic bytes (N_g = N^3, N_h = N^2 (N/2+1) on the input grid; M_g, M_h the same on
     the reduced side M of the shell fields; S shells):
-      R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill 2 S x 8 M_h (both fields
-      written); C2R 2 S (8 M_h + 4 M_g); reduction 2 S x 4 M_g (every shell field read
-      once; the kernel re-reads the fields shared by several triangle groups, from L2)."""
+      R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill S x 8 M_h (the delta fields
+      written); C2R S (8 M_h + 4 M_g); reduction S x 4 M_g (every shell field read once;
+      the kernel re-reads the fields shared by several triangle groups, from L2)."""
     import ctypes
     import torch
     import pylians_gb300.MAS_library as MASL
@@ -523,13 +524,12 @@ def bench_bispectrum(reps=5):
         _lib.call('pyl_mas_deconvolve', ptr(plan.dk), None, N, plan.mas_p, st)
         se[2].record()
         _lib.call('pyl_bk_shell_fill', ptr(plan.dk), N, m, ctypes.cast(plan._lo[0], ctypes.c_void_p),
-                  ctypes.cast(plan._hi[0], ctypes.c_void_p), S, ptr(plan.cd), ptr(plan.ci), ptr(plan.power), st)
+                  ctypes.cast(plan._hi[0], ctypes.c_void_p), S, ptr(plan.cd), None, ptr(plan.power), st)
         se[3].record()
         _lib.call('pyl_fft_c2r', ptr(plan.cd), ptr(plan.d_real), m, S, st)
-        _lib.call('pyl_fft_c2r', ptr(plan.ci), ptr(plan.i_real), m, S, st)
         se[4].record()
-        _lib.call('pyl_bk_triangles', ptr(plan.d_real), ptr(plan.i_real), m, plan.stride, S,
-                  ctypes.cast(plan._tri, ctypes.c_void_p), T, ptr(plan.num), ptr(plan.den), st)
+        _lib.call('pyl_bk_triangles', ptr(plan.d_real), None, m, plan.stride, S,
+                  ctypes.cast(plan._tri, ctypes.c_void_p), T, ptr(plan.num), None, st)
         se[5].record()
         torch.cuda.synchronize()
         acc += [se[k].elapsed_time(se[k + 1]) for k in range(5)]
@@ -545,8 +545,8 @@ def bench_bispectrum(reps=5):
     for a, b, _ in plan.tri:
         pairs[(int(a), int(b))] = pairs.get((int(a), int(b)), 0) + 1
     G = sum(-(-c // 4) for c in pairs.values())
-    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=2 * S * 8.0 * Mh,
-               fft_c2r=2 * S * (8.0 * Mh + 4.0 * Mg), triangles=2 * S * 4.0 * Mg)
+    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=S * 8.0 * Mh,
+               fft_c2r=S * (8.0 * Mh + 4.0 * Mg), triangles=S * 4.0 * Mg)
     names = ['fft_r2c', 'deconvolve', 'shell_fill', 'fft_c2r', 'triangles']
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}

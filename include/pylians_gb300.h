@@ -232,6 +232,28 @@ int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_fields, int64_t 
 int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t workspace_bytes,
                     void *stream);
 
+/* Many one-field spectra of one grid side in one launch (the batched-realization
+ * path; no counterpart in the reference, which bins one field per Pk call).  `items`
+ * is a DEVICE array of n_items records, each one pyl_pk_bin call with n_fields = 1:
+ * its field, its interlaced partner (non-NULL in every record when `interlaced`,
+ * ignored otherwise), its own zeroed-by-the-call `sums` (pyl_pk_sums_len(dims, 1)
+ * doubles) and MAS exponent.  The sums equal pyl_pk_bin's item by item (the same
+ * CTA partition and float32 partial sums; float64 atomics in another order).  The
+ * workspace (pyl_pk_bin_batch_workspace_size bytes) holds the axis-2 row table and
+ * every item's per-CTA partial sums.  A workspace size of 0, and
+ * PYL_ERR_UNSUPPORTED from the call, mean that one field's bins do not fit the
+ * one-field kernel's shared memory: bin such items one by one with pyl_pk_bin. */
+typedef struct pyl_pk_item {
+    const void *dk;
+    const void *dk_interlaced;
+    double *sums;
+    int mas_p;
+    int reserved;
+} pyl_pk_item;
+size_t pyl_pk_bin_batch_workspace_size(int dims, int n_items, int axis, int interlaced);
+int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims, int axis, int interlaced,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
 /* In place: d <- (interlace-combined d) * W(k)^-1 as float32, on every stored
  * mode (Pk_library.pyx:353-355; bispectrum_library.pyx:107-109).  This is the
  * delta_k the reference keeps with keep_deltak=True. */
@@ -252,6 +274,10 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  * the shell fields are band-limited, so the triple-product sums over out_dims^3
  * cells are (out_dims/dims)^3 times those over dims^3 cells and B, a ratio of
  * two such sums, is the same.  At most PYL_BK_MAX_SHELLS shells per call.
+ * Either output may be NULL: the indicator fields and their sums depend only on
+ * the shells, so a plan fills them once (out_delta NULL, dk may then be NULL too;
+ * power[2*s] is then 0) and every later call fills the delta fields alone
+ * (out_ind NULL; power[2*s+1] is written either way).
  *
  * pyl_bk_triangles reduces the C2R'd real fields: for triangle t with shells
  * (a,b,c) = host_tri[3t..3t+2], num[t] = sum_x d_a d_b d_c and
@@ -259,7 +285,8 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  * (the grid the fields live on); triangles sharing (a, b) are reduced together,
  * reading d_a d_b and I_a I_b once.  d_fields / i_fields are float32, shell s at
  * offset s*field_stride elements (field_stride >= dims^3, a multiple of 4;
- * buffers 16-byte aligned).
+ * buffers 16-byte aligned).  With i_fields NULL only num is computed (den may be
+ * NULL and is not touched); with d_fields NULL only den.
  */
 #define PYL_BK_MAX_SHELLS 96
 int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const int64_t *host_k2_lo,

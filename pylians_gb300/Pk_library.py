@@ -465,11 +465,13 @@ def bk_side(dims, bounds):
 class BkPlan(object):
     """Bispectra of a fixed triangle set (k1, k2, k3 in h/Mpc) on dims^3 fields: shells,
     their exact integer bounds, the reduced grid side, triangle index lists and every
-    device buffer are set up once; run(delta) enqueues the whole chain on one stream
-    (R2C, MAS deconvolution, shell fill, batched C2R of the shell fields, grouped
-    triple-product sums) with no host synchronisation, so capture() can record it as a
-    CUDA graph; result() reads the sums back and finalises B, Q and the shell powers
-    (bispectrum_library.pyx:132-190)."""
+    device buffer are set up once, and so are the indicator fields' triple sums
+    (sum_x I_a I_b I_c depends only on the shells: filled, transformed and reduced by
+    the same kernels as the delta fields, once per plan).  run(delta) enqueues the
+    data-dependent chain on one stream (R2C, MAS deconvolution, delta shell fill,
+    batched C2R of the delta shell fields, grouped triple-product sums) with no host
+    synchronisation, so capture() can record it as a CUDA graph; result() reads the
+    sums back and finalises B, Q and the shell powers (bispectrum_library.pyx:132-190)."""
 
     MAX_SHELLS = 96
 
@@ -501,9 +503,7 @@ class BkPlan(object):
         dev = self.device
         self.dk = torch.empty(_half_shape(self.dims), dtype=torch.complex64, device=dev)
         self.cd = torch.empty((S, self.half), dtype=torch.complex64, device=dev)
-        self.ci = torch.empty((S, self.half), dtype=torch.complex64, device=dev)
         self.d_real = torch.empty(S * self.stride, dtype=torch.float32, device=dev)
-        self.i_real = torch.empty(S * self.stride, dtype=torch.float32, device=dev)
         self.power = torch.empty(2 * S, dtype=torch.float64, device=dev)
         self.num = torch.empty(T, dtype=torch.float64, device=dev)
         self.den = torch.empty(T, dtype=torch.float64, device=dev)
@@ -515,6 +515,37 @@ class BkPlan(object):
         self._tri = (ctypes.c_int * (3 * T))(*[int(i) for t in tri_idx for i in t])
         self.mas_p = MAS_function(MAS)
         self.graph = None
+        self._indicator_sums()
+
+    def _fill(self, dk, out_delta, out_ind, st):
+        import ctypes
+        S = len(self.bounds)
+        for j, s0 in enumerate(range(0, S, self.MAX_SHELLS)):
+            ns = min(self.MAX_SHELLS, S - s0)
+            _lib.call('pyl_bk_shell_fill', dk, self.dims, self.side, ctypes.cast(self._lo[j], ctypes.c_void_p),
+                      ctypes.cast(self._hi[j], ctypes.c_void_p), ns,
+                      ptr(out_delta[s0]) if out_delta is not None else None,
+                      ptr(out_ind[s0]) if out_ind is not None else None, ptr(self.power[2 * s0:]), st)
+
+    def _c2r(self, spec, real, st):
+        m, S = self.side, len(self.bounds)
+        if self.stride == self.cells:
+            _lib.call('pyl_fft_c2r', ptr(spec), ptr(real), m, S, st)
+        else:
+            for s in range(S):
+                _lib.call('pyl_fft_c2r', ptr(spec[s]), ptr(real[s * self.stride:]), m, 1, st)
+
+    def _indicator_sums(self):
+        """den[t] = sum_x I_a I_b I_c on the reduced grid, once: the indicator fields are
+        filled into the delta buffers (which every run overwrites), transformed and
+        reduced, with no delta input."""
+        import ctypes
+        with torch.cuda.device(self.device):
+            st = stream_ptr(None)
+            self._fill(None, None, self.cd, st)
+            self._c2r(self.cd, self.d_real, st)
+            _lib.call('pyl_bk_triangles', None, ptr(self.d_real), self.side, self.stride, len(self.bounds),
+                      ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), None, ptr(self.den), st)
 
     def run(self, delta, stream=None):
         """Enqueue the chain on `delta` (a dims^3 float32 grid); nothing waits on the host."""
@@ -527,20 +558,10 @@ class BkPlan(object):
         d, m, S = self.dims, self.side, len(self.bounds)
         _lib.call('pyl_fft_r2c', ptr(x), ptr(self.dk), d, 1, st)
         _lib.call('pyl_mas_deconvolve', ptr(self.dk), None, d, self.mas_p, st)
-        for j, s0 in enumerate(range(0, S, self.MAX_SHELLS)):
-            ns = min(self.MAX_SHELLS, S - s0)
-            _lib.call('pyl_bk_shell_fill', ptr(self.dk), d, m, ctypes.cast(self._lo[j], ctypes.c_void_p),
-                      ctypes.cast(self._hi[j], ctypes.c_void_p), ns, ptr(self.cd[s0]), ptr(self.ci[s0]),
-                      ptr(self.power[2 * s0:]), st)
-        if self.stride == self.cells:
-            _lib.call('pyl_fft_c2r', ptr(self.cd), ptr(self.d_real), m, S, st)
-            _lib.call('pyl_fft_c2r', ptr(self.ci), ptr(self.i_real), m, S, st)
-        else:
-            for s in range(S):
-                _lib.call('pyl_fft_c2r', ptr(self.cd[s]), ptr(self.d_real[s * self.stride:]), m, 1, st)
-                _lib.call('pyl_fft_c2r', ptr(self.ci[s]), ptr(self.i_real[s * self.stride:]), m, 1, st)
-        _lib.call('pyl_bk_triangles', ptr(self.d_real), ptr(self.i_real), m, self.stride, S,
-                  ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), ptr(self.num), ptr(self.den), st)
+        self._fill(ptr(self.dk), self.cd, None, st)
+        self._c2r(self.cd, self.d_real, st)
+        _lib.call('pyl_bk_triangles', ptr(self.d_real), None, m, self.stride, S,
+                  ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), ptr(self.num), None, st)
 
     def capture(self, delta):
         """Record run(delta) (fixed address) as a CUDA graph; replay() relaunches it."""

@@ -47,6 +47,8 @@ SIGNATURES = {
     'pyl_pk_workspace_size': (_SZ, [_I, _I, _I]),
     'pyl_pk_bin': (_I, [_P, _P, _I, _I64, _I, _I, _P, _P, _P, _SZ, _P]),
     'pyl_pk_geometry': (_I, [_I, _I, _P, _P, _SZ, _P]),
+    'pyl_pk_bin_batch_workspace_size': (_SZ, [_I, _I, _I, _I]),
+    'pyl_pk_bin_batch': (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
     'pyl_mas_deconvolve': (_I, [_P, _P, _I, _I, _P]),
     'pyl_bk_shell_fill': (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _P, _P]),
     'pyl_bk_triangles': (_I, [_P, _P, _I, _I64, _I, _P, _I, _P, _P, _P]),

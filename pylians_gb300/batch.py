@@ -10,7 +10,9 @@ interlacing.  One step runs:
     (pyl_ma_batch_tiled); method 'atomic' is ONE persistent launch of
     red.global deposits (pyl_ma_batch);
   * one batched cuFFT R2C per grid-size class;
-  * the fused P(k) bin kernel per realization (pyl_pk_bin).
+  * one launch of the fused P(k) bin kernel per (grid size, interlacing) class
+    over all of its realizations (pyl_pk_bin_batch), or pyl_pk_bin per
+    realization where a grid's bins do not fit that kernel's shared memory.
 Everything is stream-ordered, so `capture()` turns a step into one CUDA graph
 and `replay()` launches the whole batch at once.  Results equal the
 one-at-a-time path (pipeline.ParticlePk) up to float summation order.
@@ -27,6 +29,7 @@ REAL_DT = np.dtype([('pos', '<u8'), ('grid', '<u8'), ('grid2', '<u8'), ('inv', '
                     ('halfcell', '<f4'), ('scale', '<f4'), ('dims', '<i4'), ('mas', '<i4'),
                     ('reserved', '<i4')])
 ITEM_DT = np.dtype([('first', '<i8'), ('count', '<u4'), ('real', '<u4')])
+PK_ITEM_DT = np.dtype([('dk', '<u8'), ('dk2', '<u8'), ('sums', '<u8'), ('mas_p', '<i4'), ('reserved', '<i4')])
 
 
 class RealizationBatch(object):
@@ -57,7 +60,33 @@ class RealizationBatch(object):
         self.sums = [torch.empty(L.pyl_pk_sums_len(int(s['dims']), 1), dtype=torch.float64, device=self.device)
                      for s in self.specs]
         self.mas_p = [PKL.ctypes_int_array([_lib.MAS_INDEX[s['MAS']]]) for s in self.specs]
-        nbytes = max(L.pyl_pk_workspace_size(d, 1, self.axis) for d in self.classes)
+        # binning: one pyl_pk_bin_batch launch per (grid size, interlacing) class, each
+        # realization a device record (field, partner, sums, MAS); classes whose bins do
+        # not fit the batched kernel go one realization at a time
+        self.bin_classes, self.bin_single = [], []
+        nbytes = 0
+        for d in sorted(self.classes):
+            for inter in (False, True):
+                members = [i for i in sorted(set(self.classes[d]))
+                           if bool(self.specs[i].get('interlaced')) == inter]
+                if not members:
+                    continue
+                ws = L.pyl_pk_bin_batch_workspace_size(d, len(members), self.axis, int(inter))
+                if ws == 0:
+                    self.bin_single.extend(members)
+                    continue
+                rec = np.zeros(len(members), dtype=PK_ITEM_DT)
+                for j, i in enumerate(members):
+                    sp = self.specs[i]
+                    rec[j]['dk'] = self.dk[d][sp['slot']].data_ptr()
+                    rec[j]['dk2'] = self.dk[d][sp['slot2']].data_ptr() if inter else 0
+                    rec[j]['sums'] = self.sums[i].data_ptr()
+                    rec[j]['mas_p'] = _lib.MAS_INDEX[sp['MAS']]
+                table = torch.from_numpy(rec.view(np.uint8)).to(self.device)
+                self.bin_classes.append((d, inter, len(members), table))
+                nbytes = max(nbytes, ws)
+        for i in self.bin_single:
+            nbytes = max(nbytes, L.pyl_pk_workspace_size(int(self.specs[i]['dims']), 1, self.axis))
         self.pk_ws_bytes = nbytes
         self.pk_ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -136,7 +165,11 @@ class RealizationBatch(object):
                       ptr(self.counter), self.ctas_per_sm, st)
         for d, g in self.grids.items():
             _lib.call('pyl_fft_r2c', ptr(g), ptr(self.dk[d]), d, g.shape[0], st)
-        for i, s in enumerate(self.specs):
+        for d, inter, n, table in self.bin_classes:
+            _lib.call('pyl_pk_bin_batch', ptr(table), n, d, self.axis, int(inter), ptr(self.pk_ws),
+                      self.pk_ws_bytes, st)
+        for i in self.bin_single:
+            s = self.specs[i]
             d = int(s['dims'])
             dk = self.dk[d]
             dk2 = dk[s['slot2']] if s.get('interlaced') else None

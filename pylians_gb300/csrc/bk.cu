@@ -41,7 +41,9 @@ struct ShellBounds {
 // grid's own signed frequencies, each stored mode once.  The mode's value and
 // indicator go to slot (kx mod M, ky mod M, kz) of every shell that holds it; the
 // Parseval sums use the N grid's weights (1 on the kz = 0 and kz = N/2 planes, 2
-// elsewhere).
+// elsewhere).  FD / FI: write the delta / indicator fields (the indicator fields
+// only depend on the shells, so a plan writes them once).
+template <bool FD, bool FI>
 __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restrict__ dk, int dims, int K, int M,
                                                          ShellBounds sb, float2 *__restrict__ od,
                                                          float2 *__restrict__ oi, double *power)
@@ -66,14 +68,16 @@ __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restric
         if (!any) continue;
         const long long src = ((long long)(kx < 0 ? kx + dims : kx) * dims + (ky < 0 ? ky + dims : ky)) * nz + kz;
         const long long dst = ((long long)(kx < 0 ? kx + M : kx) * M + (ky < 0 ? ky + M : ky)) * mz + kz;
-        const float2 v = __ldg(dk + src);
+        const float2 v = FD ? __ldg(dk + src) : make_float2(0.0f, 0.0f);
         const double w = (kz == 0 || (even && kz == dims / 2)) ? 1.0 : 2.0;
         const double p2 = w * ((double)v.x * v.x + (double)v.y * v.y);
         for (int s = 0; s < sb.n; s++) {
             if (n2 >= sb.lo[s] && n2 < sb.hi[s]) {
-                od[s * half_m + dst] = v;
-                oi[s * half_m + dst] = make_float2(1.0f, 0.0f);
-                atomicAdd(acc + 2 * s, p2);
+                if (FD) {
+                    od[s * half_m + dst] = v;
+                    atomicAdd(acc + 2 * s, p2);
+                }
+                if (FI) oi[s * half_m + dst] = make_float2(1.0f, 0.0f);
                 atomicAdd(acc + 2 * s + 1, w);
             }
         }
@@ -97,8 +101,9 @@ struct TriGroups {
 };
 
 // blockIdx.y = group; float32 partial sums over 8 float4 steps, float64 above.
-// Products (d_a d_b) d_c, as the reference forms d12 * d3 (:183-186).
-template <int NC>
+// Products (d_a d_b) d_c, as the reference forms d12 * d3 (:183-186).  WD / WI:
+// reduce the delta / indicator fields (num / den).
+template <int NC, bool WD, bool WI>
 __device__ __forceinline__ void tri_group(const float *__restrict__ d, const float *__restrict__ I, long long cells,
                                           long long fs, const TriGroups &tg, int gi, double *num, double *den)
 {
@@ -116,16 +121,26 @@ __device__ __forceinline__ void tri_group(const float *__restrict__ d, const flo
 #pragma unroll
     for (int j = 0; j < NC; j++) { sn[j] = sd[j] = 0.0; fn[j] = fd[j] = 0.0f; }
     int k = 0;
+#pragma unroll 1    // unrolled, the one-sided forms spill at the 85-register cap
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
-        const float4 x = __ldg(da + i), y = __ldg(db + i), p = __ldg(ia + i), q = __ldg(ib + i);
-        const float4 xy = make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w);
-        const float4 pq = make_float4(p.x * q.x, p.y * q.y, p.z * q.z, p.w * q.w);
+        if (WD) {
+            const float4 x = __ldg(da + i), y = __ldg(db + i);
+            const float4 xy = make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w);
 #pragma unroll
-        for (int j = 0; j < NC; j++) {
-            const float4 z = __ldg(dc[j] + i), r = __ldg(ic[j] + i);
-            fn[j] += xy.x * z.x + xy.y * z.y + xy.z * z.z + xy.w * z.w;
-            fd[j] += pq.x * r.x + pq.y * r.y + pq.z * r.z + pq.w * r.w;
+            for (int j = 0; j < NC; j++) {
+                const float4 z = __ldg(dc[j] + i);
+                fn[j] += xy.x * z.x + xy.y * z.y + xy.z * z.z + xy.w * z.w;
+            }
+        }
+        if (WI) {
+            const float4 p = __ldg(ia + i), q = __ldg(ib + i);
+            const float4 pq = make_float4(p.x * q.x, p.y * q.y, p.z * q.z, p.w * q.w);
+#pragma unroll
+            for (int j = 0; j < NC; j++) {
+                const float4 r = __ldg(ic[j] + i);
+                fd[j] += pq.x * r.x + pq.y * r.y + pq.z * r.z + pq.w * r.w;
+            }
         }
         if (++k == 8) {
 #pragma unroll
@@ -141,8 +156,8 @@ __device__ __forceinline__ void tri_group(const float *__restrict__ d, const flo
         const float *a1 = I + tg.a[gi] * fs, *b1 = I + tg.b[gi] * fs;
 #pragma unroll
         for (int j = 0; j < NC; j++) {
-            sn[j] += (a0[i] * b0[i]) * d[tg.c[gi][j] * fs + i];
-            sd[j] += (a1[i] * b1[i]) * I[tg.c[gi][j] * fs + i];
+            if (WD) sn[j] += (a0[i] * b0[i]) * d[tg.c[gi][j] * fs + i];
+            if (WI) sd[j] += (a1[i] * b1[i]) * I[tg.c[gi][j] * fs + i];
         }
     }
     __shared__ double wsn[8][GC], wsd[8][GC];
@@ -159,21 +174,22 @@ __device__ __forceinline__ void tri_group(const float *__restrict__ d, const flo
     if (threadIdx.x < NC) {
         double a = 0.0, b = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += wsn[w][threadIdx.x]; b += wsd[w][threadIdx.x]; }
-        atomicAdd(num + tg.t[gi][threadIdx.x], a);
-        atomicAdd(den + tg.t[gi][threadIdx.x], b);
+        if (WD) atomicAdd(num + tg.t[gi][threadIdx.x], a);
+        if (WI) atomicAdd(den + tg.t[gi][threadIdx.x], b);
     }
 }
 
+template <bool WD, bool WI>
 __global__ void __launch_bounds__(256, 3) triangle_group_kernel(const float *__restrict__ d,
                                                                 const float *__restrict__ I, long long cells,
                                                                 long long fs, TriGroups tg, double *num, double *den)
 {
     const int gi = blockIdx.y;
     switch (tg.n[gi]) {     // the third-shell count of a group is uniform over its CTAs
-        case 1: tri_group<1>(d, I, cells, fs, tg, gi, num, den); break;
-        case 2: tri_group<2>(d, I, cells, fs, tg, gi, num, den); break;
-        case 3: tri_group<3>(d, I, cells, fs, tg, gi, num, den); break;
-        default: tri_group<4>(d, I, cells, fs, tg, gi, num, den); break;
+        case 1: tri_group<1, WD, WI>(d, I, cells, fs, tg, gi, num, den); break;
+        case 2: tri_group<2, WD, WI>(d, I, cells, fs, tg, gi, num, den); break;
+        case 3: tri_group<3, WD, WI>(d, I, cells, fs, tg, gi, num, den); break;
+        default: tri_group<4, WD, WI>(d, I, cells, fs, tg, gi, num, den); break;
     }
 }
 
@@ -186,7 +202,9 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
                                  const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
                                  double *power, void *stream)
 {
-    PYL_CHECK_ARG(dk && out_delta && out_ind && power && host_k2_lo && host_k2_hi, "null pointer");
+    PYL_CHECK_ARG(power && host_k2_lo && host_k2_hi, "null pointer");
+    PYL_CHECK_ARG(out_delta || out_ind, "no output field");
+    PYL_CHECK_ARG(dk || !out_delta, "the delta fields need dk");
     PYL_CHECK_ARG(dims >= 2 && dims <= 4096, "dims out of range");
     PYL_CHECK_ARG(n_shells >= 1 && n_shells <= PYL_BK_MAX_SHELLS, "1..96 shells per call");
     ShellBounds sb;
@@ -205,15 +223,19 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
                   "out_dims must equal dims, or exceed 3 K (and 2 K) with K the largest shell wave number");
     const long long half_m = (long long)out_dims * out_dims * (out_dims / 2 + 1);
     cudaStream_t st = (cudaStream_t)stream;
-    PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half_m * n_shells, st));
-    PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half_m * n_shells, st));
+    if (out_delta) PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half_m * n_shells, st));
+    if (out_ind) PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half_m * n_shells, st));
     PYL_CUDA(cudaMemsetAsync(power, 0, sizeof(double) * 2 * n_shells, st));
     const long long side = std::min(K, dims / 2) + std::min(K, (dims - 1) / 2) + 1;
     const long long cube = side * side * (std::min(K, dims / 2) + 1);
     long long blocks = (cube + 255) / 256;
     if (blocks > (long long)num_sms() * 8) blocks = (long long)num_sms() * 8;
-    shell_fill_kernel<<<(unsigned)std::max(1LL, blocks), 256, 0, st>>>((const float2 *)dk, dims, K, out_dims, sb,
-                                                                      (float2 *)out_delta, (float2 *)out_ind, power);
+    const unsigned g = (unsigned)std::max(1LL, blocks);
+    const float2 *src = (const float2 *)dk;
+    float2 *od = (float2 *)out_delta, *oi = (float2 *)out_ind;
+    if (od && oi) shell_fill_kernel<true, true><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
+    else if (od) shell_fill_kernel<true, false><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
+    else shell_fill_kernel<false, true><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
@@ -222,7 +244,9 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
                                 int64_t field_stride, int n_shells, const int *host_tri, int n_tri,
                                 double *num, double *den, void *stream)
 {
-    PYL_CHECK_ARG(d_fields && i_fields && host_tri && num && den, "null pointer");
+    PYL_CHECK_ARG(host_tri, "null pointer");
+    PYL_CHECK_ARG(d_fields || i_fields, "no field set");
+    PYL_CHECK_ARG((!d_fields || num) && (!i_fields || den), "null sum buffer");
     PYL_CHECK_ARG(dims >= 2 && n_shells >= 1 && n_tri >= 1, "bad sizes");
     PYL_CHECK_ARG((((uintptr_t)d_fields) & 15) == 0 && (((uintptr_t)i_fields) & 15) == 0,
                   "field buffers must be 16-byte aligned");
@@ -232,8 +256,8 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
     for (int t = 0; t < 3 * n_tri; t++)
         PYL_CHECK_ARG(host_tri[t] >= 0 && host_tri[t] < n_shells, "triangle shell index out of range");
     cudaStream_t st = (cudaStream_t)stream;
-    PYL_CUDA(cudaMemsetAsync(num, 0, sizeof(double) * n_tri, st));
-    PYL_CUDA(cudaMemsetAsync(den, 0, sizeof(double) * n_tri, st));
+    if (d_fields) PYL_CUDA(cudaMemsetAsync(num, 0, sizeof(double) * n_tri, st));
+    if (i_fields) PYL_CUDA(cudaMemsetAsync(den, 0, sizeof(double) * n_tri, st));
     // groups: triangles of equal (a, b), at most GC each
     std::map<std::pair<int, int>, std::vector<int>> by_ab;
     for (int t = 0; t < n_tri; t++) by_ab[std::make_pair(host_tri[3 * t], host_tri[3 * t + 1])].push_back(t);
@@ -261,8 +285,13 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
         long long b = std::max(8LL, (long long)num_sms() * 16 / ng);
         if (b > bx) b = bx;
         if (b < 1) b = 1;
-        triangle_group_kernel<<<dim3((unsigned)b, (unsigned)ng), 256, 0, st>>>(d_fields, i_fields, cells, field_stride,
-                                                                              tg, num, den);
+        const dim3 grid((unsigned)b, (unsigned)ng);
+        if (d_fields && i_fields)
+            triangle_group_kernel<true, true><<<grid, 256, 0, st>>>(d_fields, i_fields, cells, field_stride, tg, num, den);
+        else if (d_fields)
+            triangle_group_kernel<true, false><<<grid, 256, 0, st>>>(d_fields, i_fields, cells, field_stride, tg, num, den);
+        else
+            triangle_group_kernel<false, true><<<grid, 256, 0, st>>>(d_fields, i_fields, cells, field_stride, tg, num, den);
         PYL_LAUNCH_CHECK();
     }
     return PYL_OK;

@@ -76,6 +76,7 @@ struct BinArgs {
     int warp_arrays;       // axis 2: per-warp kz arrays in shared memory
     float *part;           // one field: per-CTA partial sums in global memory (null: shared memory)
     int part_stride;       // floats per CTA: 3D bins x 4, then k_per bins (axes 0/1)
+    const pyl_pk_item *items;  // batched one-field spectra: item blockIdx.y (dk, dk2, sums, MAS)
 };
 
 struct BinSmem {
@@ -389,17 +390,37 @@ inline int seq_chunk(int nz)
 inline unsigned seq_chunk_magic(int chunk) { return (unsigned)((0x100000000ull + chunk - 1) / chunk); }
 
 
-template <bool INTER, int AXIS>
+// BATCH: blockIdx.y picks an item of a.items (its field, partner, sums, MAS and
+// its slice of the partial sums); the CTA partition along blockIdx.x is a
+// one-field call's.
+template <bool INTER, int AXIS, bool BATCH>
 __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
     extern __shared__ float sm[];
     const PkDims d = a.d;
     const int dims = d.dims, nz = d.nz;
     const SeqSmem L = seq_smem(d, AXIS, INTER, chunk, a.part != nullptr);
+    // one field: the kernel parameters themselves (read from the constant bank,
+    // no registers held); batched: the item's record
+    const float2 *bdk = nullptr, *bdk2 = nullptr;
+    double *bsums = nullptr;
+    int bmas = 0;
+    if (BATCH) {
+        const pyl_pk_item it = a.items[blockIdx.y];
+        bdk = (const float2 *)it.dk;
+        bdk2 = (const float2 *)it.dk_interlaced;
+        bsums = it.sums;
+        bmas = it.mas_p;
+    }
+    const float2 *dk = BATCH ? bdk : a.dk;
+    const float2 *dk2 = BATCH ? bdk2 : a.dk2;
+    double *sums = BATCH ? bsums : a.sums;
+    const int mas = BATCH ? bmas : a.mas_p[0];
+    float *part_base = (BATCH && a.part) ? a.part + (long long)blockIdx.y * gridDim.x * a.part_stride : a.part;
     float *corr = sm + L.corr;
     float2 *ph = (float2 *)(sm + L.ph);
     float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
-    for (int i = threadIdx.x; i < dims; i += blockDim.x) corr[i] = mas_corr_f(freq_of(i, dims), dims, a.mas_p[0]);
+    for (int i = threadIdx.x; i < dims; i += blockDim.x) corr[i] = mas_corr_f(freq_of(i, dims), dims, mas);
     if (INTER) {
         for (int i = threadIdx.x; i < dims; i += blockDim.x) {
             float s, c;
@@ -412,7 +433,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m2 = d.middle * d.middle;
-    double *P3 = a.sums;
+    double *P3 = sums;
     double *PH = P3 + (long long)d.nb3 * 3;
     double *P1 = PH + d.nb3;
     double *P2 = P1 + d.nb1;
@@ -421,7 +442,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     float *w1 = w2 + nz;
     const int kz_begin = lane * chunk;
     const int kz_end = min(nz, kz_begin + chunk);
-    float *part = a.part ? a.part + (long long)blockIdx.x * a.part_stride : nullptr;
+    float *part = part_base ? part_base + (long long)blockIdx.x * a.part_stride : nullptr;
     float r1 = 0.0f;
     int cur_ring = -1;
 
@@ -455,9 +476,9 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
         // pass 1: per-mode power and phase^2, coalesced along kz
 #pragma unroll 2
         for (int kz = lane; kz < nz; kz += 32) {
-            float2 v = __ldg(a.dk + row + kz);
+            float2 v = __ldg(dk + row + kz);
             if (INTER) {
-                const float2 w = __ldg(a.dk2 + row + kz);
+                const float2 w = __ldg(dk2 + row + kz);
                 const float2 t = ph[kz];
                 const float2 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
                 v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
@@ -578,10 +599,16 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
 // blockIdx.y splits the CTAs into groups, each thread sums one slot over its
 // group in float64.  k_per slots (axes 0/1): each CTA's plane fixes k_par, so a
 // thread per (CTA, k_per) adds its value where it belongs.
+// With items, blockIdx.z is the item: its sums, and its n_cta x stride slice of part.
 __global__ void __launch_bounds__(256) pk_part_reduce_kernel(const float *__restrict__ part, int n_cta,
                                                              int stride, int per_group, int chunks, int axis,
-                                                             PkDims d, double *__restrict__ sums)
+                                                             PkDims d, double *__restrict__ sums,
+                                                             const pyl_pk_item *__restrict__ items)
 {
+    if (items) {
+        sums = items[blockIdx.z].sums;
+        part += (long long)blockIdx.z * n_cta * stride;
+    }
     double *P3 = sums, *PH = P3 + (long long)d.nb3 * 3;
     double *P2 = PH + d.nb3 + d.nb1;
     const int n3 = d.nb3 * 4;
@@ -604,6 +631,13 @@ __global__ void __launch_bounds__(256) pk_part_reduce_kernel(const float *__rest
             atomicAdd(P2 + (long long)(d.kmax_par + 1) * kper + kpar, (double)v);
         }
     }
+}
+
+// Zeroes every item's sums (blockIdx.x = item).
+__global__ void __launch_bounds__(256) pk_items_zero_kernel(const pyl_pk_item *__restrict__ items, long long len)
+{
+    double *s = items[blockIdx.x].sums;
+    for (long long i = threadIdx.x; i < len; i += blockDim.x) s[i] = 0.0;
 }
 
 // Data-independent per-bin sums with the same traversal: N3 and K3 = sum |k|
@@ -853,6 +887,7 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     a.rows = nullptr;
     a.part = nullptr;
     a.part_stride = 0;
+    a.items = nullptr;
     for (int f = 0; f < MAX_FIELDS; f++) {
         a.mas_p[f] = f < n_fields ? host_mas_p[f] : 0;
         PYL_CHECK_ARG(a.mas_p[f] >= 0 && a.mas_p[f] <= 4, "MAS exponent must be 0..4");
@@ -898,8 +933,8 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
             }
 #define PYL_SEQ(I, A)                                                              \
     do {                                                                           \
-        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A>, sms));                \
-        pk_bin_seq_kernel<I, A><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
+        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A, false>, sms));         \
+        pk_bin_seq_kernel<I, A, false><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
             if (inter) {
                 if (axis == 0) PYL_SEQ(true, 0); else if (axis == 1) PYL_SEQ(true, 1); else PYL_SEQ(true, 2);
@@ -912,7 +947,7 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
                 const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
                 const int groups = 16, per_group = (int)((blocks + groups - 1) / groups);
                 pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups), 256, 0, st>>>(
-                    a.part, (int)blocks, sp.stride, per_group, a.chunks, axis, d, sums);
+                    a.part, (int)blocks, sp.stride, per_group, a.chunks, axis, d, sums, nullptr);
                 PYL_LAUNCH_CHECK();
             }
             return PYL_OK;
@@ -949,6 +984,99 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     return PYL_OK;
 }
 
+// Whether the one-field kernel's shared memory holds this grid's bins.
+bool batch_fits(const PkDims &d, int axis, bool inter)
+{
+    if (axis == 2 && sizeof(float) * bin_smem(d, 1, 1, axis, inter, 1).total > SMEM_LIMIT) return false;
+    return sizeof(float) * (size_t)seq_smem(d, axis, inter, seq_chunk(d.nz), true).total <= SMEM_LIMIT;
+}
+
+// Batched one-field spectra: the axis-2 row table, then each item's per-CTA
+// partial sums (the one-field call's CTA partition).  0: not batchable.
+extern "C" size_t pyl_pk_bin_batch_workspace_size(int dims, int n_items, int axis, int interlaced)
+{
+    if (dims < 2 || dims > 8192 || n_items < 1 || axis < 0 || axis > 2) return 0;
+    const PkDims d = pk_dims(dims);
+    if (!batch_fits(d, axis, interlaced != 0)) return 0;
+    const SeqPart sp = seq_part(d, axis);
+    return (axis == 2 ? ring_layout(nullptr, d).bytes : 0) +
+           align256(sizeof(float) * (size_t)sp.blocks * sp.stride * (size_t)n_items);
+}
+
+extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims, int axis, int interlaced,
+                                void *workspace, size_t workspace_bytes, void *stream)
+{
+    PYL_CHECK_ARG(items != nullptr, "null pointer");
+    PYL_CHECK_ARG(dims >= 2 && dims <= 8192, "dims out of range");
+    PYL_CHECK_ARG(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+    PYL_CHECK_ARG(n_items >= 1 && n_items <= 65535, "1..65535 items per call");
+    const PkDims d = pk_dims(dims);
+    const bool inter = interlaced != 0;
+    if (!batch_fits(d, axis, inter)) {
+        set_error("pyl_pk_bin_batch: this grid's bins exceed the one-field kernel's shared memory");
+        return PYL_ERR_UNSUPPORTED;
+    }
+    const size_t need = pyl_pk_bin_batch_workspace_size(dims, n_items, axis, interlaced);
+    if (workspace == nullptr || workspace_bytes < need) {
+        set_error("pyl_pk_bin_batch: needs " + std::to_string(need) + " workspace bytes");
+        return PYL_ERR_WORKSPACE;
+    }
+    const int chunk = seq_chunk(d.nz);
+    const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk, true).total;
+    BinArgs a;
+    a.dk = a.dk2 = nullptr;
+    a.fstride = 0;
+    a.F = a.C = 1;
+    a.axis = axis;
+    a.sums = nullptr;
+    a.geom = nullptr;
+    a.d = d;
+    a.rows = nullptr;
+    a.items = items;
+    for (int f = 0; f < MAX_FIELDS; f++) a.mas_p[f] = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const SeqPart sp = seq_part(d, axis);
+    size_t ring_bytes = 0;
+    if (axis == 2) {
+        const RingWs w = ring_layout(workspace, d);
+        ring_bytes = w.bytes;
+        int rc = build_rings(d, w, st);
+        if (rc) return rc;
+        a.rows = w.rows;
+        a.rows_per_cta = RING_ROWS_PER_CTA;
+        a.chunks = 1;
+        a.warp_arrays = 1;
+    } else {
+        a.chunks = seq_plane_chunks(dims);
+        a.rows_per_cta = 0;
+        a.warp_arrays = 0;
+    }
+    a.part = (float *)((char *)workspace + ring_bytes);
+    a.part_stride = sp.stride;
+    pk_items_zero_kernel<<<n_items, 256, 0, st>>>(items, pyl_pk_sums_len(dims, 1));
+    PYL_LAUNCH_CHECK();
+    PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride * n_items, st));
+    const dim3 grid(sp.blocks, (unsigned)n_items);
+#define PYL_SEQB(I, A)                                                             \
+    do {                                                                           \
+        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A, true>, sms));          \
+        pk_bin_seq_kernel<I, A, true><<<grid, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
+    } while (0)
+    if (inter) {
+        if (axis == 0) PYL_SEQB(true, 0); else if (axis == 1) PYL_SEQB(true, 1); else PYL_SEQB(true, 2);
+    } else {
+        if (axis == 0) PYL_SEQB(false, 0); else if (axis == 1) PYL_SEQB(false, 1); else PYL_SEQB(false, 2);
+    }
+#undef PYL_SEQB
+    PYL_LAUNCH_CHECK();
+    const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
+    const int groups = 16, per_group = (int)((sp.blocks + groups - 1) / groups);
+    pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups, (unsigned)n_items), 256, 0, st>>>(
+        a.part, (int)sp.blocks, sp.stride, per_group, a.chunks, axis, d, nullptr, items);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
 extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t workspace_bytes,
                                void *stream)
 {
@@ -968,6 +1096,7 @@ extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace
     a.rows = nullptr;
     a.part = nullptr;
     a.part_stride = 0;
+    a.items = nullptr;
     for (int f = 0; f < MAX_FIELDS; f++) a.mas_p[f] = 0;
     unsigned blocks;
     if (axis == 2) {

@@ -76,6 +76,24 @@ def test_pk_rejects_bad_arguments(lib):
     assert lib.pyl_pk_bin(buf, None, 1, 0, 32, 0, bad, buf, None, 0, None) == 1
 
 
+def test_pk_batch_sizes_and_arguments(lib):
+    lib.pyl_pk_bin_batch_workspace_size.restype = ctypes.c_size_t
+    size = lib.pyl_pk_bin_batch_workspace_size
+    # per-item partial sums grow with the item count; axis 2 adds the row table
+    one, two = size(64, 1, 0, 1), size(64, 2, 0, 1)
+    assert 0 < one < two
+    assert size(64, 2, 2, 0) > 0
+    # 0: not batchable (bad sizes, or bins beyond the one-field kernel's shared memory)
+    assert size(1, 4, 0, 0) == 0 and size(64, 0, 0, 0) == 0 and size(64, 4, 3, 0) == 0
+    assert size(8192, 1, 0, 1) == 0
+    buf = ctypes.c_void_p(16)
+    assert lib.pyl_pk_bin_batch(None, 4, 64, 0, 0, buf, 1 << 30, None) == 1
+    assert lib.pyl_pk_bin_batch(buf, 0, 64, 0, 0, buf, 1 << 30, None) == 1
+    assert lib.pyl_pk_bin_batch(buf, 4, 64, 0, 0, buf, 16, None) == 4
+    assert 'workspace' in lib.pyl_last_error().decode()
+    assert lib.pyl_pk_bin_batch(buf, 4, 8192, 0, 1, buf, 1 << 30, None) == 5
+
+
 def test_bk_rejects_bad_arguments(lib):
     buf = ctypes.c_void_p(16)
     lo = (ctypes.c_int64 * 1)(1)
@@ -87,6 +105,16 @@ def test_bk_rejects_bad_arguments(lib):
     assert lib.pyl_bk_shell_fill(buf, 64, 80, lo, hi, 1, buf, buf, buf, None) == 1
     tri = (ctypes.c_int * 3)(0, 0, 5)
     assert lib.pyl_bk_triangles(buf, buf, 16, 4096, 2, tri, 1, buf, buf, None) == 1
+    # either field set may be omitted, not both; each set needs its sum buffer
+    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, 1, None, None, buf, None) == 1
+    assert 'no output' in lib.pyl_last_error().decode()
+    assert lib.pyl_bk_shell_fill(None, 64, 64, lo, hi, 1, buf, None, buf, None) == 1
+    assert 'need dk' in lib.pyl_last_error().decode()
+    tri = (ctypes.c_int * 3)(0, 0, 1)
+    assert lib.pyl_bk_triangles(None, None, 16, 4096, 2, tri, 1, buf, buf, None) == 1
+    assert lib.pyl_bk_triangles(buf, None, 16, 4096, 2, tri, 1, None, buf, None) == 1
+    assert 'sum buffer' in lib.pyl_last_error().decode()
+    assert lib.pyl_bk_triangles(None, buf, 16, 4096, 2, tri, 1, buf, None, None) == 1
 
 
 def test_python_facade_errors_without_gpu():

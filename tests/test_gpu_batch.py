@@ -62,3 +62,40 @@ def test_autotune_cache_written(mods):
     assert k in autotune.ITEM_CANDIDATES
     assert os.path.exists(os.environ['PYL_AUTOTUNE_CACHE'])
     assert autotune.item_size(48, 50000, 'TSC', True, tune=False) == k
+
+
+@pytest.mark.parametrize('axis', [0, 1, 2])
+@pytest.mark.parametrize('inter', [False, True])
+def test_pk_bin_batch_equals_one_field_calls(mods, axis, inter):
+    """pyl_pk_bin_batch bins each item with the one-field call's CTA partition and
+    float32 partial sums: item by item the float64 sums agree with pyl_pk_bin up to
+    the order of the float64 atomics."""
+    import ctypes
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr
+    from pylians_gb300.batch import PK_ITEM_DT
+    L = _lib.load()
+    dims, n = 48, 5
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(11 + axis + 3 * inter)
+    shape = (n, dims, dims, dims // 2 + 1)
+    dk = torch.complex(torch.randn(shape, generator=gen, device='cuda'), torch.randn(shape, generator=gen, device='cuda'))
+    dk2 = torch.complex(torch.randn(shape, generator=gen, device='cuda'), torch.randn(shape, generator=gen, device='cuda'))
+    mas = [1, 2, 3, 4, 2]
+    slen = L.pyl_pk_sums_len(dims, 1)
+    one = torch.zeros((n, slen), dtype=torch.float64, device='cuda')
+    ws = torch.empty(max(L.pyl_pk_workspace_size(dims, 1, axis), 1), dtype=torch.uint8, device='cuda')
+    for i in range(n):
+        mp = (ctypes.c_int * 1)(mas[i])
+        _lib.call('pyl_pk_bin', ptr(dk[i]), ptr(dk2[i]) if inter else None, 1, dk[0].numel(), dims, axis, mp,
+                  ptr(one[i]), ptr(ws), ws.numel(), None)
+    many = torch.full((n, slen), 7.0, dtype=torch.float64, device='cuda')    # zeroed by the call
+    rec = np.zeros(n, dtype=PK_ITEM_DT)
+    for i in range(n):
+        rec[i] = (dk[i].data_ptr(), dk2[i].data_ptr() if inter else 0, many[i].data_ptr(), mas[i], 0)
+    table = torch.from_numpy(rec.view(np.uint8)).cuda()
+    nb = L.pyl_pk_bin_batch_workspace_size(dims, n, axis, int(inter))
+    wsb = torch.empty(nb, dtype=torch.uint8, device='cuda')
+    _lib.call('pyl_pk_bin_batch', ptr(table), n, dims, axis, int(inter), ptr(wsb), nb, None)
+    a, b = many.cpu().numpy(), one.cpu().numpy()
+    assert np.all(np.abs(a - b) <= 1e-12 * np.abs(b).max(axis=1, keepdims=True))
