@@ -237,8 +237,9 @@ int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t wo
  * is a DEVICE array of n_items records, each one pyl_pk_bin call with n_fields = 1:
  * its field, its interlaced partner (non-NULL in every record when `interlaced`,
  * ignored otherwise), its own zeroed-by-the-call `sums` (pyl_pk_sums_len(dims, 1)
- * doubles) and MAS exponent.  The sums equal pyl_pk_bin's item by item (the same
- * CTA partition and float32 partial sums; float64 atomics in another order).  The
+ * doubles) and MAS exponent.  The sums agree with pyl_pk_bin's item by item to
+ * float32 rounding (the same CTA partition and float32 partial sums, whose float
+ * atomics run in no fixed order in either call).  The
  * workspace (pyl_pk_bin_batch_workspace_size bytes) holds the axis-2 row table and
  * every item's per-CTA partial sums.  A workspace size of 0, and
  * PYL_ERR_UNSUPPORTED from the call, mean that one field's bins do not fit the

@@ -9,6 +9,7 @@ P(k) mode loop); this file restates the rest in numpy, each part citing the
 reference lines it follows:
 
   MA()                MAS_library.pyx:57-112 (dispatch, 2D renormalisation)
+  ma_acc64()          the same weights summed in float64 (no accumulation rounding)
   ma_f64()            CICW_d MAS_library.pyx:229-266, NGPW_d :338-358 (float64 grids)
   frequencies()       Pk_library.pyx:59-64
   MAS_function()      Pk_library.pyx:75-81
@@ -65,6 +66,8 @@ def lib():
         L.oracle_ma.argtypes = [P, ctypes.c_int64, ctypes.c_int, P, ctypes.c_int, ctypes.c_float,
                                 ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
         L.oracle_ma.restype = ctypes.c_int
+        L.oracle_ma_acc64.argtypes = L.oracle_ma.argtypes
+        L.oracle_ma_acc64.restype = ctypes.c_int
         L.oracle_pk_modes.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int] + [P] * 12
         L.oracle_pk_modes.restype = ctypes.c_int
         L.oracle_cic_interp.argtypes = [P, ctypes.c_int, ctypes.c_float, P, ctypes.c_int64, P]
@@ -96,6 +99,18 @@ def ma_kernel(pos, number, BoxSize, MAS, W=None, threads=1, flavor=0):
                          float(BoxSize), MAS_INDEX[MAS], _ptr(w), int(threads), int(flavor))
     if rc:
         raise ValueError('oracle_ma failed (%d)' % rc)
+
+
+def ma_acc64(pos, number, BoxSize, MAS, W=None, threads=1):
+    """ma_kernel (flavor 0, 3D) with the reference's float32 weights and products added
+    to the float64 grid ``number``: no float32 accumulation rounding."""
+    assert pos.dtype == np.float32 and pos.flags.c_contiguous and pos.shape[1] == 3
+    assert number.dtype == np.float64 and number.flags.c_contiguous and number.ndim == 3
+    w = None if W is None else np.ascontiguousarray(W, dtype=np.float32)
+    rc = lib().oracle_ma_acc64(_ptr(pos), pos.shape[0], 3, _ptr(number), number.shape[0], float(BoxSize),
+                               MAS_INDEX[MAS], _ptr(w), int(threads), 0)
+    if rc:
+        raise ValueError('oracle_ma_acc64 failed (%d)' % rc)
 
 
 def ma_f64(pos, number, BoxSize, MAS, W):

@@ -36,9 +36,16 @@
 
 static inline int wrap(int i, int n) { int r = i % n; return r < 0 ? r + n : r; }
 
-static inline void add_cell(float *grid, int64_t idx, float v, int atomic)
+static inline void add_cell(float *grid, double *grid64, int64_t idx, float v, int atomic)
 {
-    if (atomic) {
+    if (grid64) {
+        if (atomic) {
+#pragma omp atomic
+            grid64[idx] += (double)v;
+        } else {
+            grid64[idx] += (double)v;
+        }
+    } else if (atomic) {
 #pragma omp atomic
         grid[idx] += v;
     } else {
@@ -54,8 +61,8 @@ static inline void add_cell(float *grid, int64_t idx, float v, int atomic)
  *           one deposit per (l,m).
  * mas: 1 NGP, 2 CIC, 3 TSC, 4 PCS.   ndim: 2 or 3.   w may be NULL.
  */
-int oracle_ma(const float *pos, int64_t n, int ndim, float *grid, int dims,
-              float box, int mas, const float *w, int threads, int flavor)
+static int ma_any(const float *pos, int64_t n, int ndim, float *grid, double *grid64, int dims,
+                  float box, int mas, const float *w, int threads, int flavor)
 {
     if (ndim != 2 && ndim != 3) return 1;
     if (mas < 1 || mas > 4) return 2;
@@ -119,7 +126,7 @@ int oracle_ma(const float *pos, int64_t n, int ndim, float *grid, int dims,
         }
         if (mas == 1) {
             int64_t cell = idx[0][0] * sa + idx[1][0] * sb + idx[2][0] * sc;
-            add_cell(grid, cell, w ? w[i] : 1.0f, atomic);
+            add_cell(grid, grid64, cell, w ? w[i] : 1.0f, atomic);
             continue;
         }
         for (int l = 0; l < support; l++)
@@ -129,10 +136,28 @@ int oracle_ma(const float *pos, int64_t n, int ndim, float *grid, int dims,
                     float v = C[0][l] * C[1][m];
                     v = v * C[2][q];
                     if (w) v = v * w[i];
-                    add_cell(grid, cell, v, atomic);
+                    add_cell(grid, grid64, cell, v, atomic);
                 }
     }
     return 0;
+}
+
+int oracle_ma(const float *pos, int64_t n, int ndim, float *grid, int dims,
+              float box, int mas, const float *w, int threads, int flavor)
+{
+    return ma_any(pos, n, ndim, grid, NULL, dims, box, mas, w, threads, flavor);
+}
+
+/*
+ * oracle_ma with the same float32 weights and products added to a float64 grid:
+ * the reference's arithmetic without its float32 accumulation rounding (one ulp
+ * of the cell value per add, which the MAS deconvolution amplifies near the
+ * Nyquist corner).  For comparisons whose error budget is the tested path's own.
+ */
+int oracle_ma_acc64(const float *pos, int64_t n, int ndim, double *grid, int dims,
+                    float box, int mas, const float *w, int threads, int flavor)
+{
+    return ma_any(pos, n, ndim, NULL, grid, dims, box, mas, w, threads, flavor);
 }
 
 /*

@@ -95,6 +95,22 @@ def test_ma_openmp_matches_serial(ma):
     np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize('mas', ['NGP', 'CIC', 'TSC', 'PCS'])
+def test_ma_acc64_matches_golden(ma, mas):
+    """The float64-sum oracle keeps the reference's weights: its grid, rounded to
+    float32, matches the compiled reference's within float32 accumulation rounding
+    (NGP counts exactly)."""
+    pos = ma['grid_pos']
+    N, L = int(ma['grid_meta'][0]), float(ma['grid_meta'][1])
+    g = np.zeros((N, N, N), np.float64)
+    O.ma_acc64(pos, g, L, mas, threads=4)
+    ref = ma['MA3D_%s' % mas]
+    if mas == 'NGP':
+        np.testing.assert_array_equal(g.astype(np.float32), ref)
+    else:
+        assert np.abs(g - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
 def _cmp_attr(x, y, name):
     x = np.asarray(x); y = np.asarray(y)
     assert x.shape == y.shape, name
