@@ -595,6 +595,216 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     }
 }
 
+// ---- axes 0/1: the four sign rows of a (|k_plane|, |k_row|) pair at once ----------
+// With the line of sight along x (axis 0) a CTA's plane fixes |kx| = p and a row
+// fixes |ky| = q; every bin index (|k| from p^2 + q^2 + kz^2, k_per from q^2 + kz^2),
+// mu^2 = p^2 / k^2 and the 1D test depend on p^2 and q^2 only, so the rows
+// (+-kx, +-ky) have the same bins at every kz (axis 1: x and y swapped).  CTA
+// blockIdx.x / chunks takes plane representative p in [0, dims/2] (planes p and
+// dims - p), a warp row representative q (rows q and dims - q): pass 1 sums the
+// (up to four) modes' |d|^2 and phase^2 at each kz, pass 2 walks the bins once for
+// all of them.  The bin walk, its flushes and the staging are a quarter of the
+// one-row-at-a-time kernel's; the loads and per-mode arithmetic are the same.
+// Each mode's power is |v|^2 (mf)^2 with mf the deconvolution factor, shared by the
+// four modes; phase = atan(Re v / |v|) does not depend on mf > 0.
+__host__ __device__ inline int sym_groups(int dims) { return dims / 2 + 1; }
+
+template <bool INTER, int AXIS, bool BATCH>
+__global__ void __launch_bounds__(256) pk_bin_sym_kernel(BinArgs a, int chunk, unsigned chunk_magic)
+{
+    static_assert(AXIS == 0 || AXIS == 1, "axes 0 and 1");
+    extern __shared__ float sm[];
+    const PkDims d = a.d;
+    const int dims = d.dims, nz = d.nz;
+    const SeqSmem L = seq_smem(d, AXIS, INTER, chunk, a.part != nullptr);
+    const float2 *bdk = nullptr, *bdk2 = nullptr;
+    double *bsums = nullptr;
+    int bmas = 0;
+    if (BATCH) {
+        const pyl_pk_item it = a.items[blockIdx.y];
+        bdk = (const float2 *)it.dk;
+        bdk2 = (const float2 *)it.dk_interlaced;
+        bsums = it.sums;
+        bmas = it.mas_p;
+    }
+    const float2 *dk = BATCH ? bdk : a.dk;
+    const float2 *dk2 = BATCH ? bdk2 : a.dk2;
+    double *sums = BATCH ? bsums : a.sums;
+    const int mas = BATCH ? bmas : a.mas_p[0];
+    float *part_base = (BATCH && a.part) ? a.part + (long long)blockIdx.y * gridDim.x * a.part_stride : a.part;
+    float *corr = sm + L.corr;
+    float2 *ph = (float2 *)(sm + L.ph);
+    float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
+    for (int i = threadIdx.x; i < dims; i += blockDim.x) corr[i] = mas_corr_f(freq_of(i, dims), dims, mas);
+    if (INTER) {
+        for (int i = threadIdx.x; i < dims; i += blockDim.x) {
+            float sn, cs;
+            sincospif((float)freq_of(i, dims) / (float)dims, &sn, &cs);
+            ph[i] = make_float2(cs, sn);
+        }
+    }
+    for (int i = L.acc3 + threadIdx.x; i < L.stage; i += blockDim.x) sm[i] = 0.0f;
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m2 = d.middle * d.middle;
+    double *P3 = sums;
+    double *PH = P3 + (long long)d.nb3 * 3;
+    double *P1 = PH + d.nb3;
+    double *P2 = P1 + d.nb1;
+    float2 *stage = (float2 *)(sm + L.stage) + warp * 32 * (chunk + 1);
+    const int kz_begin = lane * chunk;
+    const int kz_end = min(nz, kz_begin + chunk);
+    float *part = part_base ? part_base + (long long)blockIdx.x * a.part_stride : nullptr;
+    float r1 = 0.0f;
+    const bool even = (dims & 1) == 0;
+
+    const int G = sym_groups(dims);
+    const int p = blockIdx.x / a.chunks;                 // |k_par|
+    const int cid = blockIdx.x % a.chunks;
+    const int per = (G + a.chunks - 1) / a.chunks;
+    const int q0 = cid * per, q1 = min(G, q0 + per);
+    const int np = (p == 0 || 2 * p == dims) ? 1 : 2;
+    for (int q = q0 + warp; q < q1; q += NW) {
+        const int nq = (q == 0 || 2 * q == dims) ? 1 : 2;
+        // the physical rows: plane index p or dims - p, row index q or dims - q
+        long long off[4];
+        float2 pxy[4];
+        unsigned skip0 = 0u, skipm = 0u;                 // Hermitian skips on the kz = 0 / N/2 planes
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            // unused sign choices (np or nq of 1) repeat the representative, in range
+            const int pi = ((r & 1) && np == 2) ? dims - p : p, qi = ((r & 2) && nq == 2) ? dims - q : q;
+            const int kxx = AXIS == 0 ? pi : qi, kyy = AXIS == 0 ? qi : pi;
+            off[r] = ((long long)kxx * dims + kyy) * nz;
+            const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
+            pxy[r] = make_float2(1.0f, 0.0f);
+            if (INTER) {
+                const float2 px = ph[kxx], py = ph[kyy];
+                pxy[r] = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
+            }
+            if (hermitian_skip(kx, ky, 0, d)) skip0 |= 1u << r;
+            if (even && hermitian_skip(kx, ky, d.middle, d)) skipm |= 1u << r;
+        }
+        // rows r = (row sign << 1) | plane sign; a sign choice of a representative
+        // with no partner (0 or dims/2) is not used (its row repeats one that is)
+        const unsigned used = 1u | (np == 2 ? 2u : 0u) | (nq == 2 ? 4u : 0u) | (np == 2 && nq == 2 ? 8u : 0u);
+        const float cxy = __fmul_rn(corr[p], corr[q]);
+        // pass 1: the summed |d|^2 and phase^2 of the rows at each kz, coalesced along
+        // kz; all four rows are loaded (in range for every sign choice), so the loads
+        // of an iteration are issued together
+#pragma unroll 2
+        for (int kz = lane; kz < nz; kz += 32) {
+            float2 t = make_float2(1.0f, 0.0f);
+            if (INTER) t = ph[kz];
+            const unsigned skip = kz == 0 ? skip0 : ((even && kz == d.middle) ? skipm : 0u);
+            const unsigned take = used & ~skip;
+            float2 v[4], w[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                v[r] = __ldg(dk + off[r] + kz);
+                if (INTER) w[r] = __ldg(dk2 + off[r] + kz);
+            }
+            float a2s = 0.0f, p2s = 0.0f;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                float2 u = v[r];
+                if (INTER) {
+                    const float2 pz = make_float2(pxy[r].x * t.x - pxy[r].y * t.y, pxy[r].x * t.y + pxy[r].y * t.x);
+                    u.x = 0.5f * (u.x + (w[r].x * pz.x - w[r].y * pz.y));
+                    u.y = 0.5f * (u.y + (w[r].x * pz.y + w[r].y * pz.x));
+                }
+                const float a2 = u.x * u.x + u.y * u.y;
+                const float phase = a2 > 0.0f ? atan_unit(u.x * rsqrtf(a2)) : 0.0f;
+                if ((take >> r) & 1u) {
+                    a2s += a2;
+                    p2s += phase * phase;
+                }
+            }
+            const float mf = __fmul_rn(cxy, corr[kz]);
+            stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(a2s * (mf * mf), p2s);
+        }
+        __syncwarp();
+        // pass 2: this lane's run of kz, sums kept while the bins stay the same
+        if (kz_begin < kz_end) {
+            const int kperp2 = q * q;               // k_per^2 - kz^2
+            const int kxy2 = p * p + q * q;
+            int kz = kz_begin;
+            int n2 = kxy2 + kz * kz;
+            int ki = isqrt_exact(n2);
+            int kp2 = kperp2 + kz * kz;
+            int kper = isqrt_exact(kp2);
+            const float kpar2f = (float)(p * p);
+            float s0 = 0.0f, s2 = 0.0f, s4 = 0.0f, sp = 0.0f, sd = 0.0f;
+            const float2 *run = stage + lane * (chunk + 1);
+            for (; kz < kz_end; kz++) {
+                const float2 e = run[kz - kz_begin];
+                const float val = e.x;
+                const float mu2 = n2 ? __fdividef(kpar2f, (float)n2) : 0.0f;
+                const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
+                const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
+                s0 += val;
+                s2 += val * l2;
+                s4 += val * l4;
+                sp += e.y;
+                sd += val;
+                if (n2 <= m2) r1 += val;
+                const int dn = 2 * kz + 1;
+                n2 += dn;
+                const bool new3 = (ki + 1) * (ki + 1) <= n2;
+                kp2 += dn;
+                const bool new2 = (kper + 1) * (kper + 1) <= kp2;
+                if (new3 || kz + 1 == kz_end) {
+                    if (part) {
+                        atomicAdd(reinterpret_cast<float4 *>(part + ki * 4), make_float4(s0, s2, s4, sp));
+                    } else {
+                        float *b3 = acc3 + ki * 4;
+                        if (s0 != 0.0f) atomicAdd(b3, s0);
+                        if (s2 != 0.0f) atomicAdd(b3 + 1, s2);
+                        if (s4 != 0.0f) atomicAdd(b3 + 2, s4);
+                        if (sp != 0.0f) atomicAdd(b3 + 3, sp);
+                    }
+                    s0 = s2 = s4 = sp = 0.0f;
+                    ki += new3 ? 1 : 0;
+                }
+                if (new2 || kz + 1 == kz_end) {
+                    if (part) atomicAdd(part + d.nb3 * 4 + kper, sd);
+                    else if (sd != 0.0f) atomicAdd(acc2 + kper, sd);
+                    sd = 0.0f;
+                    kper += new2 ? 1 : 0;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    {
+        float v = r1;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(acc1 + p, v);
+    }
+    __syncthreads();
+    if (!part) {
+        for (int i = threadIdx.x; i < d.nb3 * 4; i += blockDim.x) {
+            const float v = acc3[i];
+            if (v == 0.0f) continue;
+            const int bin = i >> 2, s = i & 3;
+            if (s < 3) atomicAdd(P3 + (long long)bin * 3 + s, (double)v);
+            else atomicAdd(PH + bin, (double)v);
+        }
+    }
+    for (int i = threadIdx.x; i < d.nb1; i += blockDim.x) {
+        const float v = acc1[i];
+        if (v != 0.0f) atomicAdd(P1 + i, (double)v);
+    }
+    if (!part) {
+        for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) {
+            const float v = acc2[i];
+            if (v == 0.0f) continue;
+            atomicAdd(P2 + (long long)(d.kmax_par + 1) * i + p, (double)v);
+        }
+    }
+}
+
 // Per-CTA partial sums of pk_bin_seq_kernel into the float64 sums.  3D slots:
 // blockIdx.y splits the CTAs into groups, each thread sums one slot over its
 // group in float64.  k_per slots (axes 0/1): each CTA's plane fixes k_par, so a
@@ -627,7 +837,7 @@ __global__ void __launch_bounds__(256) pk_part_reduce_kernel(const float *__rest
         for (int c = c0; c < c1; c++) {
             const float v = part[(long long)c * stride + s];
             if (v == 0.0f) continue;
-            const int kpar = abs(freq_of(c / chunks, d.dims));
+            const int kpar = c / chunks;        // pk_bin_sym_kernel: CTA c holds plane |k_par| = c / chunks
             atomicAdd(P2 + (long long)(d.kmax_par + 1) * kper + kpar, (double)v);
         }
     }
@@ -818,26 +1028,27 @@ inline int plane_chunks(int dims)
 constexpr int RING_ROWS_PER_CTA = 256;
 constexpr size_t SMEM_LIMIT = 200 * 1024;
 
-// One-field launches (pk_bin_seq_kernel): axes 0/1 give each plane c CTAs, enough
-// for several waves at 2-3 resident CTAs per SM; axis 2 walks the ring table.
-inline int seq_plane_chunks(int dims)
-{
-    int c = 1;
-    while ((long long)dims * c < 8LL * num_sms() && c * 2 * NW <= dims) c *= 2;
-    return c;
-}
-
 struct SeqPart {
     unsigned blocks;
     int stride;           // floats per CTA (a multiple of 4: float4 slots stay aligned)
     size_t bytes;
 };
 
+// Axes 0/1 (pk_bin_sym_kernel): CTAs per plane representative, several waves at
+// 2-3 resident CTAs per SM and at least two row representatives per warp.
+inline int sym_chunks(int dims)
+{
+    const int G = sym_groups(dims);
+    int c = 1;
+    while ((long long)G * c < 8LL * num_sms() && c * NW * 2 <= G) c *= 2;
+    return c;
+}
+
 inline SeqPart seq_part(const PkDims &d, int axis)
 {
     SeqPart p;
     p.blocks = axis == 2 ? (unsigned)(((long long)d.dims * d.dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA)
-                         : (unsigned)(d.dims * seq_plane_chunks(d.dims));
+                         : (unsigned)(sym_groups(d.dims) * sym_chunks(d.dims));
     p.stride = (d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1) + 3) & ~3;
     p.bytes = align256(sizeof(float) * (size_t)p.blocks * p.stride);
     return p;
@@ -917,8 +1128,8 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     if (n_fields == 1 && (axis != 2 || a.warp_arrays)) {
         const int chunk = seq_chunk(d.nz);
         if (axis != 2) {
-            a.chunks = seq_plane_chunks(dims);
-            blocks = (unsigned)(dims * a.chunks);
+            a.chunks = sym_chunks(dims);
+            blocks = (unsigned)(sym_groups(dims) * a.chunks);
         }
         const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
         const SeqPart sp = seq_part(d, axis);
@@ -931,15 +1142,19 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
                 a.part = (float *)((char *)workspace + ring_bytes);
                 PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride, st));
             }
-#define PYL_SEQ(I, A)                                                              \
+#define PYL_SEQ(K, I, A)                                                           \
     do {                                                                           \
-        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A, false>, sms));         \
-        pk_bin_seq_kernel<I, A, false><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
+        PYL_CUDA(ensure_smem(K<I, A, false>, sms));                         \
+        K<I, A, false><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
             if (inter) {
-                if (axis == 0) PYL_SEQ(true, 0); else if (axis == 1) PYL_SEQ(true, 1); else PYL_SEQ(true, 2);
+                if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, true, 0);
+                else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, true, 1);
+                else PYL_SEQ(pk_bin_seq_kernel, true, 2);
             } else {
-                if (axis == 0) PYL_SEQ(false, 0); else if (axis == 1) PYL_SEQ(false, 1); else PYL_SEQ(false, 2);
+                if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, false, 0);
+                else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, false, 1);
+                else PYL_SEQ(pk_bin_seq_kernel, false, 2);
             }
 #undef PYL_SEQ
             PYL_LAUNCH_CHECK();
@@ -1047,7 +1262,7 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
         a.chunks = 1;
         a.warp_arrays = 1;
     } else {
-        a.chunks = seq_plane_chunks(dims);
+        a.chunks = sym_chunks(dims);
         a.rows_per_cta = 0;
         a.warp_arrays = 0;
     }
@@ -1057,15 +1272,19 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
     PYL_LAUNCH_CHECK();
     PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride * n_items, st));
     const dim3 grid(sp.blocks, (unsigned)n_items);
-#define PYL_SEQB(I, A)                                                             \
+#define PYL_SEQB(K, I, A)                                                          \
     do {                                                                           \
-        PYL_CUDA(ensure_smem(pk_bin_seq_kernel<I, A, true>, sms));          \
-        pk_bin_seq_kernel<I, A, true><<<grid, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
+        PYL_CUDA(ensure_smem(K<I, A, true>, sms));                          \
+        K<I, A, true><<<grid, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
     if (inter) {
-        if (axis == 0) PYL_SEQB(true, 0); else if (axis == 1) PYL_SEQB(true, 1); else PYL_SEQB(true, 2);
+        if (axis == 0) PYL_SEQB(pk_bin_sym_kernel, true, 0);
+        else if (axis == 1) PYL_SEQB(pk_bin_sym_kernel, true, 1);
+        else PYL_SEQB(pk_bin_seq_kernel, true, 2);
     } else {
-        if (axis == 0) PYL_SEQB(false, 0); else if (axis == 1) PYL_SEQB(false, 1); else PYL_SEQB(false, 2);
+        if (axis == 0) PYL_SEQB(pk_bin_sym_kernel, false, 0);
+        else if (axis == 1) PYL_SEQB(pk_bin_sym_kernel, false, 1);
+        else PYL_SEQB(pk_bin_seq_kernel, false, 2);
     }
 #undef PYL_SEQB
     PYL_LAUNCH_CHECK();
