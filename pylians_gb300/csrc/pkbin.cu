@@ -390,12 +390,105 @@ inline int seq_chunk(int nz)
 inline unsigned seq_chunk_magic(int chunk) { return (unsigned)((0x100000000ull + chunk - 1) / chunk); }
 
 
+// ---- the four sign rows of a representative (|kx|, |ky|) ----------------------------
+// Every bin index (|k|^2 = kx^2 + ky^2 + kz^2, k_per^2, k_par^2 for any line of
+// sight) and every Legendre weight depends on kx^2 and ky^2 only, so the rows
+// (+-kx, +-ky) share their bins at every kz: the one-field kernels sum the (up to
+// four) modes' |d|^2 and phase^2 at each kz and walk the bins once for all of
+// them (a quarter of the bin walk, its flushes and the staging of one row at a
+// time; the loads and per-mode arithmetic are the same).  The representatives are
+// 0..dims/2 on each axis; 0 and dims/2 have no partner.  Each mode's power is
+// |v|^2 mf^2 with mf the deconvolution factor, shared by the four modes; its phase
+// atan(Re v / |v|) does not depend on mf > 0.
+__host__ __device__ inline int sym_groups(int dims) { return dims / 2 + 1; }
+
+struct SignRows {
+    long long off[4];       // row r = (y sign << 1) | x sign
+    float2 pxy[4];          // interlacing phase exp(i pi (kx + ky) / dims) of each row
+    unsigned skip0, skipm;  // rows whose kz = 0 / kz = dims/2 modes the Hermitian skip drops
+    unsigned used;          // rows that exist (a representative without partner repeats row 0)
+};
+
+template <bool INTER>
+__device__ __forceinline__ SignRows sign_rows(int xr, int yr, const PkDims &d, const float2 *ph)
+{
+    const int dims = d.dims;
+    const bool even = (dims & 1) == 0;
+    const int nx = (xr == 0 || 2 * xr == dims) ? 1 : 2, ny = (yr == 0 || 2 * yr == dims) ? 1 : 2;
+    SignRows R;
+    R.skip0 = R.skipm = 0u;
+    R.used = 1u | (nx == 2 ? 2u : 0u) | (ny == 2 ? 4u : 0u) | (nx == 2 && ny == 2 ? 8u : 0u);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int kxx = ((r & 1) && nx == 2) ? dims - xr : xr;     // in range for every r
+        const int kyy = ((r & 2) && ny == 2) ? dims - yr : yr;
+        R.off[r] = ((long long)kxx * dims + kyy) * d.nz;
+        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
+        R.pxy[r] = make_float2(1.0f, 0.0f);
+        if (INTER) {
+            const float2 px = ph[kxx], py = ph[kyy];
+            R.pxy[r] = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
+        }
+        if (hermitian_skip(kx, ky, 0, d)) R.skip0 |= 1u << r;
+        if (even && hermitian_skip(kx, ky, d.middle, d)) R.skipm |= 1u << r;
+    }
+    return R;
+}
+
+// Pass 1 for one representative: the summed power and phase^2 of its rows at each
+// kz (lanes along kz, coalesced), into the warp's staging array at kz + kz / chunk.
+// All four rows are loaded (in range for every r), so an iteration's loads issue
+// together.
+template <bool INTER>
+__device__ __forceinline__ void stage_sign_rows(const SignRows &R, const float2 *__restrict__ dk,
+                                                const float2 *__restrict__ dk2, const float *corr,
+                                                const float2 *ph, float cxy, const PkDims &d, float2 *stage,
+                                                unsigned chunk_magic, int lane)
+{
+    const bool even = (d.dims & 1) == 0;
+#pragma unroll 2
+    for (int kz = lane; kz < d.nz; kz += 32) {
+        float2 t = make_float2(1.0f, 0.0f);
+        if (INTER) t = ph[kz];
+        const unsigned skip = kz == 0 ? R.skip0 : ((even && kz == d.middle) ? R.skipm : 0u);
+        const unsigned take = R.used & ~skip;
+        float2 v[4], w[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            v[r] = __ldg(dk + R.off[r] + kz);
+            if (INTER) w[r] = __ldg(dk2 + R.off[r] + kz);
+        }
+        float a2s = 0.0f, p2s = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float2 u = v[r];
+            if (INTER) {
+                const float2 pz = make_float2(R.pxy[r].x * t.x - R.pxy[r].y * t.y, R.pxy[r].x * t.y + R.pxy[r].y * t.x);
+                u.x = 0.5f * (u.x + (w[r].x * pz.x - w[r].y * pz.y));
+                u.y = 0.5f * (u.y + (w[r].x * pz.y + w[r].y * pz.x));
+            }
+            const float a2 = u.x * u.x + u.y * u.y;
+            const float phase = a2 > 0.0f ? atan_unit(u.x * rsqrtf(a2)) : 0.0f;
+            if ((take >> r) & 1u) {
+                a2s += a2;
+                p2s += phase * phase;
+            }
+        }
+        const float mf = __fmul_rn(cxy, corr[kz]);
+        stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(a2s * (mf * mf), p2s);
+    }
+}
+
+// One field, axis 2 (axes 0/1: pk_bin_sym_kernel below): the representatives
+// (|kx|, |ky|) in the order of their k_per ring (a.rows), each the four sign rows of
+// sign_rows; per-warp kz-indexed 2D and 1D sums, flushed when the ring changes.
 // BATCH: blockIdx.y picks an item of a.items (its field, partner, sums, MAS and
 // its slice of the partial sums); the CTA partition along blockIdx.x is a
 // one-field call's.
 template <bool INTER, int AXIS, bool BATCH>
 __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
+    static_assert(AXIS == 2, "axis 2 (rows in k_per ring order)");
     extern __shared__ float sm[];
     const PkDims d = a.d;
     const int dims = d.dims, nz = d.nz;
@@ -419,7 +512,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     float *part_base = (BATCH && a.part) ? a.part + (long long)blockIdx.y * gridDim.x * a.part_stride : a.part;
     float *corr = sm + L.corr;
     float2 *ph = (float2 *)(sm + L.ph);
-    float *acc3 = sm + L.acc3, *acc1 = sm + L.acc1, *acc2 = sm + L.acc2;
+    float *acc3 = sm + L.acc3;
     for (int i = threadIdx.x; i < dims; i += blockDim.x) corr[i] = mas_corr_f(freq_of(i, dims), dims, mas);
     if (INTER) {
         for (int i = threadIdx.x; i < dims; i += blockDim.x) {
@@ -443,23 +536,21 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
     const int kz_begin = lane * chunk;
     const int kz_end = min(nz, kz_begin + chunk);
     float *part = part_base ? part_base + (long long)blockIdx.x * a.part_stride : nullptr;
-    float r1 = 0.0f;
     int cur_ring = -1;
 
-    const RowIter it = row_iter(a, warp);
-    for (int q = 0; q < it.count; q++) {
-        int kxx, kyy;
-        row_coords(a, it, it.first + q * it.step, kxx, kyy);
-        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
-        const long long row = ((long long)kxx * dims + kyy) * nz;
-        const float cxy = __fmul_rn(corr[kxx], corr[kyy]);
-        float2 pxy = make_float2(1.0f, 0.0f);
-        if (INTER) {
-            const float2 px = ph[kxx], py = ph[kyy];
-            pxy = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
-        }
-        const int ring = AXIS == 2 ? isqrt_exact(kx * kx + ky * ky) : 0;
-        if (AXIS == 2 && ring != cur_ring) {
+    // the CTA's run of the representatives' table (ring order), split among the warps
+    const int G = sym_groups(dims);
+    const long long total = (long long)G * G;
+    const long long b = (long long)blockIdx.x * a.rows_per_cta;
+    const long long e = min(total, b + a.rows_per_cta);
+    const int per_warp = (a.rows_per_cta + NW - 1) / NW;
+    const long long wb = b + (long long)warp * per_warp;
+    const int count = wb < e ? (int)min((long long)per_warp, e - wb) : 0;
+    for (int j = 0; j < count; j++) {
+        const unsigned rid = a.rows[wb + j];
+        const int kx = (int)(rid / (unsigned)G), ky = (int)(rid % (unsigned)G);    // representatives
+        const int ring = isqrt_exact(kx * kx + ky * ky);
+        if (ring != cur_ring) {
             __syncwarp();
             if (cur_ring >= 0) {
                 for (int kz = lane; kz < nz; kz += 32) {
@@ -473,64 +564,32 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
             cur_ring = ring;
             __syncwarp();
         }
-        // pass 1: per-mode power and phase^2, coalesced along kz
-#pragma unroll 2
-        for (int kz = lane; kz < nz; kz += 32) {
-            float2 v = __ldg(dk + row + kz);
-            if (INTER) {
-                const float2 w = __ldg(dk2 + row + kz);
-                const float2 t = ph[kz];
-                const float2 pz = make_float2(pxy.x * t.x - pxy.y * t.y, pxy.x * t.y + pxy.y * t.x);
-                v.x = 0.5f * (v.x + (w.x * pz.x - w.y * pz.y));
-                v.y = 0.5f * (v.y + (w.x * pz.y + w.y * pz.x));
-            }
-            const float mf = __fmul_rn(cxy, corr[kz]);
-            const float re = __fmul_rn(v.x, mf), im = __fmul_rn(v.y, mf);
-            float p2 = re * re + im * im;
-            float phase = p2 > 0.0f ? atan_unit(re * rsqrtf(p2)) : 0.0f;
-            if (hermitian_skip(kx, ky, kz, d)) { p2 = 0.0f; phase = 0.0f; }
-            stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(p2, phase * phase);   // kz + kz / chunk
-        }
+        const SignRows R = sign_rows<INTER>(kx, ky, d, ph);
+        stage_sign_rows<INTER>(R, dk, dk2, corr, ph, __fmul_rn(corr[kx], corr[ky]), d, stage, chunk_magic, lane);
         __syncwarp();
         // pass 2: this lane's run of kz, sums kept while the bins stay the same
         if (kz_begin < kz_end) {
-            const int kperp2 = AXIS == 0 ? ky * ky : kx * kx;     // axes 0/1: k_per^2 - kz^2
             const int kxy2 = kx * kx + ky * ky;
             int kz = kz_begin;
             int n2 = kxy2 + kz * kz;
             int ki = isqrt_exact(n2);
-            int kp2 = kperp2 + kz * kz;
-            int kper = AXIS == 2 ? ring : isqrt_exact(kp2);
-            const int kpar_c = AXIS == 0 ? kx * kx : ky * ky;
-            float s0 = 0.0f, s2 = 0.0f, s4 = 0.0f, sp = 0.0f, sd = 0.0f;
+            float s0 = 0.0f, s2 = 0.0f, s4 = 0.0f, sp = 0.0f;
             const float2 *run = stage + lane * (chunk + 1);
             for (; kz < kz_end; kz++) {
                 const float2 e = run[kz - kz_begin];
                 const float val = e.x;
-                const int kpar2 = AXIS == 2 ? kz * kz : kpar_c;
-                const float mu2 = n2 ? __fdividef((float)kpar2, (float)n2) : 0.0f;
+                const float mu2 = n2 ? __fdividef((float)(kz * kz), (float)n2) : 0.0f;
                 const float l2 = 0.5f * (3.0f * mu2 - 1.0f);
                 const float l4 = 0.125f * ((35.0f * mu2 - 30.0f) * mu2 + 3.0f);
                 s0 += val;
                 s2 += val * l2;
                 s4 += val * l4;
                 sp += e.y;
-                if (AXIS == 2) {
-                    w2[kz] += val;
-                    if (n2 <= m2) w1[kz] += val;
-                } else {
-                    sd += val;
-                    if (n2 <= m2) r1 += val;
-                }
+                w2[kz] += val;
+                if (n2 <= m2) w1[kz] += val;
                 // step to kz + 1
-                const int dn = 2 * kz + 1;
-                n2 += dn;
+                n2 += 2 * kz + 1;
                 const bool new3 = (ki + 1) * (ki + 1) <= n2;
-                bool new2 = false;
-                if (AXIS != 2) {
-                    kp2 += dn;
-                    new2 = (kper + 1) * (kper + 1) <= kp2;
-                }
                 if (new3 || kz + 1 == kz_end) {
                     if (part) {                         // one vector reduction in L2
                         atomicAdd(reinterpret_cast<float4 *>(part + ki * 4), make_float4(s0, s2, s4, sp));
@@ -544,30 +603,18 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
                     s0 = s2 = s4 = sp = 0.0f;
                     ki += new3 ? 1 : 0;
                 }
-                if (AXIS != 2 && (new2 || kz + 1 == kz_end)) {
-                    if (part) atomicAdd(part + d.nb3 * 4 + kper, sd);
-                    else if (sd != 0.0f) atomicAdd(acc2 + kper, sd);
-                    sd = 0.0f;
-                    kper += new2 ? 1 : 0;
-                }
             }
         }
         __syncwarp();
     }
     // per-warp flushes
-    if (AXIS != 2) {
-        float v = r1;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-        if (lane == 0 && v != 0.0f) atomicAdd(acc1 + abs(freq_of(it.plane, dims)), v);
-    } else {
-        __syncwarp();
-        for (int kz = lane; kz < nz; kz += 32) {
-            const float v2 = w2[kz];
-            if (cur_ring >= 0 && v2 != 0.0f)
-                atomicAdd(P2 + (long long)(d.kmax_par + 1) * cur_ring + kz, (double)v2);
-            const float v1 = w1[kz];
-            if (v1 != 0.0f) atomicAdd(P1 + kz, (double)v1);
-        }
+    __syncwarp();
+    for (int kz = lane; kz < nz; kz += 32) {
+        const float v2 = w2[kz];
+        if (cur_ring >= 0 && v2 != 0.0f)
+            atomicAdd(P2 + (long long)(d.kmax_par + 1) * cur_ring + kz, (double)v2);
+        const float v1 = w1[kz];
+        if (v1 != 0.0f) atomicAdd(P1 + kz, (double)v1);
     }
     __syncthreads();
     if (!part) {
@@ -579,36 +626,12 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
             else atomicAdd(PH + bin, (double)v);
         }
     }
-    if (AXIS != 2) {
-        for (int i = threadIdx.x; i < d.nb1; i += blockDim.x) {
-            const float v = acc1[i];
-            if (v != 0.0f) atomicAdd(P1 + i, (double)v);
-        }
-        if (!part) {
-            const int kpar = abs(freq_of(it.plane, dims));
-            for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) {
-                const float v = acc2[i];
-                if (v == 0.0f) continue;
-                atomicAdd(P2 + (long long)(d.kmax_par + 1) * i + kpar, (double)v);
-            }
-        }
-    }
 }
 
-// ---- axes 0/1: the four sign rows of a (|k_plane|, |k_row|) pair at once ----------
-// With the line of sight along x (axis 0) a CTA's plane fixes |kx| = p and a row
-// fixes |ky| = q; every bin index (|k| from p^2 + q^2 + kz^2, k_per from q^2 + kz^2),
-// mu^2 = p^2 / k^2 and the 1D test depend on p^2 and q^2 only, so the rows
-// (+-kx, +-ky) have the same bins at every kz (axis 1: x and y swapped).  CTA
-// blockIdx.x / chunks takes plane representative p in [0, dims/2] (planes p and
-// dims - p), a warp row representative q (rows q and dims - q): pass 1 sums the
-// (up to four) modes' |d|^2 and phase^2 at each kz, pass 2 walks the bins once for
-// all of them.  The bin walk, its flushes and the staging are a quarter of the
-// one-row-at-a-time kernel's; the loads and per-mode arithmetic are the same.
-// Each mode's power is |v|^2 (mf)^2 with mf the deconvolution factor, shared by the
-// four modes; phase = atan(Re v / |v|) does not depend on mf > 0.
-__host__ __device__ inline int sym_groups(int dims) { return dims / 2 + 1; }
-
+// ---- axes 0/1 ---------------------------------------------------------------------
+// CTA blockIdx.x / chunks takes plane representative p (|k_par| with the line of
+// sight along x for axis 0, y for axis 1), its warps the row representatives q
+// of the CTA's chunk; each (p, q) is the four sign rows of sign_rows.
 template <bool INTER, int AXIS, bool BATCH>
 __global__ void __launch_bounds__(256) pk_bin_sym_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
@@ -657,73 +680,15 @@ __global__ void __launch_bounds__(256) pk_bin_sym_kernel(BinArgs a, int chunk, u
     const int kz_end = min(nz, kz_begin + chunk);
     float *part = part_base ? part_base + (long long)blockIdx.x * a.part_stride : nullptr;
     float r1 = 0.0f;
-    const bool even = (dims & 1) == 0;
 
     const int G = sym_groups(dims);
     const int p = blockIdx.x / a.chunks;                 // |k_par|
     const int cid = blockIdx.x % a.chunks;
     const int per = (G + a.chunks - 1) / a.chunks;
     const int q0 = cid * per, q1 = min(G, q0 + per);
-    const int np = (p == 0 || 2 * p == dims) ? 1 : 2;
     for (int q = q0 + warp; q < q1; q += NW) {
-        const int nq = (q == 0 || 2 * q == dims) ? 1 : 2;
-        // the physical rows: plane index p or dims - p, row index q or dims - q
-        long long off[4];
-        float2 pxy[4];
-        unsigned skip0 = 0u, skipm = 0u;                 // Hermitian skips on the kz = 0 / N/2 planes
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            // unused sign choices (np or nq of 1) repeat the representative, in range
-            const int pi = ((r & 1) && np == 2) ? dims - p : p, qi = ((r & 2) && nq == 2) ? dims - q : q;
-            const int kxx = AXIS == 0 ? pi : qi, kyy = AXIS == 0 ? qi : pi;
-            off[r] = ((long long)kxx * dims + kyy) * nz;
-            const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
-            pxy[r] = make_float2(1.0f, 0.0f);
-            if (INTER) {
-                const float2 px = ph[kxx], py = ph[kyy];
-                pxy[r] = make_float2(px.x * py.x - px.y * py.y, px.x * py.y + px.y * py.x);
-            }
-            if (hermitian_skip(kx, ky, 0, d)) skip0 |= 1u << r;
-            if (even && hermitian_skip(kx, ky, d.middle, d)) skipm |= 1u << r;
-        }
-        // rows r = (row sign << 1) | plane sign; a sign choice of a representative
-        // with no partner (0 or dims/2) is not used (its row repeats one that is)
-        const unsigned used = 1u | (np == 2 ? 2u : 0u) | (nq == 2 ? 4u : 0u) | (np == 2 && nq == 2 ? 8u : 0u);
-        const float cxy = __fmul_rn(corr[p], corr[q]);
-        // pass 1: the summed |d|^2 and phase^2 of the rows at each kz, coalesced along
-        // kz; all four rows are loaded (in range for every sign choice), so the loads
-        // of an iteration are issued together
-#pragma unroll 2
-        for (int kz = lane; kz < nz; kz += 32) {
-            float2 t = make_float2(1.0f, 0.0f);
-            if (INTER) t = ph[kz];
-            const unsigned skip = kz == 0 ? skip0 : ((even && kz == d.middle) ? skipm : 0u);
-            const unsigned take = used & ~skip;
-            float2 v[4], w[4];
-#pragma unroll
-            for (int r = 0; r < 4; r++) {
-                v[r] = __ldg(dk + off[r] + kz);
-                if (INTER) w[r] = __ldg(dk2 + off[r] + kz);
-            }
-            float a2s = 0.0f, p2s = 0.0f;
-#pragma unroll
-            for (int r = 0; r < 4; r++) {
-                float2 u = v[r];
-                if (INTER) {
-                    const float2 pz = make_float2(pxy[r].x * t.x - pxy[r].y * t.y, pxy[r].x * t.y + pxy[r].y * t.x);
-                    u.x = 0.5f * (u.x + (w[r].x * pz.x - w[r].y * pz.y));
-                    u.y = 0.5f * (u.y + (w[r].x * pz.y + w[r].y * pz.x));
-                }
-                const float a2 = u.x * u.x + u.y * u.y;
-                const float phase = a2 > 0.0f ? atan_unit(u.x * rsqrtf(a2)) : 0.0f;
-                if ((take >> r) & 1u) {
-                    a2s += a2;
-                    p2s += phase * phase;
-                }
-            }
-            const float mf = __fmul_rn(cxy, corr[kz]);
-            stage[kz + __umulhi((unsigned)kz, chunk_magic)] = make_float2(a2s * (mf * mf), p2s);
-        }
+        const SignRows R = sign_rows<INTER>(AXIS == 0 ? p : q, AXIS == 0 ? q : p, d, ph);
+        stage_sign_rows<INTER>(R, dk, dk2, corr, ph, __fmul_rn(corr[p], corr[q]), d, stage, chunk_magic, lane);
         __syncwarp();
         // pass 2: this lane's run of kz, sums kept while the bins stay the same
         if (kz_begin < kz_end) {
@@ -938,17 +903,34 @@ __global__ void __launch_bounds__(256) pk_geometry_kernel(BinArgs a)
 }
 
 // ---- ring table for axis 2: rows (kxx*dims + kyy) sorted by k_per = isqrt(kx^2+ky^2)
-__global__ void __launch_bounds__(256) ring_count_kernel(PkDims d, unsigned *cnt)
+// Row tables: every row (kxx, kyy), id kxx * dims + kyy, or with sym only the
+// representatives (p, q) of the four sign rows, p, q in [0, dims/2], id p * G + q.
+__device__ __forceinline__ int ring_of(long long r, const PkDims &d, bool sym)
+{
+    if (sym) {
+        const int G = d.dims / 2 + 1;
+        const int p = (int)(r / G), q = (int)(r % G);
+        return isqrt_exact(p * p + q * q);
+    }
+    const int kx = freq_of((int)(r / d.dims), d.dims), ky = freq_of((int)(r % d.dims), d.dims);
+    return isqrt_exact(kx * kx + ky * ky);
+}
+
+__host__ __device__ inline long long ring_rows(const PkDims &d, bool sym)
+{
+    const long long side = sym ? d.dims / 2 + 1 : d.dims;
+    return side * side;
+}
+
+__global__ void __launch_bounds__(256) ring_count_kernel(PkDims d, bool sym, unsigned *cnt)
 {
     extern __shared__ unsigned h[];
     for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    const long long total = (long long)d.dims * d.dims;
+    const long long total = ring_rows(d, sym);
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < total;
-         r += (long long)gridDim.x * blockDim.x) {
-        const int kx = freq_of((int)(r / d.dims), d.dims), ky = freq_of((int)(r % d.dims), d.dims);
-        atomicAdd(h + isqrt_exact(kx * kx + ky * ky), 1u);
-    }
+         r += (long long)gridDim.x * blockDim.x)
+        atomicAdd(h + ring_of(r, d, sym), 1u);
     __syncthreads();
     for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x)
         if (h[i]) atomicAdd(cnt + i, h[i]);
@@ -973,14 +955,12 @@ __global__ void __launch_bounds__(1024) ring_scan_kernel(const unsigned *cnt, in
     for (int i = b; i < e; i++) { cursor[i] = run; run += cnt[i]; }
 }
 
-__global__ void __launch_bounds__(256) ring_fill_kernel(PkDims d, unsigned *cursor, unsigned *rows)
+__global__ void __launch_bounds__(256) ring_fill_kernel(PkDims d, bool sym, unsigned *cursor, unsigned *rows)
 {
-    const long long total = (long long)d.dims * d.dims;
+    const long long total = ring_rows(d, sym);
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < total;
-         r += (long long)gridDim.x * blockDim.x) {
-        const int kx = freq_of((int)(r / d.dims), d.dims), ky = freq_of((int)(r % d.dims), d.dims);
-        rows[atomicAdd(cursor + isqrt_exact(kx * kx + ky * ky), 1u)] = (unsigned)r;
-    }
+         r += (long long)gridDim.x * blockDim.x)
+        rows[atomicAdd(cursor + ring_of(r, d, sym), 1u)] = (unsigned)r;
 }
 
 inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
@@ -1002,18 +982,18 @@ RingWs ring_layout(void *base, const PkDims &d)
     return w;
 }
 
-int build_rings(const PkDims &d, const RingWs &w, cudaStream_t st)
+int build_rings(const PkDims &d, const RingWs &w, bool sym, cudaStream_t st)
 {
     const int n = d.kmax_per + 1;
     PYL_CUDA(cudaMemsetAsync(w.cnt, 0, sizeof(unsigned) * n, st));
-    const long long total = (long long)d.dims * d.dims;
+    const long long total = ring_rows(d, sym);
     int blocks = (int)min((total + 255) / 256, (long long)num_sms() * 4);
     if (blocks < 1) blocks = 1;
-    ring_count_kernel<<<blocks, 256, sizeof(unsigned) * n, st>>>(d, w.cnt);
+    ring_count_kernel<<<blocks, 256, sizeof(unsigned) * n, st>>>(d, sym, w.cnt);
     PYL_LAUNCH_CHECK();
     ring_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, n, w.cursor);
     PYL_LAUNCH_CHECK();
-    ring_fill_kernel<<<blocks, 256, 0, st>>>(d, w.cursor, w.rows);
+    ring_fill_kernel<<<blocks, 256, 0, st>>>(d, sym, w.cursor, w.rows);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
@@ -1047,7 +1027,7 @@ inline int sym_chunks(int dims)
 inline SeqPart seq_part(const PkDims &d, int axis)
 {
     SeqPart p;
-    p.blocks = axis == 2 ? (unsigned)(((long long)d.dims * d.dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA)
+    p.blocks = axis == 2 ? (unsigned)((ring_rows(d, true) + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA)
                          : (unsigned)(sym_groups(d.dims) * sym_chunks(d.dims));
     p.stride = (d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1) + 3) & ~3;
     p.bytes = align256(sizeof(float) * (size_t)p.blocks * p.stride);
@@ -1105,6 +1085,15 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
     }
     const bool inter = dk_interlaced != nullptr;
     cudaStream_t st = (cudaStream_t)stream;
+    // one field: the four-sign-row kernels when their shared memory fits (with the
+    // per-CTA partial sums when the workspace holds them); else pk_bin_kernel
+    const int chunk = seq_chunk(d.nz);
+    const bool warp_arrays = axis == 2 && sizeof(float) * bin_smem(d, a.F, a.C, axis, inter, 1).total <= SMEM_LIMIT;
+    const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
+    const SeqPart sp = seq_part(d, axis);
+    const bool use_part = n_fields == 1 && workspace != nullptr && workspace_bytes >= ring_bytes + sp.bytes;
+    const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk, use_part).total;
+    const bool seq = n_fields == 1 && (axis != 2 || warp_arrays) && sms <= SMEM_LIMIT;
     unsigned blocks;
     if (axis == 2) {
         const RingWs w = ring_layout(workspace, d);
@@ -1112,61 +1101,50 @@ extern "C" int pyl_pk_bin(const void *dk, const void *dk_interlaced, int n_field
             set_error("pyl_pk_bin: axis 2 needs " + std::to_string(w.bytes) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
         }
-        int rc = build_rings(d, w, st);
+        int rc = build_rings(d, w, seq, st);
         if (rc) return rc;
         a.rows = w.rows;
         a.rows_per_cta = RING_ROWS_PER_CTA;
         a.chunks = 1;
-        blocks = (unsigned)(((long long)dims * dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
-        a.warp_arrays = sizeof(float) * bin_smem(d, a.F, a.C, axis, inter, 1).total <= SMEM_LIMIT;
+        a.warp_arrays = warp_arrays;
+        blocks = (unsigned)((ring_rows(d, seq) + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
     } else {
-        a.chunks = plane_chunks(dims);
         a.rows_per_cta = 0;
         a.warp_arrays = 0;
-        blocks = (unsigned)(dims * a.chunks);
+        a.chunks = seq ? sym_chunks(dims) : plane_chunks(dims);
+        blocks = (unsigned)((seq ? sym_groups(dims) : dims) * a.chunks);
     }
-    if (n_fields == 1 && (axis != 2 || a.warp_arrays)) {
-        const int chunk = seq_chunk(d.nz);
-        if (axis != 2) {
-            a.chunks = sym_chunks(dims);
-            blocks = (unsigned)(sym_groups(dims) * a.chunks);
+    if (seq) {
+        PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
+        a.part_stride = sp.stride;
+        if (use_part) {
+            a.part = (float *)((char *)workspace + ring_bytes);
+            PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride, st));
         }
-        const size_t ring_bytes = axis == 2 ? ring_layout(nullptr, d).bytes : 0;
-        const SeqPart sp = seq_part(d, axis);
-        const bool use_part = workspace != nullptr && workspace_bytes >= ring_bytes + sp.bytes && sp.blocks == blocks;
-        const size_t sms = sizeof(float) * (size_t)seq_smem(d, axis, inter, chunk, use_part).total;
-        if (sms <= SMEM_LIMIT) {
-            PYL_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * pyl_pk_sums_len(dims, 1), st));
-            a.part_stride = sp.stride;
-            if (use_part) {
-                a.part = (float *)((char *)workspace + ring_bytes);
-                PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride, st));
-            }
 #define PYL_SEQ(K, I, A)                                                           \
     do {                                                                           \
         PYL_CUDA(ensure_smem(K<I, A, false>, sms));                         \
         K<I, A, false><<<blocks, 256, sms, st>>>(a, chunk, seq_chunk_magic(chunk)); \
     } while (0)
-            if (inter) {
-                if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, true, 0);
-                else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, true, 1);
-                else PYL_SEQ(pk_bin_seq_kernel, true, 2);
-            } else {
-                if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, false, 0);
-                else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, false, 1);
-                else PYL_SEQ(pk_bin_seq_kernel, false, 2);
-            }
-#undef PYL_SEQ
-            PYL_LAUNCH_CHECK();
-            if (a.part) {
-                const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
-                const int groups = 16, per_group = (int)((blocks + groups - 1) / groups);
-                pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups), 256, 0, st>>>(
-                    a.part, (int)blocks, sp.stride, per_group, a.chunks, axis, d, sums, nullptr);
-                PYL_LAUNCH_CHECK();
-            }
-            return PYL_OK;
+        if (inter) {
+            if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, true, 0);
+            else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, true, 1);
+            else PYL_SEQ(pk_bin_seq_kernel, true, 2);
+        } else {
+            if (axis == 0) PYL_SEQ(pk_bin_sym_kernel, false, 0);
+            else if (axis == 1) PYL_SEQ(pk_bin_sym_kernel, false, 1);
+            else PYL_SEQ(pk_bin_seq_kernel, false, 2);
         }
+#undef PYL_SEQ
+        PYL_LAUNCH_CHECK();
+        if (a.part) {
+            const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
+            const int groups = 16, per_group = (int)((blocks + groups - 1) / groups);
+            pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups), 256, 0, st>>>(
+                a.part, (int)blocks, sp.stride, per_group, a.chunks, axis, d, sums, nullptr);
+            PYL_LAUNCH_CHECK();
+        }
+        return PYL_OK;
     }
     const size_t smem = sizeof(float) * (size_t)bin_smem(d, a.F, a.C, axis, inter, a.warp_arrays).total;
     if (smem > SMEM_LIMIT) {
@@ -1255,7 +1233,7 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
     if (axis == 2) {
         const RingWs w = ring_layout(workspace, d);
         ring_bytes = w.bytes;
-        int rc = build_rings(d, w, st);
+        int rc = build_rings(d, w, true, st);
         if (rc) return rc;
         a.rows = w.rows;
         a.rows_per_cta = RING_ROWS_PER_CTA;
@@ -1324,7 +1302,7 @@ extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace
             set_error("pyl_pk_geometry: axis 2 needs " + std::to_string(w.bytes) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
         }
-        int rc = build_rings(d, w, st);
+        int rc = build_rings(d, w, false, st);
         if (rc) return rc;
         a.rows = w.rows;
         a.rows_per_cta = RING_ROWS_PER_CTA;
