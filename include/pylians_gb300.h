@@ -41,7 +41,8 @@ extern "C" {
 #define PYL_STRATEGY_AUTO 0   /* library picks by grid size and particle count */
 #define PYL_STRATEGY_ATOMIC 1 /* one thread per particle, atomics into the grid */
 #define PYL_STRATEGY_TILED 2  /* bin particles by tile, deposit tiles in shared memory;
-                                 3D and fewer than 2^32 - 16 particles (else ATOMIC runs) */
+                                 3D; calls of 2^32 - 4096 particles and more run as
+                                 consecutive passes (pyl_ma_set_pass_limit) */
 #define PYL_STRATEGY_SORTED 3 /* radix sort by cell + fixed-order per-cell gather: bit-reproducible */
 
 const char *pyl_strerror(int status);
@@ -377,6 +378,17 @@ int pyl_stage_times(double *ms_out, int n);
  * value restores that default.  Change them only between calls (the workspace
  * size depends on the first). */
 int pyl_ma_set_thresholds(int owned_min_dims, double tot_min_per_cell);
+
+/* Particles per pass of the tiled deposit (no counterpart in the reference, whose
+ * loop counter is a 64-bit long, MAS_library.pyx:123-166): its records and bin
+ * offsets are 32-bit, so a call with more particles than the limit (default
+ * 2^32 - 4096) deposits consecutive slices of at most that many, each pass
+ * accumulating (pyl_ma) or, for the overdensity, the first storing -1 + value
+ * and the others accumulating, with the mean density of the whole call; the
+ * workspace is one pass's.  Process-wide, rounded down to a multiple of 1024
+ * (at least 1024; negative restores the default), for tests and for callers
+ * that want smaller workspaces.  Change it only between calls. */
+int pyl_ma_set_pass_limit(int64_t max_particles);
 
 /* Device-side error word (no counterpart in the reference): nonzero when a kernel's
  * bounded wait for its own bulk copies ran out and the kernel left early (its

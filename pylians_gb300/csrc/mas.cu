@@ -44,6 +44,7 @@ __device__ unsigned g_tma_error;
 
 std::atomic<int> g_owned_min_dims{OWNED_MIN_DIMS};
 std::atomic<double> g_tot_min_per_cell{TOT_MIN_PER_CELL};
+std::atomic<long long> g_tiled_pass_max{TILED_PASS_MAX};
 
 namespace {
 std::mutex g_err_mu;
@@ -172,7 +173,8 @@ extern "C" size_t pyl_ma_workspace_size(int64_t n_particles, int ndim, int dims,
     if (s == PYL_STRATEGY_SORTED && ndim == 3 && sorted_supported(n_particles, dims))
         return sorted_workspace_bytes(n_particles, dims) + 256;
     if (s == PYL_STRATEGY_TILED && ndim == 3)
-        return tiled_layout(nullptr, n_particles, dims, owned_halo_floats(mas, dims, interlaced != 0)).bytes + 256;
+        return tiled_layout(nullptr, tiled_pass_len(n_particles), dims,
+                            owned_halo_floats(mas, dims, interlaced != 0)).bytes + 256;
     return 256;
 }
 
@@ -211,26 +213,30 @@ extern "C" int pyl_ma(const float *pos, const float *weights, int64_t n, int ndi
         return launch_sorted(mas, pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, workspace, 1.0f,
                              nullptr, true, st);
     }
-    if (s == PYL_STRATEGY_TILED && (ndim != 3 || n > 0xFFFFFFF0ll)) s = PYL_STRATEGY_ATOMIC;
+    if (s == PYL_STRATEGY_TILED && ndim != 3) s = PYL_STRATEGY_ATOMIC;
     Owned ow{false, nullptr, 0, 0.0f, 0};
+    const long long pass = tiled_pass_len(n);
     if (s == PYL_STRATEGY_TILED) {
-        const size_t need = tiled_layout(nullptr, n, dims).bytes;
+        const size_t need = tiled_layout(nullptr, pass, dims).bytes;
         if (workspace_bytes < need || workspace == nullptr) {
             set_error("pyl_ma: tiled strategy needs " + std::to_string(need) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
         }
         // owned-cell write-out when the workspace also holds the halo blocks
         const size_t need_owned =
-            tiled_layout(nullptr, n, dims, owned_halo_floats(mas, dims, grid_interlaced != nullptr)).bytes;
+            tiled_layout(nullptr, pass, dims, owned_halo_floats(mas, dims, grid_interlaced != nullptr)).bytes;
         ow.on = owned_applies(dims) && workspace_bytes >= need_owned;
     }
     int rc = PYL_OK;
     if (n > 0) {
+        // tiled: consecutive passes of at most `pass` particles, each accumulating
 #define PYL_DISPATCH(M)                                                                              \
     case M:                                                                                          \
         if (s == PYL_STRATEGY_TILED)                                                                 \
-            rc = launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,        \
-                                 workspace, sc, st, err, nullptr, ow);                               \
+            for (long long o = 0; o < n && rc == PYL_OK; o += pass)                                  \
+                rc = launch_tiled<M>(pos + 3 * o, weights ? weights + o : nullptr, std::min(pass, n - o), \
+                                     grid, grid_interlaced, dims, inv, halfcell, workspace, sc, st, err,  \
+                                     nullptr, ow);                                                   \
         else if (ndim == 3)                                                                          \
             rc = launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st); \
         else                                                                                         \
@@ -329,8 +335,8 @@ int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float
     const float inv = (float)dims / box_size;
     const float halfcell = (float)(0.5 * (double)box_size / dims);
     int s = pick_strategy(strategy, 3, dims, n);
-    if (s == PYL_STRATEGY_TILED && n > 0xFFFFFFF0ll) s = PYL_STRATEGY_ATOMIC;
     // the owned-cell write-out stores -1 + value into every cell: no fill pass
+    // (with several tiled passes, the first stores and the others accumulate)
     const Owned ow{s == PYL_STRATEGY_TILED && owned_applies(dims), nullptr, 1, -1.0f, 0};
     if (!ow.on) {
         const int blocks = grid_blocks(cells / 4 + 1, 256, 8);
@@ -356,20 +362,40 @@ int ma_overdensity_impl(const float *pos, const float *weights, int64_t n, float
     if (s == PYL_STRATEGY_SORTED)
         return launch_sorted(mas, pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, workspace, sc.host,
                              sc.dev, false, st);
-    switch (mas) {
-#define PYL_OD(M)                                                                                    \
-    case M:                                                                                          \
-        return s == PYL_STRATEGY_TILED                                                               \
-                   ? launch_tiled<M>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell,   \
-                                     workspace, sc, st, err, fused, ow)                              \
-                   : launch_atomic<M, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
-        PYL_OD(PYL_MAS_NGP)
-        PYL_OD(PYL_MAS_CIC)
-        PYL_OD(PYL_MAS_TSC)
-        PYL_OD(PYL_MAS_PCS)
-#undef PYL_OD
+    if (s != PYL_STRATEGY_TILED) {
+        switch (mas) {
+            case PYL_MAS_NGP: return launch_atomic<PYL_MAS_NGP, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
+            case PYL_MAS_CIC: return launch_atomic<PYL_MAS_CIC, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
+            case PYL_MAS_TSC: return launch_atomic<PYL_MAS_TSC, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
+            default: return launch_atomic<PYL_MAS_PCS, 3>(pos, weights, n, grid, grid_interlaced, dims, inv, halfcell, sc, st);
+        }
     }
-    return PYL_ERR_INVALID;
+    // tiled: consecutive passes of at most `pass` particles; the scale is the whole
+    // call's, and with the owned-cell write-out only the first pass stores
+    const long long pass = tiled_pass_len(n);
+    int rc = PYL_OK;
+    for (long long o = 0; o < n && rc == PYL_OK; o += pass) {
+        const long long cnt = std::min(pass, n - o);
+        const float *p = pos + 3 * o;
+        const float *w = weights ? weights + o : nullptr;
+        Owned owp = ow;
+        if (o > 0) owp.fill_mode = 0;
+        RsdArgs rp;
+        const RsdArgs *fp = nullptr;
+        if (fused) {
+            rp = *fused;
+            rp.pos = fused->pos + 3 * o;
+            rp.vel = fused->vel + 3 * o;
+            fp = &rp;
+        }
+        switch (mas) {
+            case PYL_MAS_NGP: rc = launch_tiled<PYL_MAS_NGP>(p, w, cnt, grid, grid_interlaced, dims, inv, halfcell, workspace, sc, st, err, fp, owp); break;
+            case PYL_MAS_CIC: rc = launch_tiled<PYL_MAS_CIC>(p, w, cnt, grid, grid_interlaced, dims, inv, halfcell, workspace, sc, st, err, fp, owp); break;
+            case PYL_MAS_TSC: rc = launch_tiled<PYL_MAS_TSC>(p, w, cnt, grid, grid_interlaced, dims, inv, halfcell, workspace, sc, st, err, fp, owp); break;
+            default: rc = launch_tiled<PYL_MAS_PCS>(p, w, cnt, grid, grid_interlaced, dims, inv, halfcell, workspace, sc, st, err, fp, owp); break;
+        }
+    }
+    return rc;
 }
 
 }  // namespace
@@ -591,6 +617,16 @@ extern "C" int pyl_ma_set_thresholds(int owned_min_dims, double tot_min_per_cell
     PYL_CHECK_ARG(!(tot_min_per_cell != tot_min_per_cell), "tot_min_per_cell is NaN");
     pyl::g_owned_min_dims.store(owned_min_dims < 0 ? pyl::OWNED_MIN_DIMS : owned_min_dims);
     pyl::g_tot_min_per_cell.store(tot_min_per_cell < 0.0 ? pyl::TOT_MIN_PER_CELL : tot_min_per_cell);
+    return PYL_OK;
+}
+
+extern "C" int pyl_ma_set_pass_limit(int64_t max_particles)
+{
+    PYL_CHECK_ARG(max_particles != 0, "max_particles must be positive (or negative for the default)");
+    long long v = max_particles < 0 ? pyl::TILED_PASS_MAX : std::min((long long)max_particles, pyl::TILED_PASS_MAX);
+    v = v / 1024 * 1024;
+    PYL_CHECK_ARG(v >= 1024, "max_particles must be at least 1024");
+    pyl::g_tiled_pass_max.store(v);
     return PYL_OK;
 }
 

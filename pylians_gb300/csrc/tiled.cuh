@@ -154,6 +154,13 @@ constexpr double TOT_MIN_PER_CELL = 2.0;
 // the large-grid code paths on small grids with it).
 extern std::atomic<int> g_owned_min_dims;
 extern std::atomic<double> g_tot_min_per_cell;
+
+// Particles per tiled pass: records, bin counts and offsets are 32-bit, so calls
+// with more particles run the tiled deposit over consecutive passes of at most
+// this many (a multiple of 1024, so every pass's positions stay 16-byte aligned).
+constexpr long long TILED_PASS_MAX = 0xFFFFF000ll;
+extern std::atomic<long long> g_tiled_pass_max;
+inline long long tiled_pass_len(long long n) { return n < g_tiled_pass_max.load() ? n : g_tiled_pass_max.load(); }
 inline bool owned_applies(int dims) { return dims % TB == 0 && dims >= g_owned_min_dims.load(); }
 
 // Floats of the owned-cell halo buffers of both grids (0 when the grid does not

@@ -196,3 +196,23 @@ def test_wait_probe_and_thresholds_reject_bad_arguments(lib):
     assert lib.pyl_ma_set_thresholds(0, 1.0) == 1
     assert lib.pyl_ma_set_thresholds(-1, float('nan')) == 1
     assert lib.pyl_ma_set_thresholds(-1, -1.0) == 0
+
+
+def test_pass_limit_sizes_the_workspace(lib):
+    size = lib.pyl_ma_workspace_size
+    size.restype = ctypes.c_size_t
+    size.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.pyl_ma_set_pass_limit.argtypes = [ctypes.c_int64]
+    # a call of 2048^3 particles needs one pass's workspace, not the whole call's
+    big = size(2048 ** 3, 3, 2048, 2, 2, 1)
+    assert big == size((1 << 32) - 4096, 3, 2048, 2, 2, 1)
+    assert big < 16 * 2048 ** 3
+    try:
+        assert lib.pyl_ma_set_pass_limit(0) == 1
+        assert lib.pyl_ma_set_pass_limit(1000) == 1            # below one 1024-particle block
+        assert lib.pyl_ma_set_pass_limit(5000) == 0            # rounded down to 4096
+        assert size(10 ** 6, 3, 64, 2, 2, 0) == size(4096, 3, 64, 2, 2, 0)
+    finally:
+        assert lib.pyl_ma_set_pass_limit(-1) == 0
+    assert size(10 ** 6, 3, 64, 2, 2, 0) > size(4096, 3, 64, 2, 2, 0)
+
