@@ -815,8 +815,13 @@ __global__ void __launch_bounds__(256) pk_items_zero_kernel(const pyl_pk_item *_
     for (long long i = threadIdx.x; i < len; i += blockDim.x) s[i] = 0.0;
 }
 
-// Data-independent per-bin sums with the same traversal: N3 and K3 = sum |k|
-// by 3D bin, N1 by |k_par| for |k| <= N/2 (K1 = |k_par| N1), N2 by 2D bin.
+// Data-independent per-bin sums: N3 and K3 = sum |k| by 3D bin, N1 by |k_par| for
+// |k| <= N/2 (K1 = |k_par| N1), N2 by 2D bin.  The modes are walked by sign-row
+// representatives like the one-field bin kernels (axes 0/1: CTA = plane
+// representative p, warps = row representatives q; axis 2: the representatives'
+// ring table): each (p, q, kz) stands for its m = 1..4 sign rows not dropped by
+// the Hermitian skip, counted m times, with |k| = sqrt(p^2 + q^2 + kz^2) in
+// float64 (one square root per representative instead of per mode).
 // shared memory (doubles): N3[nb3] K3[nb3] N1[nb1] N2[kmax_per+1] (axis 0/1) or
 // per-warp kz arrays c2[NW][nz] c1[NW][nz] (axis 2).
 template <int AXIS>
@@ -831,16 +836,44 @@ __global__ void __launch_bounds__(256) pk_geometry_kernel(BinArgs a)
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long m2 = (long long)d.middle * d.middle;
+    const bool even = (dims & 1) == 0;
     double *gK1 = a.geom, *gN1 = gK1 + d.nb1, *gN2 = gN1 + d.nb1, *gK3 = gN2 + d.nb2, *gN3 = gK3 + d.nb3;
     double *c2 = N2 + warp * 2 * nz, *c1 = c2 + nz;   // axis 2
     float n1reg = 0.0f;
     int cur_ring = -1;
-    const RowIter it = row_iter(a, warp);
-    for (int q = 0; q < it.count; q++) {
-        int kxx, kyy;
-        row_coords(a, it, it.first + q * it.step, kxx, kyy);
-        const int kx = freq_of(kxx, dims), ky = freq_of(kyy, dims);
-        const int ring = AXIS == 2 ? isqrt_exact(kx * kx + ky * ky) : 0;
+    const int G = sym_groups(dims);
+    // this warp's representatives: (p, q) of a plane (axes 0/1) or a run of the ring table
+    int p = 0, q_first = 0, q_step = 1, count = 0;
+    long long wb = 0;
+    if (AXIS != 2) {
+        p = blockIdx.x / a.chunks;
+        const int cid = blockIdx.x % a.chunks, per = (G + a.chunks - 1) / a.chunks;
+        const int q0 = cid * per, q1 = min(G, q0 + per);
+        q_first = q0 + warp;
+        q_step = NW;
+        count = q_first < q1 ? (q1 - q_first + NW - 1) / NW : 0;
+    } else {
+        const long long total = (long long)G * G;
+        const long long b = (long long)blockIdx.x * a.rows_per_cta, e = min(total, b + a.rows_per_cta);
+        const int per_warp = (a.rows_per_cta + NW - 1) / NW;
+        wb = b + (long long)warp * per_warp;
+        count = wb < e ? (int)min((long long)per_warp, e - wb) : 0;
+    }
+    for (int j = 0; j < count; j++) {
+        int xr, yr;                                  // |kx|, |ky| representatives
+        if (AXIS == 2) {
+            const unsigned rid = a.rows[wb + j];
+            xr = (int)(rid / (unsigned)G);
+            yr = (int)(rid % (unsigned)G);
+        } else {
+            const int q = q_first + j * q_step;
+            xr = AXIS == 0 ? p : q;
+            yr = AXIS == 0 ? q : p;
+        }
+        const SignRows R = sign_rows<false>(xr, yr, d, nullptr);
+        const int mall = __popc(R.used), m0 = __popc(R.used & ~R.skip0), mm = __popc(R.used & ~R.skipm);
+        const int kxy2 = xr * xr + yr * yr;
+        const int ring = AXIS == 2 ? isqrt_exact(kxy2) : 0;
         if (AXIS == 2 && ring != cur_ring) {
             if (cur_ring >= 0)
                 for (int kz = lane; kz < nz; kz += 32)
@@ -850,36 +883,37 @@ __global__ void __launch_bounds__(256) pk_geometry_kernel(BinArgs a)
                     }
             cur_ring = ring;
         }
+        const int kper2 = AXIS == 0 ? yr * yr : xr * xr;      // axes 0/1: k_per^2 - kz^2
         for (int kz0 = 0; kz0 < nz; kz0 += 32) {
             const int kz = kz0 + lane;
             const bool valid = kz < nz;
-            const bool live = valid && !hermitian_skip(kx, ky, kz, d);
-            const int n2 = kx * kx + ky * ky + kz * kz;
+            const int m = !valid ? 0 : (kz == 0 ? m0 : ((even && kz == d.middle) ? mm : mall));
+            const int n2 = kxy2 + kz * kz;
             const int ki = valid ? isqrt_exact(n2) : KEY_NONE;
             const Seg s3 = seg_of(ki);
-            const float cnt = seg_sum(live ? 1.0f : 0.0f, s3.start);
-            const double ks = seg_sum(live ? sqrt((double)n2) : 0.0, s3.start);
+            const float cnt = seg_sum((float)m, s3.start);
+            const double ks = seg_sum(m ? (double)m * sqrt((double)n2) : 0.0, s3.start);
             if (s3.tail && ki != KEY_NONE && cnt != 0.0f) {
                 atomicAdd(N3 + ki, (double)cnt);
                 atomicAdd(K3 + ki, ks);
             }
-            const bool in1d = live && (long long)n2 <= m2;
+            const bool in1d = m && (long long)n2 <= m2;
             if (AXIS != 2) {
-                const int kper = AXIS == 0 ? isqrt_exact(ky * ky + kz * kz) : isqrt_exact(kx * kx + kz * kz);
+                const int kper = isqrt_exact(kper2 + kz * kz);
                 const Seg s2 = seg_of(valid ? kper : KEY_NONE);
-                const float c = seg_sum(live ? 1.0f : 0.0f, s2.start);
+                const float c = seg_sum((float)m, s2.start);
                 if (s2.tail && valid && c != 0.0f) atomicAdd(N2 + kper, (double)c);
-                if (in1d) n1reg += 1.0f;
-            } else if (live) {
-                c2[kz] += 1.0;
-                if (in1d) c1[kz] += 1.0;
+                if (in1d) n1reg += (float)m;
+            } else if (m) {
+                c2[kz] += (double)m;
+                if (in1d) c1[kz] += (double)m;
             }
         }
     }
     if (AXIS != 2) {
         float v = n1reg;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-        if (lane == 0 && v != 0.0f) atomicAdd(N1 + abs(freq_of(it.plane, dims)), (double)v);
+        if (lane == 0 && v != 0.0f) atomicAdd(N1 + p, (double)v);
     } else {
         for (int kz = lane; kz < nz; kz += 32) {
             if (cur_ring >= 0 && c2[kz] != 0.0)
@@ -896,9 +930,8 @@ __global__ void __launch_bounds__(256) pk_geometry_kernel(BinArgs a)
     if (AXIS != 2) {
         for (int i = threadIdx.x; i < d.nb1; i += blockDim.x)
             if (N1[i] != 0.0) { atomicAdd(gN1 + i, N1[i]); atomicAdd(gK1 + i, N1[i] * i); }
-        const int kpar = abs(freq_of(it.plane, dims));
         for (int i = threadIdx.x; i <= d.kmax_per; i += blockDim.x)
-            if (N2[i] != 0.0) atomicAdd(gN2 + (long long)(d.kmax_par + 1) * i + kpar, N2[i]);
+            if (N2[i] != 0.0) atomicAdd(gN2 + (long long)(d.kmax_par + 1) * i + p, N2[i]);
     }
 }
 
@@ -1302,18 +1335,18 @@ extern "C" int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace
             set_error("pyl_pk_geometry: axis 2 needs " + std::to_string(w.bytes) + " workspace bytes");
             return PYL_ERR_WORKSPACE;
         }
-        int rc = build_rings(d, w, false, st);
+        int rc = build_rings(d, w, true, st);
         if (rc) return rc;
         a.rows = w.rows;
         a.rows_per_cta = RING_ROWS_PER_CTA;
         a.chunks = 1;
         a.warp_arrays = 1;
-        blocks = (unsigned)(((long long)dims * dims + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
+        blocks = (unsigned)((ring_rows(d, true) + RING_ROWS_PER_CTA - 1) / RING_ROWS_PER_CTA);
     } else {
-        a.chunks = plane_chunks(dims);
+        a.chunks = sym_chunks(dims);
         a.rows_per_cta = 0;
         a.warp_arrays = 0;
-        blocks = (unsigned)(dims * a.chunks);
+        blocks = (unsigned)(sym_groups(dims) * a.chunks);
     }
     const size_t smem = sizeof(double) * (2 * d.nb3 + d.nb1 + (axis == 2 ? 2 * NW * d.nz : d.kmax_per + 1));
     if (smem > SMEM_LIMIT) {
