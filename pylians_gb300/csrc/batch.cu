@@ -179,6 +179,29 @@ __device__ __forceinline__ int bt_key_rt(int mas, const float *p, float inv, int
     }
 }
 
+// Positions of particles q .. q+3 (q a multiple of 4, so 48 bytes from a 16-byte
+// aligned base): three 16-byte loads instead of twelve 4-byte ones; lanes of a
+// warp read consecutive 48-byte groups.  Particles at or past `end` are not read.
+__device__ __forceinline__ void load_quad(const float *pos, long long q, long long end, bool vec, float p[4][3])
+{
+    if (vec && q + 4 <= end) {
+        const float4 *g = reinterpret_cast<const float4 *>(pos + 3 * q);
+        const float4 a = __ldg(g), b = __ldg(g + 1), c = __ldg(g + 2);
+        p[0][0] = a.x; p[0][1] = a.y; p[0][2] = a.z;
+        p[1][0] = a.w; p[1][1] = b.x; p[1][2] = b.y;
+        p[2][0] = b.z; p[2][1] = b.w; p[2][2] = c.x;
+        p[3][0] = c.y; p[3][1] = c.z; p[3][2] = c.w;
+    } else {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (q + u < end) {
+                p[u][0] = __ldg(pos + 3 * (q + u));
+                p[u][1] = __ldg(pos + 3 * (q + u) + 1);
+                p[u][2] = __ldg(pos + 3 * (q + u) + 2);
+            }
+    }
+}
+
 __global__ void __launch_bounds__(1024) bt_count_kernel(const pyl_batch_real *__restrict__ reals,
                                                         const pyl_batch_item *__restrict__ items, int n_items,
                                                         const unsigned *__restrict__ tile_base,
@@ -200,9 +223,14 @@ __global__ void __launch_bounds__(1024) bt_count_kernel(const pyl_batch_real *__
         }
         for (int t = threadIdx.x; t < ntiles; t += blockDim.x) h[t] = 0u;
         __syncthreads();
-        for (long long i = item.first + threadIdx.x; i < item.first + item.count; i += blockDim.x) {
-            const float p[3] = {__ldg(r.pos + 3 * i), __ldg(r.pos + 3 * i + 1), __ldg(r.pos + 3 * i + 2)};
-            atomicAdd(h + bt_key_rt(r.mas, p, r.inv, r.dims, nt), 1u);
+        const long long end = item.first + item.count;
+        const bool vec = (item.first & 3) == 0 && (((uintptr_t)r.pos) & 15) == 0;
+        for (long long q = item.first + 4 * (long long)threadIdx.x; q < end; q += 4 * (long long)blockDim.x) {
+            float p[4][3];
+            load_quad(r.pos, q, end, vec, p);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (q + u < end) atomicAdd(h + bt_key_rt(r.mas, p[u], r.inv, r.dims, nt), 1u);
         }
         __syncthreads();
         const unsigned base = tile_base[item.real];
@@ -238,15 +266,68 @@ __global__ void __launch_bounds__(1024) bt_scan_kernel(const unsigned *__restric
     if (threadIdx.x == blockDim.x - 1) offsets[n] = (unsigned)part[threadIdx.x];
 }
 
+// Exclusive scan of v[0..n) in place, n <= 4 * blockDim.x (each thread four
+// consecutive entries); warp_tot: 32 entries of scratch.  All threads call it.
+__device__ __forceinline__ void bt_block_scan4(unsigned *v, int n, unsigned *warp_tot)
+{
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = (blockDim.x + 31) >> 5;
+    unsigned x[4], tot = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        x[k] = 4 * t + k < n ? v[4 * t + k] : 0u;
+        tot += x[k];
+    }
+    unsigned inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const unsigned wt = lane < nw ? warp_tot[lane] : 0u;
+        unsigned wi = wt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < nw) warp_tot[lane] = wi - wt;
+    }
+    __syncthreads();
+    unsigned run = inc - tot + warp_tot[w];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (4 * t + k < n) {
+            v[4 * t + k] = run;
+            run += x[k];
+        }
+    __syncthreads();
+}
+
+// Per 4096-particle batch of an item: ranks per bin from shared-memory counters,
+// one global atomic per bin touched reserves its run in the bin's range, the batch
+// is sorted by bin in shared memory, and the runs are written out coalesced
+// (consecutive threads, consecutive slots of a run).
+constexpr size_t BT_PLACE_SMEM = sizeof(unsigned) * 2 * BT_MAX_TILES + sizeof(float4) * BT_BATCH +
+                                 sizeof(unsigned short) * BT_BATCH;
+
 __global__ void __launch_bounds__(1024) bt_place_kernel(const pyl_batch_real *__restrict__ reals,
                                                         const pyl_batch_item *__restrict__ items, int n_items,
                                                         const unsigned *__restrict__ tile_base,
                                                         unsigned *__restrict__ cursor, unsigned n_total,
                                                         float4 *__restrict__ rec, unsigned *counter)
 {
-    __shared__ unsigned bcnt[BT_MAX_TILES], gbase[BT_MAX_TILES];
+    extern __shared__ __align__(16) unsigned char praw[];
+    unsigned *bcnt = (unsigned *)praw, *gbase = bcnt + BT_MAX_TILES;
+    float4 *stage = (float4 *)(gbase + BT_MAX_TILES);
+    unsigned short *skey = (unsigned short *)(stage + BT_BATCH);
+    __shared__ unsigned wt[32];
     __shared__ int cur;
     constexpr int U = BT_BATCH / 1024;
+    static_assert(U == 4, "four particles per thread and batch");
+    static_assert(BT_MAX_TILES <= 65536, "bin keys held as 16 bits");
     for (;;) {
         if (threadIdx.x == 0) cur = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -261,20 +342,24 @@ __global__ void __launch_bounds__(1024) bt_place_kernel(const pyl_batch_real *__
             __syncthreads();
             continue;
         }
+        const bool vec = (item.first & 3) == 0 && (((uintptr_t)r.pos) & 15) == 0;
         for (long long s0 = item.first; s0 < end; s0 += BT_BATCH) {
+            const int c = (int)min((long long)BT_BATCH, end - s0);
             for (int t = threadIdx.x; t < ntiles; t += blockDim.x) bcnt[t] = 0u;
             __syncthreads();
             float4 v[U];
             int key[U];
             unsigned rank[U];
+            // thread t takes particles s0 + 4t .. s0 + 4t + 3 (BT_BATCH = 4 x 1024)
+            float p[U][3];
+            load_quad(r.pos, s0 + 4 * threadIdx.x, end, vec, p);
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                const long long i = s0 + threadIdx.x + u * 1024;
+                const long long i = s0 + 4 * threadIdx.x + u;
                 key[u] = -1;
                 if (i < end) {
-                    v[u] = make_float4(__ldg(r.pos + 3 * i), __ldg(r.pos + 3 * i + 1), __ldg(r.pos + 3 * i + 2), 1.0f);
-                    const float p[3] = {v[u].x, v[u].y, v[u].z};
-                    key[u] = bt_key_rt(r.mas, p, r.inv, r.dims, nt);
+                    v[u] = make_float4(p[u][0], p[u][1], p[u][2], 1.0f);
+                    key[u] = bt_key_rt(r.mas, p[u], r.inv, r.dims, nt);
                     rank[u] = atomicAdd(bcnt + key[u], 1u);
                 }
             }
@@ -282,12 +367,20 @@ __global__ void __launch_bounds__(1024) bt_place_kernel(const pyl_batch_real *__
             for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
                 if (bcnt[t]) gbase[t] = atomicAdd(cursor + base + t, bcnt[t]);
             __syncthreads();
+            bt_block_scan4(bcnt, ntiles, wt);                  // bcnt: the batch's run starts
 #pragma unroll
             for (int u = 0; u < U; u++)
                 if (key[u] >= 0) {
-                    const unsigned dst = gbase[key[u]] + rank[u];
-                    if (dst < n_total) rec[dst] = v[u];
+                    const unsigned slot = bcnt[key[u]] + rank[u];
+                    stage[slot] = v[u];
+                    skey[slot] = (unsigned short)key[u];
                 }
+            __syncthreads();
+            for (int sidx = threadIdx.x; sidx < c; sidx += blockDim.x) {
+                const unsigned k = skey[sidx];
+                const unsigned dst = gbase[k] + ((unsigned)sidx - bcnt[k]);
+                if (dst < n_total) rec[dst] = stage[sidx];
+            }
             __syncthreads();
         }
         __syncthreads();
@@ -478,8 +571,9 @@ extern "C" int pyl_ma_batch_tiled(const pyl_batch_real *reals, int n_reals, cons
     PYL_LAUNCH_CHECK();
     bt_scan_kernel<<<1, 1024, 0, st>>>(ws.counts, total_tiles, ws.offsets, ws.cursor);
     PYL_LAUNCH_CHECK();
-    bt_place_kernel<<<grid, 1024, 0, st>>>(reals, items, n_items, tile_base, ws.cursor, (unsigned)total_particles,
-                                           ws.rec, ws.counters + 1);
+    PYL_CUDA(ensure_smem(bt_place_kernel, BT_PLACE_SMEM));
+    bt_place_kernel<<<grid, 1024, BT_PLACE_SMEM, st>>>(reals, items, n_items, tile_base, ws.cursor,
+                                                       (unsigned)total_particles, ws.rec, ws.counters + 1);
     PYL_LAUNCH_CHECK();
     PYL_CUDA(ensure_smem(bt_deposit_kernel, BT_DEPOSIT_SMEM));
     bt_deposit_kernel<<<(unsigned)num_sms(), 1024, BT_DEPOSIT_SMEM, st>>>(
