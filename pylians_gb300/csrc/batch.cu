@@ -410,7 +410,10 @@ __device__ __forceinline__ void bt_deposit_bin(unsigned *smw, const float4 *__re
                                     : fx_support<MAS, 0, E>(p, r.inv, r.halfcell, r.dims, o, C);
                 if (mode == 0) {
                     if (MAS == PYL_MAS_CIC) bad |= (unsigned)!(C[0][1] >= 0.0f && C[1][1] >= 0.0f && C[2][1] >= 0.0f);
-                    seen |= fx_scatter_or<MAS, E>(smw, b0, C);
+                    // z weights times 2^22 (exact): each corner one FFMA into the fixed-point format
+#pragma unroll
+                    for (int q = 0; q < S; q++) C[2][q] = __fmul_rn(C[2][q], FX_SCALE);
+                    seen |= fx_scatter_or<MAS, E, (MAS == PYL_MAS_NGP), true>(smw, b0, C);
                 } else {
                     float_scatter<MAS, E>(facc, b0, C);
                 }
