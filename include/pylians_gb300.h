@@ -239,8 +239,8 @@ int pyl_pk_geometry(int dims, int axis, double *geom, void *workspace, size_t wo
  * its field, its interlaced partner (non-NULL in every record when `interlaced`,
  * ignored otherwise), its own zeroed-by-the-call `sums` (pyl_pk_sums_len(dims, 1)
  * doubles) and MAS exponent.  The sums agree with pyl_pk_bin's item by item to
- * float32 rounding (the same CTA partition and float32 partial sums, whose float
- * atomics run in no fixed order in either call).  The
+ * float32 rounding (the same kernels; with many items each CTA takes more rows
+ * than in a one-field call, so the float32 partial sums group differently).  The
  * workspace (pyl_pk_bin_batch_workspace_size bytes) holds the axis-2 row table and
  * every item's per-CTA partial sums.  A workspace size of 0, and
  * PYL_ERR_UNSUPPORTED from the call, mean that one field's bins do not fit the

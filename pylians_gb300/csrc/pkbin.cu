@@ -1217,16 +1217,51 @@ bool batch_fits(const PkDims &d, int axis, bool inter)
     return sizeof(float) * (size_t)seq_smem(d, axis, inter, seq_chunk(d.nz), true).total <= SMEM_LIMIT;
 }
 
+// CTA partition of a batched launch: the one-field call's one, coarsened while
+// the items together still give several waves (8 CTAs per SM) -- fewer CTAs per
+// item amortise each CTA's tables, zeroing and flushes over more rows, which
+// small grids need.  Axes 0/1: row chunks per plane representative; axis 2:
+// representatives per CTA.
+struct BatchPart {
+    int chunks, rows_per_cta;
+    unsigned blocks;      // CTAs per item
+    int stride;           // partial-sum floats per CTA
+};
+
+inline BatchPart batch_part(const PkDims &d, int axis, int n_items)
+{
+    BatchPart b;
+    const long long target = 8LL * num_sms();
+    b.stride = seq_part(d, axis).stride;
+    if (axis != 2) {
+        const int G = sym_groups(d.dims);
+        const int cmax = sym_chunks(d.dims);
+        int c = 1;
+        while (c < cmax && (long long)G * c * n_items < target) c *= 2;
+        b.chunks = c;
+        b.rows_per_cta = 0;
+        b.blocks = (unsigned)(G * c);
+    } else {
+        const long long rows = ring_rows(d, true);
+        int rpc = RING_ROWS_PER_CTA;
+        while (rpc < 16 * RING_ROWS_PER_CTA && ((rows + 2 * rpc - 1) / (2 * rpc)) * n_items >= target) rpc *= 2;
+        b.chunks = 1;
+        b.rows_per_cta = rpc;
+        b.blocks = (unsigned)((rows + rpc - 1) / rpc);
+    }
+    return b;
+}
+
 // Batched one-field spectra: the axis-2 row table, then each item's per-CTA
-// partial sums (the one-field call's CTA partition).  0: not batchable.
+// partial sums.  0: not batchable.
 extern "C" size_t pyl_pk_bin_batch_workspace_size(int dims, int n_items, int axis, int interlaced)
 {
     if (dims < 2 || dims > 8192 || n_items < 1 || axis < 0 || axis > 2) return 0;
     const PkDims d = pk_dims(dims);
     if (!batch_fits(d, axis, interlaced != 0)) return 0;
-    const SeqPart sp = seq_part(d, axis);
+    const BatchPart bp = batch_part(d, axis, n_items);
     return (axis == 2 ? ring_layout(nullptr, d).bytes : 0) +
-           align256(sizeof(float) * (size_t)sp.blocks * sp.stride * (size_t)n_items);
+           align256(sizeof(float) * (size_t)bp.blocks * bp.stride * (size_t)n_items);
 }
 
 extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims, int axis, int interlaced,
@@ -1261,7 +1296,7 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
     a.items = items;
     for (int f = 0; f < MAX_FIELDS; f++) a.mas_p[f] = 0;
     cudaStream_t st = (cudaStream_t)stream;
-    const SeqPart sp = seq_part(d, axis);
+    const BatchPart bp = batch_part(d, axis, n_items);
     size_t ring_bytes = 0;
     if (axis == 2) {
         const RingWs w = ring_layout(workspace, d);
@@ -1269,20 +1304,18 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
         int rc = build_rings(d, w, true, st);
         if (rc) return rc;
         a.rows = w.rows;
-        a.rows_per_cta = RING_ROWS_PER_CTA;
-        a.chunks = 1;
         a.warp_arrays = 1;
     } else {
-        a.chunks = sym_chunks(dims);
-        a.rows_per_cta = 0;
         a.warp_arrays = 0;
     }
+    a.chunks = bp.chunks;
+    a.rows_per_cta = bp.rows_per_cta;
     a.part = (float *)((char *)workspace + ring_bytes);
-    a.part_stride = sp.stride;
+    a.part_stride = bp.stride;
     pk_items_zero_kernel<<<n_items, 256, 0, st>>>(items, pyl_pk_sums_len(dims, 1));
     PYL_LAUNCH_CHECK();
-    PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)sp.blocks * sp.stride * n_items, st));
-    const dim3 grid(sp.blocks, (unsigned)n_items);
+    PYL_CUDA(cudaMemsetAsync(a.part, 0, sizeof(float) * (size_t)bp.blocks * bp.stride * n_items, st));
+    const dim3 grid(bp.blocks, (unsigned)n_items);
 #define PYL_SEQB(K, I, A)                                                          \
     do {                                                                           \
         PYL_CUDA(ensure_smem(K<I, A, true>, sms));                          \
@@ -1300,9 +1333,9 @@ extern "C" int pyl_pk_bin_batch(const pyl_pk_item *items, int n_items, int dims,
 #undef PYL_SEQB
     PYL_LAUNCH_CHECK();
     const int slots = d.nb3 * 4 + (axis == 2 ? 0 : d.kmax_per + 1);
-    const int groups = 16, per_group = (int)((sp.blocks + groups - 1) / groups);
+    const int groups = 16, per_group = (int)((bp.blocks + groups - 1) / groups);
     pk_part_reduce_kernel<<<dim3((slots + 255) / 256, groups, (unsigned)n_items), 256, 0, st>>>(
-        a.part, (int)sp.blocks, sp.stride, per_group, a.chunks, axis, d, nullptr, items);
+        a.part, (int)bp.blocks, bp.stride, per_group, a.chunks, axis, d, nullptr, items);
     PYL_LAUNCH_CHECK();
     return PYL_OK;
 }
