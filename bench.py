@@ -476,17 +476,18 @@ def bench_zeldovich(reps=3):
 def bench_bispectrum(reps=5):
     """Bispectra of a 256^3 CIC overdensity (1000 Mpc/h, 256^3 uniform particles): k1=0.1,
     k2=0.2 h/Mpc with 32 theta bins, plus 20 equilateral triangles k=0.02..0.4 h/Mpc, all 52
-    triangles through one BkPlan (one R2C, one shell fill, one batched C2R, one grouped
-    reduction per call; the indicator fields' sums are the plan's, made once).  Device
-    time by CUDA events on the launching stream, per stage and for the whole chain; the
-    call time adds the read-back and finalisation.
+    triangles through one BkPlan (one R2C, one shell fill, one batched C2R; the 32-theta
+    group summed in Fourier space from the product of its two shared shells, the
+    equilateral triangles reduced in real space; the indicator fields' sums are the
+    plan's, made once).  Device time by CUDA events on the launching stream, per stage
+    and for the whole chain; the call time adds the read-back and finalisation.
 
     Algorithmic bytes (N_g = N^3, N_h = N^2 (N/2+1) on the input grid; M_g, M_h the same on
-    the reduced side M of the shell fields; S shells):
-      R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill S x 8 M_h (the delta fields
-      written); C2R S (8 M_h + 4 M_g); reduction S x 4 M_g (every shell field read once;
-      the kernel re-reads the fields shared by several triangle groups, from L2)."""
-    import ctypes
+    the reduced side M of the shell fields; R shells needed in real space, G Fourier groups):
+      R2C 4 N_g + 8 N_h; deconvolution 16 N_h; shell fill R x 8 M_h (fields written); C2R
+      R (8 M_h + 4 M_g); triangle sums: the real-space reduction reads each of its fields
+      once (4 M_g each), and each Fourier group reads two fields and writes the product
+      (12 M_g), transforms it (4 M_g + 8 M_h) and reads it back (8 M_h)."""
     import torch
     import pylians_gb300.MAS_library as MASL
     import pylians_gb300.Pk_library as PKL
@@ -512,7 +513,7 @@ def bench_bispectrum(reps=5):
     ev[1].record()
     torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / reps
-    # stages: the launches of BkPlan.run with events between them (S <= 96: one fill call)
+    # stages: the steps of BkPlan.run with events between them
     st = stream_ptr()
     S, T, m = len(plan.bounds), len(plan.tri), plan.side
     se = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
@@ -523,13 +524,11 @@ def bench_bispectrum(reps=5):
         se[1].record()
         _lib.call('pyl_mas_deconvolve', ptr(plan.dk), None, N, plan.mas_p, st)
         se[2].record()
-        _lib.call('pyl_bk_shell_fill', ptr(plan.dk), N, m, ctypes.cast(plan._lo[0], ctypes.c_void_p),
-                  ctypes.cast(plan._hi[0], ctypes.c_void_p), S, ptr(plan.cd), None, ptr(plan.power), st)
+        plan._fill(ptr(plan.dk), plan.cd, None, st)
         se[3].record()
-        _lib.call('pyl_fft_c2r', ptr(plan.cd), ptr(plan.d_real), m, S, st)
+        plan._c2r(plan.cd, plan.d_real, st)
         se[4].record()
-        _lib.call('pyl_bk_triangles', ptr(plan.d_real), None, m, plan.stride, S,
-                  ctypes.cast(plan._tri, ctypes.c_void_p), T, ptr(plan.num), None, st)
+        plan._sums(ptr(plan.dk), False, plan.num, st)
         se[5].record()
         torch.cuda.synchronize()
         acc += [se[k].elapsed_time(se[k + 1]) for k in range(5)]
@@ -541,25 +540,25 @@ def bench_bispectrum(reps=5):
     t_call = (time.perf_counter() - t0) / reps * 1e3
     Ng, Nh = N ** 3, N * N * (N // 2 + 1)
     Mg, Mh = m ** 3, m * m * (m // 2 + 1)
-    pairs = {}
-    for a, b, _ in plan.tri:
-        pairs[(int(a), int(b))] = pairs.get((int(a), int(b)), 0) + 1
-    G = sum(-(-c // 4) for c in pairs.values())
-    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=S * 8.0 * Mh,
-               fft_c2r=S * (8.0 * Mh + 4.0 * Mg), triangles=S * 4.0 * Mg)
+    R, G = plan.R, len(plan._dots)
+    real_fields = len(set(int(x) for x in plan._tri[:3 * plan.n_real]))
+    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=R * 8.0 * Mh,
+               fft_c2r=R * (8.0 * Mh + 4.0 * Mg),
+               triangles=real_fields * 4.0 * Mg + G * (12.0 * Mg + 4.0 * Mg + 16.0 * Mh))
     names = ['fft_r2c', 'deconvolve', 'shell_fill', 'fft_c2r', 'triangles']
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
     hbm = peaks.get('hbm_gbs', 6800.0)
     stages = {nm: dict(ms=float(acc[k]), gbs=alg[nm] / (acc[k] / 1e3) / 1e9,
                        frac=alg[nm] / (acc[k] / 1e3) / 1e9 / hbm) for k, nm in enumerate(names)}
+    dom = max(names, key=lambda nm: stages[nm]['ms'])
     del plan, d
     torch.cuda.empty_cache()
-    return dict(metric='bispectra/s', value=len(tris) / (ms / 1e3), triangles=len(tris), shells=S, groups=G,
-                reduced_side=m, ms_per_call_device=ms, ms_per_call_host=t_call,
-                value_host=len(tris) / (t_call / 1e3), stages=stages,
-                roofline=dict(kernel='triangles', bound='hbm', achieved=stages['triangles']['gbs'], peak=hbm,
-                              unit='GB/s', frac=stages['triangles']['frac']),
+    return dict(metric='bispectra/s', value=len(tris) / (ms / 1e3), triangles=len(tris), shells=S,
+                real_space_shells=R, fourier_groups=G, reduced_side=m, ms_per_call_device=ms,
+                ms_per_call_host=t_call, value_host=len(tris) / (t_call / 1e3), stages=stages,
+                roofline=dict(kernel=dom, bound='hbm', achieved=stages[dom]['gbs'], peak=hbm, unit='GB/s',
+                              frac=stages[dom]['frac']),
                 workload='Bk 256^3 CIC, 32-theta sweep + 20 equilateral',
                 timing='device: CUDA events around BkPlan.run; host: run + read-back + finalisation')
 

@@ -267,7 +267,8 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  * (the integer form of  k_min <= |k| < k_max  in units of kF, :73-77,116-118).
  * pyl_bk_shell_fill reads the deconvolved half-complex dims^3 field and writes,
  * for each shell, delta_s (complex64) and the indicator I_s (1+0i) as half grids
- * of side out_dims at out_delta + s*half, out_ind + s*half (half =
+ * of side out_dims at out_delta + f*half, out_ind + f*half with f = host_slot[s]
+ * (host_slot NULL: f = s; f = -1: the shell's power only, no field) (half =
  * out_dims*out_dims*(out_dims/2+1), mode (kx, ky, kz) at (kx mod out_dims,
  * ky mod out_dims, kz)), and power[2*s] = sum_x delta_s(x)^2 / dims^3,
  * power[2*s+1] = sum_x I_s(x)^2 / dims^3 on the dims^3 grid (float64, via
@@ -292,11 +293,28 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  */
 #define PYL_BK_MAX_SHELLS 96
 int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const int64_t *host_k2_lo,
-                      const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
-                      double *power, void *stream);
+                      const int64_t *host_k2_hi, const int *host_slot, int n_shells, void *out_delta,
+                      void *out_ind, double *power, void *stream);
 int pyl_bk_triangles(const float *d_fields, const float *i_fields, int dims, int64_t field_stride,
                      int n_shells, const int *host_tri, int n_tri, double *num, double *den,
                      void *stream);
+
+/* Triangle sums in Fourier space (no counterpart in the reference, which reduces
+ * every triangle in real space, bispectrum_library.pyx:162-190).  For triangles
+ * sharing their first two shells (a, b): pyl_bk_product forms P_ab = d_a d_b on the
+ * out_dims^3 grid (float32, 16-byte aligned buffers), the caller transforms it
+ * (pyl_fft_r2c) into prod_hat, and pyl_bk_shell_dots adds to out[host_dst[t]]
+ *   (1/out_dims^3) sum over the stored modes k of triangle t's third shell
+ *   (host_k2_lo[t] <= k^2 < host_k2_hi[t]) of w Re(v(k) conj(prod_hat(k))),
+ * w = 2 for modes standing for a conjugate pair (0 < kz < out_dims/2), else 1,
+ * v the deconvolved dims^3 field dk, or 1 (the indicator) when dk is NULL.  By
+ * Parseval that is sum_x d_a d_b d_c over the out_dims^3 cells, what
+ * pyl_bk_triangles reduces, so a group of triangles needs the real-space fields
+ * of its first two shells only.  out is not zeroed (accumulates).  At most
+ * PYL_BK_MAX_SHELLS triangles per call; out_dims as for pyl_bk_shell_fill. */
+int pyl_bk_product(const float *a, const float *b, float *out, int64_t n, void *stream);
+int pyl_bk_shell_dots(const void *dk, int dims, const void *prod_hat, int out_dims, const int64_t *host_k2_lo,
+                      const int64_t *host_k2_hi, const int *host_dst, int n_tri, double *out, void *stream);
 
 /* ---- learned aliasing correction (no counterpart in the reference) ----------------
  * MLP 4 -> 64 -> 64 -> 64 -> 1 with tanh hidden layers, BF16 weights and FP32

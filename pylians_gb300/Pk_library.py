@@ -464,20 +464,30 @@ def bk_side(dims, bounds):
 
 class BkPlan(object):
     """Bispectra of a fixed triangle set (k1, k2, k3 in h/Mpc) on dims^3 fields: shells,
-    their exact integer bounds, the reduced grid side, triangle index lists and every
-    device buffer are set up once, and so are the indicator fields' triple sums
-    (sum_x I_a I_b I_c depends only on the shells: filled, transformed and reduced by
-    the same kernels as the delta fields, once per plan).  run(delta) enqueues the
-    data-dependent chain on one stream (R2C, MAS deconvolution, delta shell fill,
-    batched C2R of the delta shell fields, grouped triple-product sums) with no host
-    synchronisation, so capture() can record it as a CUDA graph; result() reads the
-    sums back and finalises B, Q and the shell powers (bispectrum_library.pyx:132-190)."""
+    their exact integer bounds, the reduced grid side, triangle groups and every device
+    buffer are set up once, and so are the indicator fields' triple sums (sum_x I_a I_b
+    I_c depends only on the shells; made once per plan by the same kernels).
+
+    Triangles sharing their first two shells (a, b) form a group.  A group of several
+    triangles is summed in Fourier space: P_ab = d_a d_b on the reduced grid, its R2C,
+    and for each triangle the sum over its third shell's modes of Re(delta conj(P_ab^))
+    (Parseval: the real-space triple sum), so only d_a and d_b need real space.  A
+    lone triangle is reduced in real space (pyl_bk_triangles) from the C2R of its three
+    shells.  method='real' or 'fourier' forces one way for every group.
+
+    run(delta) enqueues the data-dependent chain on one stream (R2C, MAS deconvolution,
+    shell fill of the shells needed in real space and every shell's power, batched C2R,
+    the two kinds of triangle sums) with no host synchronisation, so capture() can
+    record it as a CUDA graph; result() reads the sums back and finalises B, Q and the
+    shell powers (bispectrum_library.pyx:132-190)."""
 
     MAX_SHELLS = 96
 
-    def __init__(self, dims, BoxSize, triangles, MAS='CIC', device=None, side=None):
+    def __init__(self, dims, BoxSize, triangles, MAS='CIC', device=None, side=None, method='auto'):
         require_cuda()
         import ctypes
+        if method not in ('auto', 'real', 'fourier'):
+            raise ValueError("method must be 'auto', 'real' or 'fourier'")
         self.dims, self.BoxSize, self.MAS = int(dims), float(BoxSize), MAS
         self.device = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
         kF = frequencies(BoxSize, dims)[0]
@@ -500,19 +510,54 @@ class BkPlan(object):
         self.half = m * m * (m // 2 + 1)
         self.cells = m ** 3
         self.stride = (self.cells + 3) // 4 * 4
+
+        # groups by (a, b); internal triangle order: real-space triangles, then the
+        # Fourier groups one after the other (result() restores the caller's order)
+        groups = {}
+        for t, (a, b, c) in enumerate(tri_idx):
+            groups.setdefault((a, b), []).append(t)
+        fourier = [(ab, ts) for ab, ts in groups.items()
+                   if method == 'fourier' or (method == 'auto' and len(ts) >= 2)]
+        in_fourier = set(t for _, ts in fourier for t in ts)
+        real_ts = [t for t in range(T) if t not in in_fourier]
+        needed = sorted(set(s for ab, _ in fourier for s in ab) |
+                        set(s for t in real_ts for s in tri_idx[t]))
+        slot = {s_: i for i, s_ in enumerate(needed)}
+        self.order = np.array(real_ts + [t for _, ts in fourier for t in ts], dtype=np.int64)
+        self.n_real, self.R = len(real_ts), len(needed)
+        self.method = method
+
         dev = self.device
         self.dk = torch.empty(_half_shape(self.dims), dtype=torch.complex64, device=dev)
-        self.cd = torch.empty((S, self.half), dtype=torch.complex64, device=dev)
-        self.d_real = torch.empty(S * self.stride, dtype=torch.float32, device=dev)
+        self.cd = torch.empty((max(self.R, 1), self.half), dtype=torch.complex64, device=dev)
+        self.d_real = torch.empty(max(self.R, 1) * self.stride, dtype=torch.float32, device=dev)
         self.power = torch.empty(2 * S, dtype=torch.float64, device=dev)
-        self.num = torch.empty(T, dtype=torch.float64, device=dev)
+        self.num = torch.empty(T, dtype=torch.float64, device=dev)       # internal order
         self.den = torch.empty(T, dtype=torch.float64, device=dev)
+        if fourier:
+            self.prod = torch.empty(self.stride, dtype=torch.float32, device=dev)
+            self.prod_hat = torch.empty(self.half, dtype=torch.complex64, device=dev)
+        I64 = ctypes.c_int64
         ch = range(0, S, self.MAX_SHELLS)
-        self._lo = [(ctypes.c_int64 * min(self.MAX_SHELLS, S - s0))(*[b[0] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
+        self._lo = [(I64 * min(self.MAX_SHELLS, S - s0))(*[b[0] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
                     for s0 in ch]
-        self._hi = [(ctypes.c_int64 * min(self.MAX_SHELLS, S - s0))(*[b[1] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
+        self._hi = [(I64 * min(self.MAX_SHELLS, S - s0))(*[b[1] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
                     for s0 in ch]
-        self._tri = (ctypes.c_int * (3 * T))(*[int(i) for t in tri_idx for i in t])
+        self._slot = [(ctypes.c_int * min(self.MAX_SHELLS, S - s0))(
+            *[slot.get(s_, -1) for s_ in range(s0, min(S, s0 + self.MAX_SHELLS))]) for s0 in ch]
+        self._tri = (ctypes.c_int * max(3 * self.n_real, 1))(*[slot[s_] for t in real_ts for s_ in tri_idx[t]])
+        # Fourier calls: (slot a, slot b, c bounds, output indices), at most MAX_SHELLS triangles each
+        self._dots = []
+        pos = self.n_real
+        for (a, b), ts in fourier:
+            for j0 in range(0, len(ts), self.MAX_SHELLS):
+                part = ts[j0:j0 + self.MAX_SHELLS]
+                n = len(part)
+                cb = [self.bounds[tri_idx[t][2]] for t in part]
+                self._dots.append((slot[a], slot[b], n, (I64 * n)(*[x[0] for x in cb]),
+                                   (I64 * n)(*[x[1] for x in cb]),
+                                   (ctypes.c_int * n)(*range(pos, pos + n))))
+                pos += n
         self.mas_p = MAS_function(MAS)
         self.graph = None
         self._indicator_sums()
@@ -523,45 +568,63 @@ class BkPlan(object):
         for j, s0 in enumerate(range(0, S, self.MAX_SHELLS)):
             ns = min(self.MAX_SHELLS, S - s0)
             _lib.call('pyl_bk_shell_fill', dk, self.dims, self.side, ctypes.cast(self._lo[j], ctypes.c_void_p),
-                      ctypes.cast(self._hi[j], ctypes.c_void_p), ns,
-                      ptr(out_delta[s0]) if out_delta is not None else None,
-                      ptr(out_ind[s0]) if out_ind is not None else None, ptr(self.power[2 * s0:]), st)
+                      ctypes.cast(self._hi[j], ctypes.c_void_p), ctypes.cast(self._slot[j], ctypes.c_void_p), ns,
+                      ptr(out_delta) if out_delta is not None else None,
+                      ptr(out_ind) if out_ind is not None else None, ptr(self.power[2 * s0:]), st)
 
     def _c2r(self, spec, real, st):
-        m, S = self.side, len(self.bounds)
+        m, R = self.side, self.R
+        if R == 0:
+            return
         if self.stride == self.cells:
-            _lib.call('pyl_fft_c2r', ptr(spec), ptr(real), m, S, st)
+            _lib.call('pyl_fft_c2r', ptr(spec), ptr(real), m, R, st)
         else:
-            for s in range(S):
+            for s in range(R):
                 _lib.call('pyl_fft_c2r', ptr(spec[s]), ptr(real[s * self.stride:]), m, 1, st)
 
-    def _indicator_sums(self):
-        """den[t] = sum_x I_a I_b I_c on the reduced grid, once: the indicator fields are
-        filled into the delta buffers (which every run overwrites), transformed and
-        reduced, with no delta input."""
+    def _sums(self, dk, indicator, out, st):
+        """Triangle sums of the fields in cd / d_real (delta fields, or the indicator
+        fields when `indicator`) into out (internal order)."""
         import ctypes
+        m = self.side
+        if self.n_real:
+            d_f, i_f = (None, ptr(self.d_real)) if indicator else (ptr(self.d_real), None)
+            o_num, o_den = (None, ptr(out)) if indicator else (ptr(out), None)
+            _lib.call('pyl_bk_triangles', d_f, i_f, m, self.stride, max(self.R, 1),
+                      ctypes.cast(self._tri, ctypes.c_void_p), self.n_real, o_num, o_den, st)
+        if self._dots:
+            out[self.n_real:].zero_()
+            for sa, sb, n, lo, hi, dst in self._dots:
+                _lib.call('pyl_bk_product', ptr(self.d_real[sa * self.stride:]), ptr(self.d_real[sb * self.stride:]),
+                          ptr(self.prod), self.cells, st)
+                _lib.call('pyl_fft_r2c', ptr(self.prod), ptr(self.prod_hat), m, 1, st)
+                _lib.call('pyl_bk_shell_dots', None if indicator else dk, self.dims, ptr(self.prod_hat), m,
+                          ctypes.cast(lo, ctypes.c_void_p), ctypes.cast(hi, ctypes.c_void_p),
+                          ctypes.cast(dst, ctypes.c_void_p), n, ptr(out), st)
+
+    def _indicator_sums(self):
+        """den = sum_x I_a I_b I_c on the reduced grid, once: the indicator fields are
+        filled into the delta buffers (which every run overwrites), transformed and
+        summed, with no delta input."""
         with torch.cuda.device(self.device):
             st = stream_ptr(None)
             self._fill(None, None, self.cd, st)
             self._c2r(self.cd, self.d_real, st)
-            _lib.call('pyl_bk_triangles', None, ptr(self.d_real), self.side, self.stride, len(self.bounds),
-                      ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), None, ptr(self.den), st)
+            self._sums(None, True, self.den, st)
 
     def run(self, delta, stream=None):
         """Enqueue the chain on `delta` (a dims^3 float32 grid); nothing waits on the host."""
-        import ctypes
         x = as_device_f32(delta, 'delta')
         if tuple(x.shape) != (self.dims,) * 3:
             raise ValueError('delta must be a %d^3 grid' % self.dims)
         self._x = x
         st = stream_ptr(stream)
-        d, m, S = self.dims, self.side, len(self.bounds)
+        d = self.dims
         _lib.call('pyl_fft_r2c', ptr(x), ptr(self.dk), d, 1, st)
         _lib.call('pyl_mas_deconvolve', ptr(self.dk), None, d, self.mas_p, st)
         self._fill(ptr(self.dk), self.cd, None, st)
         self._c2r(self.cd, self.d_real, st)
-        _lib.call('pyl_bk_triangles', ptr(self.d_real), None, m, self.stride, S,
-                  ctypes.cast(self._tri, ctypes.c_void_p), len(self.tri), ptr(self.num), None, st)
+        self._sums(ptr(self.dk), False, self.num, st)
 
     def capture(self, delta):
         """Record run(delta) (fixed address) as a CUDA graph; replay() relaunches it."""
@@ -581,7 +644,9 @@ class BkPlan(object):
         L, d = self.BoxSize, self.dims
         pw = self.power.cpu().numpy()
         P = (pw[0::2] / pw[1::2]) * (L / d ** 2) ** 3
-        B = (self.num.cpu().numpy() / self.den.cpu().numpy()) * (L ** 2 / d ** 3) ** 3
+        ratio = np.empty(len(self.tri))
+        ratio[self.order] = self.num.cpu().numpy() / self.den.cpu().numpy()
+        B = ratio * (L ** 2 / d ** 3) ** 3
         t = self.tri
         P1, P2, P3 = P[t[:, 0]], P[t[:, 1]], P[t[:, 2]]
         Q = B / (P1 * P2 + P1 * P3 + P2 * P3)

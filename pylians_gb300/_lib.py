@@ -50,7 +50,9 @@ SIGNATURES = {
     'pyl_pk_bin_batch_workspace_size': (_SZ, [_I, _I, _I, _I]),
     'pyl_pk_bin_batch': (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
     'pyl_mas_deconvolve': (_I, [_P, _P, _I, _I, _P]),
-    'pyl_bk_shell_fill': (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _P, _P]),
+    'pyl_bk_shell_fill': (_I, [_P, _I, _I, _P, _P, _P, _I, _P, _P, _P, _P]),
+    'pyl_bk_product': (_I, [_P, _P, _P, _I64, _P]),
+    'pyl_bk_shell_dots': (_I, [_P, _I, _P, _I, _P, _P, _P, _I, _P, _P]),
     'pyl_bk_triangles': (_I, [_P, _P, _I, _I64, _I, _P, _I, _P, _P, _P]),
     'pyl_mlp_param_count': (_I, []),
     'pyl_mlp_forward': (_I, [_P, _P, _I, _P, _P, _P]),

@@ -33,6 +33,7 @@ namespace {
 
 struct ShellBounds {
     long long lo[PYL_BK_MAX_SHELLS], hi[PYL_BK_MAX_SHELLS];
+    int slot[PYL_BK_MAX_SHELLS];     // output field of each shell, -1: power only
     int n;
 };
 
@@ -73,11 +74,12 @@ __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restric
         const double p2 = w * ((double)v.x * v.x + (double)v.y * v.y);
         for (int s = 0; s < sb.n; s++) {
             if (n2 >= sb.lo[s] && n2 < sb.hi[s]) {
+                const long long f = sb.slot[s];
                 if (FD) {
-                    od[s * half_m + dst] = v;
+                    if (f >= 0) od[f * half_m + dst] = v;
                     atomicAdd(acc + 2 * s, p2);
                 }
-                if (FI) oi[s * half_m + dst] = make_float2(1.0f, 0.0f);
+                if (FI && f >= 0) oi[f * half_m + dst] = make_float2(1.0f, 0.0f);
                 atomicAdd(acc + 2 * s + 1, w);
             }
         }
@@ -193,14 +195,83 @@ __global__ void __launch_bounds__(256, 3) triangle_group_kernel(const float *__r
     }
 }
 
+// out = a * b, elementwise over n floats (the float32 product the real-space
+// reduction forms first, d_a d_b).
+__global__ void __launch_bounds__(256) bk_product_kernel(const float *__restrict__ a, const float *__restrict__ b,
+                                                         float *__restrict__ out, long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long n4 = n / 4;
+    const float4 *a4 = (const float4 *)a, *b4 = (const float4 *)b;
+    float4 *o4 = (float4 *)out;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float4 x = __ldg(a4 + i), y = __ldg(b4 + i);
+        o4[i] = make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w);
+    }
+    for (long long i = n4 * 4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = a[i] * b[i];
+}
+
+// Triangle sums in Fourier space: for triangle t with third shell bounds
+// [lo[t], hi[t]), out[t] = (1/M^3) sum over the stored modes k of that shell of
+// w Re(v(k) conj(P(k))), where P is the R2C of the product field P_ab(x) on the
+// M^3 grid, v the deconvolved dims^3 field (or 1 for the indicator) and w = 2 for
+// modes standing for a conjugate pair (0 < kz < M/2), 1 otherwise.  By Parseval
+// that is sum_x P_ab(x) d_c(x) over the M^3 cells, the real-space triple sum.
+// Modes are walked as in shell_fill_kernel (the cube |kx|, |ky|, kz <= K).
+struct TriBounds {
+    long long lo[PYL_BK_MAX_SHELLS], hi[PYL_BK_MAX_SHELLS];
+    int dst[PYL_BK_MAX_SHELLS];      // output index of each triangle
+    int n;
+};
+
+__global__ void __launch_bounds__(256) shell_dot_kernel(const float2 *__restrict__ dk, int dims, int K, int M,
+                                                        TriBounds tb, const float2 *__restrict__ prod_hat,
+                                                        double *out)
+{
+    __shared__ double acc[PYL_BK_MAX_SHELLS];
+    for (int i = threadIdx.x; i < tb.n; i += blockDim.x) acc[i] = 0.0;
+    __syncthreads();
+    const int nz = dims / 2 + 1, mz = M / 2 + 1;
+    const int klo = -min(K, (dims - 1) / 2), khi = min(K, dims / 2), kzhi = min(K, dims / 2);
+    const int side = khi - klo + 1;
+    const long long cube = (long long)side * side * (kzhi + 1);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const bool even_m = (M & 1) == 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cube; i += stride) {
+        const int kz = (int)(i % (kzhi + 1));
+        const long long rr = i / (kzhi + 1);
+        const int ky = (int)(rr % side) + klo, kx = (int)(rr / side) + klo;
+        const long long n2 = (long long)kx * kx + (long long)ky * ky + (long long)kz * kz;
+        bool any = false;
+        for (int t = 0; t < tb.n; t++) any |= (n2 >= tb.lo[t]) & (n2 < tb.hi[t]);
+        if (!any) continue;
+        const long long dst = ((long long)(kx < 0 ? kx + M : kx) * M + (ky < 0 ? ky + M : ky)) * mz + kz;
+        const float2 q = __ldg(prod_hat + dst);
+        float2 v = make_float2(1.0f, 0.0f);
+        if (dk) {
+            const long long src = ((long long)(kx < 0 ? kx + dims : kx) * dims + (ky < 0 ? ky + dims : ky)) * nz + kz;
+            v = __ldg(dk + src);
+        }
+        const double w = (kz == 0 || (even_m && 2 * kz == M)) ? 1.0 : 2.0;
+        const double c = w * ((double)v.x * q.x + (double)v.y * q.y);
+        for (int t = 0; t < tb.n; t++)
+            if (n2 >= tb.lo[t] && n2 < tb.hi[t]) atomicAdd(acc + t, c);
+    }
+    __syncthreads();
+    const double inv = 1.0 / ((double)M * M * M);
+    for (int t = threadIdx.x; t < tb.n; t += blockDim.x)
+        if (acc[t] != 0.0) atomicAdd(out + tb.dst[t], acc[t] * inv);
+}
+
 }  // namespace
 }  // namespace pyl
 
 using namespace pyl;
 
 extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const int64_t *host_k2_lo,
-                                 const int64_t *host_k2_hi, int n_shells, void *out_delta, void *out_ind,
-                                 double *power, void *stream)
+                                 const int64_t *host_k2_hi, const int *host_slot, int n_shells, void *out_delta,
+                                 void *out_ind, double *power, void *stream)
 {
     PYL_CHECK_ARG(power && host_k2_lo && host_k2_hi, "null pointer");
     PYL_CHECK_ARG(out_delta || out_ind, "no output field");
@@ -214,8 +285,12 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
         PYL_CHECK_ARG(host_k2_lo[s] >= 0 && host_k2_hi[s] >= host_k2_lo[s], "bad shell bounds");
         sb.lo[s] = host_k2_lo[s];
         sb.hi[s] = host_k2_hi[s];
+        sb.slot[s] = host_slot ? host_slot[s] : s;
+        PYL_CHECK_ARG(sb.slot[s] >= -1 && sb.slot[s] < n_shells, "slot out of range");
         hi_max = std::max(hi_max, (long long)host_k2_hi[s]);
     }
+    int n_out = 0;                                   // output fields the slots address
+    for (int s = 0; s < n_shells; s++) n_out = std::max(n_out, sb.slot[s] + 1);
     // K: the largest |k| component of any shell mode (k^2 < hi_max)
     int K = 0;
     while ((long long)(K + 1) * (K + 1) < hi_max) K++;
@@ -223,8 +298,8 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
                   "out_dims must equal dims, or exceed 3 K (and 2 K) with K the largest shell wave number");
     const long long half_m = (long long)out_dims * out_dims * (out_dims / 2 + 1);
     cudaStream_t st = (cudaStream_t)stream;
-    if (out_delta) PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half_m * n_shells, st));
-    if (out_ind) PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half_m * n_shells, st));
+    if (out_delta && n_out) PYL_CUDA(cudaMemsetAsync(out_delta, 0, sizeof(float2) * half_m * n_out, st));
+    if (out_ind && n_out) PYL_CUDA(cudaMemsetAsync(out_ind, 0, sizeof(float2) * half_m * n_out, st));
     PYL_CUDA(cudaMemsetAsync(power, 0, sizeof(double) * 2 * n_shells, st));
     const long long side = std::min(K, dims / 2) + std::min(K, (dims - 1) / 2) + 1;
     const long long cube = side * side * (std::min(K, dims / 2) + 1);
@@ -296,3 +371,49 @@ extern "C" int pyl_bk_triangles(const float *d_fields, const float *i_fields, in
     }
     return PYL_OK;
 }
+
+extern "C" int pyl_bk_product(const float *a, const float *b, float *out, int64_t n, void *stream)
+{
+    PYL_CHECK_ARG(a && b && out, "null pointer");
+    PYL_CHECK_ARG(n >= 0, "negative length");
+    PYL_CHECK_ARG(((((uintptr_t)a) | ((uintptr_t)b) | ((uintptr_t)out)) & 15) == 0, "buffers must be 16-byte aligned");
+    if (n == 0) return PYL_OK;
+    long long blocks = (n / 4 + 255) / 256;
+    if (blocks > (long long)num_sms() * 8) blocks = (long long)num_sms() * 8;
+    bk_product_kernel<<<(unsigned)std::max(1LL, blocks), 256, 0, (cudaStream_t)stream>>>(a, b, out, n);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+
+extern "C" int pyl_bk_shell_dots(const void *dk, int dims, const void *prod_hat, int out_dims,
+                                 const int64_t *host_k2_lo, const int64_t *host_k2_hi, const int *host_dst,
+                                 int n_tri, double *out, void *stream)
+{
+    PYL_CHECK_ARG(prod_hat && out && host_k2_lo && host_k2_hi && host_dst, "null pointer");
+    PYL_CHECK_ARG(dims >= 2 && dims <= 4096, "dims out of range");
+    PYL_CHECK_ARG(n_tri >= 1 && n_tri <= PYL_BK_MAX_SHELLS, "1..96 triangles per call");
+    TriBounds tb;
+    tb.n = n_tri;
+    long long hi_max = 0;
+    for (int t = 0; t < n_tri; t++) {
+        PYL_CHECK_ARG(host_k2_lo[t] >= 0 && host_k2_hi[t] >= host_k2_lo[t], "bad shell bounds");
+        PYL_CHECK_ARG(host_dst[t] >= 0, "negative output index");
+        tb.lo[t] = host_k2_lo[t];
+        tb.hi[t] = host_k2_hi[t];
+        tb.dst[t] = host_dst[t];
+        hi_max = std::max(hi_max, (long long)host_k2_hi[t]);
+    }
+    int K = 0;
+    while ((long long)(K + 1) * (K + 1) < hi_max) K++;
+    PYL_CHECK_ARG(out_dims == dims || (2 * K < out_dims && 3 * K < out_dims && out_dims <= dims),
+                  "out_dims must equal dims, or exceed 3 K (and 2 K) with K the largest shell wave number");
+    const long long side = std::min(K, dims / 2) + std::min(K, (dims - 1) / 2) + 1;
+    const long long cube = side * side * (std::min(K, dims / 2) + 1);
+    long long blocks = (cube + 255) / 256;
+    if (blocks > (long long)num_sms() * 8) blocks = (long long)num_sms() * 8;
+    shell_dot_kernel<<<(unsigned)std::max(1LL, blocks), 256, 0, (cudaStream_t)stream>>>(
+        (const float2 *)dk, dims, K, out_dims, tb, (const float2 *)prod_hat, out);
+    PYL_LAUNCH_CHECK();
+    return PYL_OK;
+}
+

@@ -97,24 +97,38 @@ def test_pk_batch_sizes_and_arguments(lib):
 def test_bk_rejects_bad_arguments(lib):
     buf = ctypes.c_void_p(16)
     lo = (ctypes.c_int64 * 1)(1)
-    assert lib.pyl_bk_shell_fill(buf, 32, 32, lo, lo, 0, buf, buf, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(buf, 32, 32, lo, lo, None, 0, buf, buf, buf, None) == 1
     # a reduced side must exceed 3 K (here K = 9 for k^2 < 90): 27 is too small
     hi = (ctypes.c_int64 * 1)(90)
-    assert lib.pyl_bk_shell_fill(buf, 64, 27, lo, hi, 1, buf, buf, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(buf, 64, 27, lo, hi, None, 1, buf, buf, buf, None) == 1
     assert 'out_dims' in lib.pyl_last_error().decode()
-    assert lib.pyl_bk_shell_fill(buf, 64, 80, lo, hi, 1, buf, buf, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(buf, 64, 80, lo, hi, None, 1, buf, buf, buf, None) == 1
     tri = (ctypes.c_int * 3)(0, 0, 5)
     assert lib.pyl_bk_triangles(buf, buf, 16, 4096, 2, tri, 1, buf, buf, None) == 1
     # either field set may be omitted, not both; each set needs its sum buffer
-    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, 1, None, None, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, None, 1, None, None, buf, None) == 1
     assert 'no output' in lib.pyl_last_error().decode()
-    assert lib.pyl_bk_shell_fill(None, 64, 64, lo, hi, 1, buf, None, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(None, 64, 64, lo, hi, None, 1, buf, None, buf, None) == 1
     assert 'need dk' in lib.pyl_last_error().decode()
     tri = (ctypes.c_int * 3)(0, 0, 1)
     assert lib.pyl_bk_triangles(None, None, 16, 4096, 2, tri, 1, buf, buf, None) == 1
     assert lib.pyl_bk_triangles(buf, None, 16, 4096, 2, tri, 1, None, buf, None) == 1
     assert 'sum buffer' in lib.pyl_last_error().decode()
     assert lib.pyl_bk_triangles(None, buf, 16, 4096, 2, tri, 1, buf, None, None) == 1
+    # slots address output fields or -1 (power only); nothing past the shell count
+    slot = (ctypes.c_int * 1)(1)
+    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, slot, 1, buf, None, buf, None) == 1
+    assert 'slot' in lib.pyl_last_error().decode()
+    # Fourier-space sums: buffers, bounds, output indices, the reduced side
+    assert lib.pyl_bk_product(buf, buf, None, 10, None) == 1
+    assert lib.pyl_bk_product(ctypes.c_void_p(20), buf, buf, 10, None) == 1
+    assert 'aligned' in lib.pyl_last_error().decode()
+    dst = (ctypes.c_int * 1)(0)
+    assert lib.pyl_bk_shell_dots(buf, 64, buf, 64, lo, hi, dst, 0, buf, None) == 1
+    assert lib.pyl_bk_shell_dots(buf, 64, buf, 27, lo, hi, dst, 1, buf, None) == 1
+    assert 'out_dims' in lib.pyl_last_error().decode()
+    neg = (ctypes.c_int * 1)(-1)
+    assert lib.pyl_bk_shell_dots(buf, 64, buf, 64, lo, hi, neg, 1, buf, None) == 1
 
 
 def test_python_facade_errors_without_gpu():

@@ -114,3 +114,30 @@ def test_bk_plan_graph_replay(PKL):
     got = plan.result()
     for a, b in zip(got, ref):
         np.testing.assert_allclose(a, b, rtol=1e-12, atol=0)
+
+
+def test_fourier_groups_equal_real_space(PKL):
+    """Triangles sharing (k1, k2) summed in Fourier space (the R2C of d_1 d_2 against each
+    third shell's modes, Parseval) give the real-space triple sums: every group both
+    ways, and the default mix, agree within float32 rounding (1e-5 of the largest |B|),
+    numerators and the plan's indicator sums alike; the oracle pins one sweep."""
+    rng = np.random.default_rng(23)
+    N, L = 96, 1000.0
+    d = rng.standard_normal((N, N, N)).astype(np.float32)
+    d = (d + 0.4 * d * d).astype(np.float32)
+    theta = np.linspace(0.2, 3.0, 9)
+    k1, k2 = 0.05, 0.08
+    k3 = np.sqrt((k2 * np.sin(theta)) ** 2 + (k2 * np.cos(theta) + k1) ** 2)
+    tris = [(k1, k2, float(x)) for x in k3] + [(0.1, 0.1, 0.1), (0.06, 0.09, 0.07)]
+    out = {}
+    for method in ('real', 'fourier', 'auto'):
+        plan = PKL.BkPlan(N, L, tris, 'CIC', method=method)
+        plan.run(d)
+        out[method] = plan.result()
+    assert len(PKL.BkPlan(N, L, tris, 'CIC')._dots) == 1      # the sweep, in Fourier space
+    Br = out['real'][0]
+    for method in ('fourier', 'auto'):
+        assert np.abs(out[method][0] - Br).max() <= 1e-5 * np.abs(Br).max(), method
+        np.testing.assert_allclose(out[method][2], out['real'][2], rtol=1e-12)
+    o = O.Bk(d, L, k1, k2, theta, 'CIC', 1)
+    assert np.all(np.abs(out['auto'][0][:9] - o.B) <= 1e-3 * np.abs(o.B).max())
