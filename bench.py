@@ -512,10 +512,20 @@ def bench_bispectrum(reps=5):
         plan.run(d)
     ev[1].record()
     torch.cuda.synchronize()
+    ms_eager = ev[0].elapsed_time(ev[1]) / reps
+    # the chain as one CUDA graph (BkPlan.capture): launches without host gaps
+    plan.capture(d)
+    plan.replay()
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        plan.replay()
+    ev[1].record()
+    torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / reps
     # stages: the steps of BkPlan.run with events between them
     st = stream_ptr()
-    S, T, m = len(plan.bounds), len(plan.tri), plan.side
+    S = len(plan.bounds)
     se = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     acc = np.zeros(5)
     for _ in range(reps):
@@ -524,11 +534,15 @@ def bench_bispectrum(reps=5):
         se[1].record()
         _lib.call('pyl_mas_deconvolve', ptr(plan.dk), None, N, plan.mas_p, st)
         se[2].record()
-        plan._fill(ptr(plan.dk), plan.cd, None, st)
+        plan._powers(ptr(plan.dk), st)
+        for c in plan._classes:
+            plan._fill(c, ptr(plan.dk), st)
         se[3].record()
-        plan._c2r(plan.cd, plan.d_real, st)
+        for c in plan._classes:
+            plan._c2r(c, st)
         se[4].record()
-        plan._sums(ptr(plan.dk), False, plan.num, st)
+        for c in plan._classes:
+            plan._sums(c, ptr(plan.dk), False, plan.num, st)
         se[5].record()
         torch.cuda.synchronize()
         acc += [se[k].elapsed_time(se[k + 1]) for k in range(5)]
@@ -539,12 +553,14 @@ def bench_bispectrum(reps=5):
         plan.result()
     t_call = (time.perf_counter() - t0) / reps * 1e3
     Ng, Nh = N ** 3, N * N * (N // 2 + 1)
-    Mg, Mh = m ** 3, m * m * (m // 2 + 1)
-    R, G = plan.R, len(plan._dots)
-    real_fields = len(set(int(x) for x in plan._tri[:3 * plan.n_real]))
-    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=R * 8.0 * Mh,
-               fft_c2r=R * (8.0 * Mh + 4.0 * Mg),
-               triangles=real_fields * 4.0 * Mg + G * (12.0 * Mg + 4.0 * Mg + 16.0 * Mh))
+    R, G = plan.R, plan.n_fourier_groups
+    alg = dict(fft_r2c=4.0 * Ng + 8.0 * Nh, deconvolve=16.0 * Nh, shell_fill=0.0, fft_c2r=0.0, triangles=0.0)
+    for c in plan._classes:            # per reduced side M: M_g cells, M_h stored modes
+        Mg, Mh = float(c['cells']), float(c['half'])
+        real_fields = len(set(int(x) for x in c['tri'][:3 * c['n_real']]))
+        alg['shell_fill'] += c['R'] * 8.0 * Mh
+        alg['fft_c2r'] += c['R'] * (8.0 * Mh + 4.0 * Mg)
+        alg['triangles'] += real_fields * 4.0 * Mg + len(c['dots']) * (12.0 * Mg + 4.0 * Mg + 16.0 * Mh)
     names = ['fft_r2c', 'deconvolve', 'shell_fill', 'fft_c2r', 'triangles']
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
@@ -552,15 +568,19 @@ def bench_bispectrum(reps=5):
     stages = {nm: dict(ms=float(acc[k]), gbs=alg[nm] / (acc[k] / 1e3) / 1e9,
                        frac=alg[nm] / (acc[k] / 1e3) / 1e9 / hbm) for k, nm in enumerate(names)}
     dom = max(names, key=lambda nm: stages[nm]['ms'])
+    sides = [int(x) for x in plan.sides]
     del plan, d
     torch.cuda.empty_cache()
     return dict(metric='bispectra/s', value=len(tris) / (ms / 1e3), triangles=len(tris), shells=S,
-                real_space_shells=R, fourier_groups=G, reduced_side=m, ms_per_call_device=ms,
+                real_space_shells=R, fourier_groups=G, reduced_sides=sides,
+                ms_per_call_device=ms, ms_per_call_device_eager=ms_eager,
+                value_eager=len(tris) / (ms_eager / 1e3),
                 ms_per_call_host=t_call, value_host=len(tris) / (t_call / 1e3), stages=stages,
                 roofline=dict(kernel=dom, bound='hbm', achieved=stages[dom]['gbs'], peak=hbm, unit='GB/s',
                               frac=stages[dom]['frac']),
                 workload='Bk 256^3 CIC, 32-theta sweep + 20 equilateral',
-                timing='device: CUDA events around BkPlan.run; host: run + read-back + finalisation')
+                timing='device: CUDA events around replays of the captured BkPlan.run (value) and around '
+                       'eager BkPlan.run (value_eager); host: eager run + read-back + finalisation')
 
 
 def bench_batch(count, steps=3):

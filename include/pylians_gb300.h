@@ -277,10 +277,11 @@ int pyl_mas_deconvolve(void *dk, const void *dk_interlaced, int dims, int mas_p,
  * the shell fields are band-limited, so the triple-product sums over out_dims^3
  * cells are (out_dims/dims)^3 times those over dims^3 cells and B, a ratio of
  * two such sums, is the same.  At most PYL_BK_MAX_SHELLS shells per call.
- * Either output may be NULL: the indicator fields and their sums depend only on
- * the shells, so a plan fills them once (out_delta NULL, dk may then be NULL too;
- * power[2*s] is then 0) and every later call fills the delta fields alone
- * (out_ind NULL; power[2*s+1] is written either way).
+ * Either field set may be left out: the indicator fields and their sums depend
+ * only on the shells, so a plan fills them once (dk and out_delta NULL; power[2*s]
+ * is then 0) and every later call fills the delta fields alone (out_ind NULL);
+ * with every slot -1 and dk given, the call computes the powers alone
+ * (power[2*s+1] is written in every call).
  *
  * pyl_bk_triangles reduces the C2R'd real fields: for triangle t with shells
  * (a,b,c) = host_tri[3t..3t+2], num[t] = sum_x d_a d_b d_c and

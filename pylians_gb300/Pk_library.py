@@ -462,24 +462,37 @@ def bk_side(dims, bounds):
     return m if m < dims else dims
 
 
+def _shell_K(bounds):
+    """Largest |k| component (grid units) of a shell's modes: k^2 < hi."""
+    K = 0
+    while (K + 1) ** 2 < bounds[1]:
+        K += 1
+    return K
+
+
 class BkPlan(object):
     """Bispectra of a fixed triangle set (k1, k2, k3 in h/Mpc) on dims^3 fields: shells,
-    their exact integer bounds, the reduced grid side, triangle groups and every device
+    their exact integer bounds, triangle groups, their reduced grids and every device
     buffer are set up once, and so are the indicator fields' triple sums (sum_x I_a I_b
     I_c depends only on the shells; made once per plan by the same kernels).
 
     Triangles sharing their first two shells (a, b) form a group.  A group of several
-    triangles is summed in Fourier space: P_ab = d_a d_b on the reduced grid, its R2C,
-    and for each triangle the sum over its third shell's modes of Re(delta conj(P_ab^))
-    (Parseval: the real-space triple sum), so only d_a and d_b need real space.  A
-    lone triangle is reduced in real space (pyl_bk_triangles) from the C2R of its three
-    shells.  method='real' or 'fourier' forces one way for every group.
+    triangles is summed in Fourier space: P_ab = d_a d_b on a reduced grid, its R2C, and
+    for each triangle the sum over its third shell's modes of Re(delta conj(P_ab^))
+    (Parseval: the real-space triple sum), so only d_a and d_b need real space.  A lone
+    triangle is reduced in real space (pyl_bk_triangles) from the C2R of its shells.
+    method='real' or 'fourier' forces one way for every group.
+
+    Each group or lone triangle is evaluated on its own reduced grid, the smallest fast
+    side above 3 K with K the largest wave number of its shells (bk_side): the shell
+    fields are band-limited, so the sums there equal the full grid's up to the factor
+    (M/dims)^3 that B, a ratio, cancels.  Groups and triangles of one side share one
+    shell fill, one batched C2R and one reduction; `side` forces one side for all.
 
     run(delta) enqueues the data-dependent chain on one stream (R2C, MAS deconvolution,
-    shell fill of the shells needed in real space and every shell's power, batched C2R,
-    the two kinds of triangle sums) with no host synchronisation, so capture() can
-    record it as a CUDA graph; result() reads the sums back and finalises B, Q and the
-    shell powers (bispectrum_library.pyx:132-190)."""
+    the shell powers, then per side the shell fill, C2R and triangle sums) with no host
+    synchronisation, so capture() can record it as a CUDA graph; result() reads the sums
+    back and finalises B, Q and the shell powers (bispectrum_library.pyx:132-190)."""
 
     MAX_SHELLS = 96
 
@@ -504,113 +517,158 @@ class BkPlan(object):
         self.tri = np.asarray(tri_idx, dtype=np.int64)
         self.bounds = [shell_k2_bounds(lo, hi) for lo, hi in keys]
         S, T = len(self.bounds), len(tri_idx)
-        # side: the reduced grid (bk_side) unless the caller asks for another valid one
-        self.side = int(side) if side else bk_side(self.dims, self.bounds)
-        m = self.side
-        self.half = m * m * (m // 2 + 1)
-        self.cells = m ** 3
-        self.stride = (self.cells + 3) // 4 * 4
+        self.method = method
 
-        # groups by (a, b); internal triangle order: real-space triangles, then the
-        # Fourier groups one after the other (result() restores the caller's order)
+        # units: Fourier groups (several triangles sharing (a, b)) and lone triangles
         groups = {}
         for t, (a, b, c) in enumerate(tri_idx):
             groups.setdefault((a, b), []).append(t)
-        fourier = [(ab, ts) for ab, ts in groups.items()
-                   if method == 'fourier' or (method == 'auto' and len(ts) >= 2)]
-        in_fourier = set(t for _, ts in fourier for t in ts)
-        real_ts = [t for t in range(T) if t not in in_fourier]
-        needed = sorted(set(s for ab, _ in fourier for s in ab) |
-                        set(s for t in real_ts for s in tri_idx[t]))
-        slot = {s_: i for i, s_ in enumerate(needed)}
-        self.order = np.array(real_ts + [t for _, ts in fourier for t in ts], dtype=np.int64)
-        self.n_real, self.R = len(real_ts), len(needed)
-        self.method = method
+        units = []
+        for (a, b), ts in groups.items():
+            if method == 'fourier' or (method == 'auto' and len(ts) >= 2):
+                units.append(('fourier', (a, b), ts))
+            else:
+                units.extend(('real', None, [t]) for t in ts)
+        # reduced side of each unit (the smallest valid one), then a ladder of sides at
+        # least 3/2 apart that every unit rounds up to: a few sides, each with one
+        # shell fill, one batched C2R and one reduction, instead of one per unit
+        own = []
+        for kind, ab, ts in units:
+            sh = [s_ for t in ts for s_ in tri_idx[t]]
+            if side:
+                m = int(side)
+            else:
+                m = _fast_side(3 * max(_shell_K(self.bounds[s_]) for s_ in sh) + 1)
+                m = m if m < self.dims else self.dims
+            own.append(m)
+        ladder = []
+        for m in sorted(set(own), reverse=True):
+            if not ladder or 3 * m <= 2 * ladder[-1]:
+                ladder.append(m)
+        by_side = {}
+        for u, m in zip(units, own):
+            mm = min(x for x in ladder if x >= m)
+            by_side.setdefault(mm, []).append(u)
+        self.sides = sorted(by_side)
+        self.side = max(self.sides)
 
         dev = self.device
+        I64, I32 = ctypes.c_int64, ctypes.c_int
         self.dk = torch.empty(_half_shape(self.dims), dtype=torch.complex64, device=dev)
-        self.cd = torch.empty((max(self.R, 1), self.half), dtype=torch.complex64, device=dev)
-        self.d_real = torch.empty(max(self.R, 1) * self.stride, dtype=torch.float32, device=dev)
         self.power = torch.empty(2 * S, dtype=torch.float64, device=dev)
         self.num = torch.empty(T, dtype=torch.float64, device=dev)       # internal order
         self.den = torch.empty(T, dtype=torch.float64, device=dev)
-        if fourier:
-            self.prod = torch.empty(self.stride, dtype=torch.float32, device=dev)
-            self.prod_hat = torch.empty(self.half, dtype=torch.complex64, device=dev)
-        I64 = ctypes.c_int64
-        ch = range(0, S, self.MAX_SHELLS)
-        self._lo = [(I64 * min(self.MAX_SHELLS, S - s0))(*[b[0] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
-                    for s0 in ch]
-        self._hi = [(I64 * min(self.MAX_SHELLS, S - s0))(*[b[1] for b in self.bounds[s0:s0 + self.MAX_SHELLS]])
-                    for s0 in ch]
-        self._slot = [(ctypes.c_int * min(self.MAX_SHELLS, S - s0))(
-            *[slot.get(s_, -1) for s_ in range(s0, min(S, s0 + self.MAX_SHELLS))]) for s0 in ch]
-        self._tri = (ctypes.c_int * max(3 * self.n_real, 1))(*[slot[s_] for t in real_ts for s_ in tri_idx[t]])
-        # Fourier calls: (slot a, slot b, c bounds, output indices), at most MAX_SHELLS triangles each
-        self._dots = []
-        pos = self.n_real
-        for (a, b), ts in fourier:
-            for j0 in range(0, len(ts), self.MAX_SHELLS):
-                part = ts[j0:j0 + self.MAX_SHELLS]
-                n = len(part)
-                cb = [self.bounds[tri_idx[t][2]] for t in part]
-                self._dots.append((slot[a], slot[b], n, (I64 * n)(*[x[0] for x in cb]),
-                                   (I64 * n)(*[x[1] for x in cb]),
-                                   (ctypes.c_int * n)(*range(pos, pos + n))))
-                pos += n
+        # every shell's power: one fill call per 96 shells, no field written
+        self._pw = []
+        for s0 in range(0, S, self.MAX_SHELLS):
+            bs = self.bounds[s0:s0 + self.MAX_SHELLS]
+            self._pw.append((s0, len(bs), (I64 * len(bs))(*[b[0] for b in bs]), (I64 * len(bs))(*[b[1] for b in bs]),
+                             (I32 * len(bs))(*([-1] * len(bs)))))
+        order = []
+        self._classes = []
+        for m in self.sides:
+            us = by_side[m]
+            needed = sorted(set(s_ for kind, ab, ts in us for s_ in (ab if kind == 'fourier' else tri_idx[ts[0]])))
+            slot = {s_: i for i, s_ in enumerate(needed)}
+            half, cells = m * m * (m // 2 + 1), m ** 3
+            stride = (cells + 3) // 4 * 4
+            c = dict(side=m, R=len(needed), half=half, cells=cells, stride=stride,
+                     cd=torch.empty((len(needed), half), dtype=torch.complex64, device=dev),
+                     d_real=torch.empty(len(needed) * stride, dtype=torch.float32, device=dev),
+                     pw_scratch=torch.empty(2 * len(needed), dtype=torch.float64, device=dev))
+            # fill: the needed shells only (their own cube of modes), in chunks of 96
+            c['fill'] = []
+            for j0 in range(0, len(needed), self.MAX_SHELLS):
+                part = needed[j0:j0 + self.MAX_SHELLS]
+                c['fill'].append((j0, len(part), (I64 * len(part))(*[self.bounds[s_][0] for s_ in part]),
+                                  (I64 * len(part))(*[self.bounds[s_][1] for s_ in part]),
+                                  (I32 * len(part))(*range(j0, j0 + len(part)))))
+            real_ts = [ts[0] for kind, ab, ts in us if kind == 'real']
+            c['real_off'], c['n_real'] = len(order), len(real_ts)
+            c['tri'] = (I32 * max(3 * len(real_ts), 1))(*[slot[s_] for t in real_ts for s_ in tri_idx[t]])
+            order.extend(real_ts)
+            c['dots'] = []
+            c['fourier_off'] = len(order)
+            for kind, (a, b), ts in [u for u in us if u[0] == 'fourier']:
+                for j0 in range(0, len(ts), self.MAX_SHELLS):
+                    part = ts[j0:j0 + self.MAX_SHELLS]
+                    n = len(part)
+                    cb = [self.bounds[tri_idx[t][2]] for t in part]
+                    c['dots'].append((slot[a], slot[b], n, (I64 * n)(*[x[0] for x in cb]),
+                                      (I64 * n)(*[x[1] for x in cb]), (I32 * n)(*range(len(order), len(order) + n))))
+                    order.extend(part)
+            c['n_fourier'] = len(order) - c['fourier_off']
+            if c['dots']:
+                c['prod'] = torch.empty(stride, dtype=torch.float32, device=dev)
+                c['prod_hat'] = torch.empty(half, dtype=torch.complex64, device=dev)
+            self._classes.append(c)
+        self.order = np.array(order, dtype=np.int64)
+        self.R = sum(c['R'] for c in self._classes)                   # shell fields in real space
+        self.n_fourier_groups = sum(len(c['dots']) for c in self._classes)
         self.mas_p = MAS_function(MAS)
         self.graph = None
         self._indicator_sums()
 
-    def _fill(self, dk, out_delta, out_ind, st):
+    def _powers(self, dk, st):
         import ctypes
-        S = len(self.bounds)
-        for j, s0 in enumerate(range(0, S, self.MAX_SHELLS)):
-            ns = min(self.MAX_SHELLS, S - s0)
-            _lib.call('pyl_bk_shell_fill', dk, self.dims, self.side, ctypes.cast(self._lo[j], ctypes.c_void_p),
-                      ctypes.cast(self._hi[j], ctypes.c_void_p), ctypes.cast(self._slot[j], ctypes.c_void_p), ns,
-                      ptr(out_delta) if out_delta is not None else None,
-                      ptr(out_ind) if out_ind is not None else None, ptr(self.power[2 * s0:]), st)
+        for s0, ns, lo, hi, sl in self._pw:
+            _lib.call('pyl_bk_shell_fill', dk, self.dims, self.dims, ctypes.cast(lo, ctypes.c_void_p),
+                      ctypes.cast(hi, ctypes.c_void_p), ctypes.cast(sl, ctypes.c_void_p), ns, None, None,
+                      ptr(self.power[2 * s0:]), st)
 
-    def _c2r(self, spec, real, st):
-        m, R = self.side, self.R
+    def _fill(self, c, dk, st):
+        """The class's needed shells into its half grids: delta fields, or with dk None
+        the indicator fields."""
+        import ctypes
+        for j0, ns, lo, hi, sl in c['fill']:
+            _lib.call('pyl_bk_shell_fill', dk, self.dims, c['side'], ctypes.cast(lo, ctypes.c_void_p),
+                      ctypes.cast(hi, ctypes.c_void_p), ctypes.cast(sl, ctypes.c_void_p), ns,
+                      ptr(c['cd']) if dk is not None else None, None if dk is not None else ptr(c['cd']),
+                      ptr(c['pw_scratch'][2 * j0:]), st)
+
+    def _c2r(self, c, st):
+        m, R = c['side'], c['R']
         if R == 0:
             return
-        if self.stride == self.cells:
-            _lib.call('pyl_fft_c2r', ptr(spec), ptr(real), m, R, st)
+        if c['stride'] == c['cells']:
+            _lib.call('pyl_fft_c2r', ptr(c['cd']), ptr(c['d_real']), m, R, st)
         else:
-            for s in range(R):
-                _lib.call('pyl_fft_c2r', ptr(spec[s]), ptr(real[s * self.stride:]), m, 1, st)
+            for s_ in range(R):
+                _lib.call('pyl_fft_c2r', ptr(c['cd'][s_]), ptr(c['d_real'][s_ * c['stride']:]), m, 1, st)
 
-    def _sums(self, dk, indicator, out, st):
-        """Triangle sums of the fields in cd / d_real (delta fields, or the indicator
-        fields when `indicator`) into out (internal order)."""
+    def _sums(self, c, dk, indicator, out, st):
+        """The class's triangle sums (delta fields, or the indicator fields when
+        `indicator`) into out (internal order)."""
         import ctypes
-        m = self.side
-        if self.n_real:
-            d_f, i_f = (None, ptr(self.d_real)) if indicator else (ptr(self.d_real), None)
-            o_num, o_den = (None, ptr(out)) if indicator else (ptr(out), None)
-            _lib.call('pyl_bk_triangles', d_f, i_f, m, self.stride, max(self.R, 1),
-                      ctypes.cast(self._tri, ctypes.c_void_p), self.n_real, o_num, o_den, st)
-        if self._dots:
-            out[self.n_real:].zero_()
-            for sa, sb, n, lo, hi, dst in self._dots:
-                _lib.call('pyl_bk_product', ptr(self.d_real[sa * self.stride:]), ptr(self.d_real[sb * self.stride:]),
-                          ptr(self.prod), self.cells, st)
-                _lib.call('pyl_fft_r2c', ptr(self.prod), ptr(self.prod_hat), m, 1, st)
-                _lib.call('pyl_bk_shell_dots', None if indicator else dk, self.dims, ptr(self.prod_hat), m,
+        m, stride = c['side'], c['stride']
+        if c['n_real']:
+            d_f, i_f = (None, ptr(c['d_real'])) if indicator else (ptr(c['d_real']), None)
+            o = ptr(out[c['real_off']:])
+            _lib.call('pyl_bk_triangles', d_f, i_f, m, stride, max(c['R'], 1), ctypes.cast(c['tri'], ctypes.c_void_p),
+                      c['n_real'], None if indicator else o, o if indicator else None, st)
+        if c['dots']:
+            out[c['fourier_off']:c['fourier_off'] + c['n_fourier']].zero_()
+            for sa, sb, n, lo, hi, dst in c['dots']:
+                _lib.call('pyl_bk_product', ptr(c['d_real'][sa * stride:]), ptr(c['d_real'][sb * stride:]),
+                          ptr(c['prod']), c['cells'], st)
+                _lib.call('pyl_fft_r2c', ptr(c['prod']), ptr(c['prod_hat']), m, 1, st)
+                _lib.call('pyl_bk_shell_dots', None if indicator else dk, self.dims, ptr(c['prod_hat']), m,
                           ctypes.cast(lo, ctypes.c_void_p), ctypes.cast(hi, ctypes.c_void_p),
                           ctypes.cast(dst, ctypes.c_void_p), n, ptr(out), st)
 
+    def _chain(self, dk, indicator, out, st):
+        for c in self._classes:
+            self._fill(c, dk, st)
+            self._c2r(c, st)
+            self._sums(c, dk, indicator, out, st)
+
     def _indicator_sums(self):
-        """den = sum_x I_a I_b I_c on the reduced grid, once: the indicator fields are
+        """den = sum_x I_a I_b I_c on the reduced grids, once: the indicator fields are
         filled into the delta buffers (which every run overwrites), transformed and
         summed, with no delta input."""
         with torch.cuda.device(self.device):
             st = stream_ptr(None)
-            self._fill(None, None, self.cd, st)
-            self._c2r(self.cd, self.d_real, st)
-            self._sums(None, True, self.den, st)
+            self._chain(None, True, self.den, st)
 
     def run(self, delta, stream=None):
         """Enqueue the chain on `delta` (a dims^3 float32 grid); nothing waits on the host."""
@@ -622,9 +680,8 @@ class BkPlan(object):
         d = self.dims
         _lib.call('pyl_fft_r2c', ptr(x), ptr(self.dk), d, 1, st)
         _lib.call('pyl_mas_deconvolve', ptr(self.dk), None, d, self.mas_p, st)
-        self._fill(ptr(self.dk), self.cd, None, st)
-        self._c2r(self.cd, self.d_real, st)
-        self._sums(ptr(self.dk), False, self.num, st)
+        self._powers(ptr(self.dk), st)
+        self._chain(ptr(self.dk), False, self.num, st)
 
     def capture(self, delta):
         """Record run(delta) (fixed address) as a CUDA graph; replay() relaunches it."""

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) shell_fill_kernel(const float2 *__restric
             if (n2 >= sb.lo[s] && n2 < sb.hi[s]) {
                 const long long f = sb.slot[s];
                 if (FD) {
-                    if (f >= 0) od[f * half_m + dst] = v;
+                    if (f >= 0 && od) od[f * half_m + dst] = v;
                     atomicAdd(acc + 2 * s, p2);
                 }
                 if (FI && f >= 0) oi[f * half_m + dst] = make_float2(1.0f, 0.0f);
@@ -274,8 +274,8 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
                                  void *out_ind, double *power, void *stream)
 {
     PYL_CHECK_ARG(power && host_k2_lo && host_k2_hi, "null pointer");
-    PYL_CHECK_ARG(out_delta || out_ind, "no output field");
     PYL_CHECK_ARG(dk || !out_delta, "the delta fields need dk");
+    PYL_CHECK_ARG(dk || out_ind, "no output: give dk (delta fields and powers) or out_ind");
     PYL_CHECK_ARG(dims >= 2 && dims <= 4096, "dims out of range");
     PYL_CHECK_ARG(n_shells >= 1 && n_shells <= PYL_BK_MAX_SHELLS, "1..96 shells per call");
     ShellBounds sb;
@@ -291,6 +291,7 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
     }
     int n_out = 0;                                   // output fields the slots address
     for (int s = 0; s < n_shells; s++) n_out = std::max(n_out, sb.slot[s] + 1);
+    PYL_CHECK_ARG(n_out == 0 || !dk || out_delta, "slots address delta fields: out_delta is NULL");
     // K: the largest |k| component of any shell mode (k^2 < hi_max)
     int K = 0;
     while ((long long)(K + 1) * (K + 1) < hi_max) K++;
@@ -308,8 +309,8 @@ extern "C" int pyl_bk_shell_fill(const void *dk, int dims, int out_dims, const i
     const unsigned g = (unsigned)std::max(1LL, blocks);
     const float2 *src = (const float2 *)dk;
     float2 *od = (float2 *)out_delta, *oi = (float2 *)out_ind;
-    if (od && oi) shell_fill_kernel<true, true><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
-    else if (od) shell_fill_kernel<true, false><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
+    if (src && oi) shell_fill_kernel<true, true><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
+    else if (src) shell_fill_kernel<true, false><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
     else shell_fill_kernel<false, true><<<g, 256, 0, st>>>(src, dims, K, out_dims, sb, od, oi, power);
     PYL_LAUNCH_CHECK();
     return PYL_OK;

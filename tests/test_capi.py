@@ -106,8 +106,10 @@ def test_bk_rejects_bad_arguments(lib):
     tri = (ctypes.c_int * 3)(0, 0, 5)
     assert lib.pyl_bk_triangles(buf, buf, 16, 4096, 2, tri, 1, buf, buf, None) == 1
     # either field set may be omitted, not both; each set needs its sum buffer
-    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, None, 1, None, None, buf, None) == 1
+    assert lib.pyl_bk_shell_fill(None, 64, 64, lo, hi, None, 1, None, None, buf, None) == 1
     assert 'no output' in lib.pyl_last_error().decode()
+    assert lib.pyl_bk_shell_fill(buf, 64, 64, lo, hi, None, 1, None, None, buf, None) == 1
+    assert 'out_delta is NULL' in lib.pyl_last_error().decode()
     assert lib.pyl_bk_shell_fill(None, 64, 64, lo, hi, None, 1, buf, None, buf, None) == 1
     assert 'need dk' in lib.pyl_last_error().decode()
     tri = (ctypes.c_int * 3)(0, 0, 1)

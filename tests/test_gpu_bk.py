@@ -134,7 +134,7 @@ def test_fourier_groups_equal_real_space(PKL):
         plan = PKL.BkPlan(N, L, tris, 'CIC', method=method)
         plan.run(d)
         out[method] = plan.result()
-    assert len(PKL.BkPlan(N, L, tris, 'CIC')._dots) == 1      # the sweep, in Fourier space
+    assert PKL.BkPlan(N, L, tris, 'CIC').n_fourier_groups == 1      # the sweep, in Fourier space
     Br = out['real'][0]
     for method in ('fourier', 'auto'):
         assert np.abs(out[method][0] - Br).max() <= 1e-5 * np.abs(Br).max(), method
