@@ -462,14 +462,6 @@ def bk_side(dims, bounds):
     return m if m < dims else dims
 
 
-def _shell_K(bounds):
-    """Largest |k| component (grid units) of a shell's modes: k^2 < hi."""
-    K = 0
-    while (K + 1) ** 2 < bounds[1]:
-        K += 1
-    return K
-
-
 class BkPlan(object):
     """Bispectra of a fixed triangle set (k1, k2, k3 in h/Mpc) on dims^3 fields: shells,
     their exact integer bounds, triangle groups, their reduced grids and every device
@@ -535,12 +527,7 @@ class BkPlan(object):
         own = []
         for kind, ab, ts in units:
             sh = [s_ for t in ts for s_ in tri_idx[t]]
-            if side:
-                m = int(side)
-            else:
-                m = _fast_side(3 * max(_shell_K(self.bounds[s_]) for s_ in sh) + 1)
-                m = m if m < self.dims else self.dims
-            own.append(m)
+            own.append(int(side) if side else bk_side(self.dims, [self.bounds[s_] for s_ in sh]))
         ladder = []
         for m in sorted(set(own), reverse=True):
             if not ladder or 3 * m <= 2 * ladder[-1]:
