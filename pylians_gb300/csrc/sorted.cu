@@ -12,9 +12,12 @@
 //   3. run table: for every cell the [start, end) range of its particles in the
 //      sorted order (empty cells keep the all-ones marker).
 //   4. the particles' positions (and weights) gathered into sorted order.
-//   5. gather deposit: one thread per output cell walks the S^3 (interlaced
-//      grid: (S+1)^3) neighbouring base cells in a fixed order and, within each
-//      run, the particles in index order, recomputing the weight of its corner.
+//   5. gather deposit: one thread per output cell walks the S^3 neighbouring
+//      base cells in a fixed order and, within each run, the particles in index
+//      order, recomputing the weight of its corner.  The interlaced grid runs
+//      steps 1-5 again on the shifted positions (its own sort), so its cells
+//      also visit S^3 base cells (a gather over the plain grid's sort visited
+//      (S+1)^3 and checked each corner: 4x the work for TSC).
 //      No atomics: every cell's sum has one fixed order, so the grid is
 //      bit-reproducible whatever the launch configuration; NGP sums each cell's
 //      particles in index order, exactly the serial reference loop.
@@ -100,17 +103,22 @@ __device__ __forceinline__ float sd_weight(float p, float inv, int j, int *first
 }
 
 // ---- 1. keys --------------------------------------------------------------
-template <int MAS>
+// SHIFT: the half-cell-shifted grid's pass, on positions p + halfcell (the
+// float32 sum the other strategies form for the interlaced grid).
+template <int MAS, bool SHIFT>
 __global__ void __launch_bounds__(256) sd_key_kernel(const float *__restrict__ pos, long long n, float inv,
-                                                     int dims, unsigned *__restrict__ keys,
+                                                     float halfcell, int dims, unsigned *__restrict__ keys,
                                                      unsigned *__restrict__ vals)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
     const unsigned d = (unsigned)dims;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const unsigned cx = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i), inv), dims);
-        const unsigned cy = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i + 1), inv), dims);
-        const unsigned cz = (unsigned)wrap_index(sd_first<MAS>(__ldg(pos + 3 * i + 2), inv), dims);
+        float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
+        if (SHIFT)
+            for (int a = 0; a < 3; a++) p[a] = __fadd_rn(p[a], halfcell);
+        const unsigned cx = (unsigned)wrap_index(sd_first<MAS>(p[0], inv), dims);
+        const unsigned cy = (unsigned)wrap_index(sd_first<MAS>(p[1], inv), dims);
+        const unsigned cz = (unsigned)wrap_index(sd_first<MAS>(p[2], inv), dims);
         keys[i] = (cx * d + cy) * d + cz;
         vals[i] = (unsigned)i;
     }
@@ -315,34 +323,40 @@ __global__ void __launch_bounds__(256) sd_fill2_kernel(uint2 *__restrict__ p, lo
 }
 
 // ---- 4. positions in sorted order -------------------------------------------
+template <bool SHIFT>
 __global__ void __launch_bounds__(256) sd_gather_kernel(const float *__restrict__ pos, const float *__restrict__ w,
                                                         const unsigned *__restrict__ vals, long long n,
-                                                        float4 *__restrict__ spos)
+                                                        float halfcell, float4 *__restrict__ spos)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
         const long long i = vals[j];
-        spos[j] = make_float4(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2),
-                              w ? __ldg(w + i) : 1.0f);
+        float4 p = make_float4(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2),
+                               w ? __ldg(w + i) : 1.0f);
+        if (SHIFT) {
+            p.x = __fadd_rn(p.x, halfcell);
+            p.y = __fadd_rn(p.y, halfcell);
+            p.z = __fadd_rn(p.z, halfcell);
+        }
+        spos[j] = p;
     }
 }
 
 // ---- 5. gather deposit ----------------------------------------------------------
 // Thread (x, y, z): threadIdx.x + 32*blockIdx.x = z, threadIdx.y + 8*blockIdx.y = y,
-// blockIdx.z = x.  G = 0: plain grid, offsets 0..S-1 per axis.  G = 1: the
-// half-cell-shifted grid; a particle whose shifted first cell is f0 + delta
-// (delta 0 or 1) reaches cell c from base cell c - l with corner l - delta, so
-// offsets 0..S are visited and the corner is checked.
+// blockIdx.z = x.  The cell sums, over base cells c - (l, m, q) with offsets
+// 0..S-1 per axis in that order and each run's particles in index order, the
+// weight of its corner.  The half-cell-shifted grid runs the same gather on its
+// own sort of the shifted positions (sorted_pass<MAS, true>).
 // scale/base: out = (fold ? out : 0) + sum in fixed order, then
 //   (fold ? sum : out_old + sum * scale).
-template <int MAS, int G, bool WEIGHTED>
+template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restrict__ spos,
                                                          const uint2 *__restrict__ runs, int dims, float inv,
-                                                         float halfcell, float *__restrict__ out, float scale_h,
+                                                         float *__restrict__ out, float scale_h,
                                                          const float *__restrict__ scale_d, int fold)
 {
     constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS;
-    constexpr int R = S + G;                          // offsets visited per axis
     const int z = blockIdx.x * 32 + threadIdx.x;
     const int y = blockIdx.y * 8 + threadIdx.y;
     const int x = blockIdx.z;
@@ -351,44 +365,23 @@ __global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restric
     const long long cell = ((long long)x * d + y) * d + z;
     float acc = fold ? out[cell] : 0.0f;
 #pragma unroll 1
-    for (int l = 0; l < R; l++)
+    for (int l = 0; l < S; l++)
 #pragma unroll 1
-        for (int m = 0; m < R; m++) {
+        for (int m = 0; m < S; m++) {
             const long long row = ((long long)wrap_index(x - l, dims) * d + wrap_index(y - m, dims)) * d;
 #pragma unroll
-            for (int q = 0; q < R; q++) {
+            for (int q = 0; q < S; q++) {
                 const uint2 rr = runs[row + wrap_index(z - q, dims)];
                 if (rr.x == EMPTY) continue;
                 for (unsigned j = rr.x; j < rr.y; j++) {
                     const float4 p = spos[j];
-                    if (G == 0) {
-                        int f;
-                        const float c0 = sd_weight<MAS>(p.x, inv, l, &f);
-                        const float c1 = sd_weight<MAS>(p.y, inv, m, &f);
-                        const float c2 = sd_weight<MAS>(p.z, inv, q, &f);
-                        float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c0, c1), c2);
-                        if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
-                        acc = __fadd_rn(acc, v);
-                    } else {
-                        // corner of the shifted support: offset minus the shift of the first cell
-                        const float pp[3] = {p.x, p.y, p.z};
-                        const int off[3] = {l, m, q};
-                        float c[3];
-                        bool ok = true;
-#pragma unroll
-                        for (int a = 0; a < 3; a++) {
-                            const int f0 = sd_first<MAS>(pp[a], inv);
-                            const float ps = __fadd_rn(pp[a], halfcell);
-                            const int f1 = sd_first<MAS>(ps, inv);
-                            const int corner = off[a] - (f1 > f0 ? 1 : 0);
-                            if (corner < 0 || corner >= S) { ok = false; c[a] = 0.0f; }
-                            else { int f; c[a] = sd_weight<MAS>(ps, inv, corner, &f); }
-                        }
-                        if (!ok) continue;
-                        float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c[0], c[1]), c[2]);
-                        if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
-                        acc = __fadd_rn(acc, v);
-                    }
+                    int f;
+                    const float c0 = sd_weight<MAS>(p.x, inv, l, &f);
+                    const float c1 = sd_weight<MAS>(p.y, inv, m, &f);
+                    const float c2 = sd_weight<MAS>(p.z, inv, q, &f);
+                    float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c0, c1), c2);
+                    if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
+                    acc = __fadd_rn(acc, v);
                 }
             }
         }
@@ -439,14 +432,15 @@ inline unsigned blocks_for(long long n, int threads, int per_sm)
     return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-template <int MAS>
-int sorted_run(const float *pos, const float *w, long long n, float *grid, float *grid2, int dims, float inv,
-               float halfcell, void *workspace, float scale_h, const float *scale_d, bool fold, cudaStream_t st)
+// One grid: keys of the (shifted, for SHIFT) positions, stable radix sort, runs,
+// positions gathered into sorted order, gather deposit.
+template <int MAS, bool SHIFT>
+int sorted_pass(const float *pos, const float *w, long long n, float *out, int dims, float inv, float halfcell,
+                const SortedWs &ws, float scale_h, const float *scale_d, bool fold, cudaStream_t st)
 {
-    SortedWs ws = sorted_layout(workspace, n, dims);
     const long long cells = (long long)dims * dims * dims;
     stage_mark(PYL_STAGE_SORT, true, st);
-    sd_key_kernel<MAS><<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, n, inv, dims, ws.k0, ws.v0);
+    sd_key_kernel<MAS, SHIFT><<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, n, inv, halfcell, dims, ws.k0, ws.v0);
     PYL_LAUNCH_CHECK();
     int bits = 1;
     while (bits < 32 && (1ull << bits) < (unsigned long long)cells) bits++;
@@ -469,33 +463,27 @@ int sorted_run(const float *pos, const float *w, long long n, float *grid, float
     PYL_LAUNCH_CHECK();
     sd_runs_kernel<<<blocks_for(n, 256, 16), 256, 0, st>>>(kin, n, ws.runs);
     PYL_LAUNCH_CHECK();
-    sd_gather_kernel<<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, w, vin, n, ws.spos);
+    sd_gather_kernel<SHIFT><<<blocks_for(n, 256, 16), 256, 0, st>>>(pos, w, vin, n, halfcell, ws.spos);
     PYL_LAUNCH_CHECK();
     stage_mark(PYL_STAGE_SORT, false, st);
     stage_mark(PYL_STAGE_DEPOSIT, true, st);
     const dim3 blk(32, 8), grd((unsigned)((dims + 31) / 32), (unsigned)((dims + 7) / 8), (unsigned)dims);
     const int f = fold ? 1 : 0;
-    if (w) {
-        sd_deposit_kernel<MAS, 0, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid,
-                                                            scale_h, scale_d, f);
-        PYL_LAUNCH_CHECK();
-        if (grid2) {
-            sd_deposit_kernel<MAS, 1, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid2,
-                                                                scale_h, scale_d, f);
-            PYL_LAUNCH_CHECK();
-        }
-    } else {
-        sd_deposit_kernel<MAS, 0, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid,
-                                                             scale_h, scale_d, f);
-        PYL_LAUNCH_CHECK();
-        if (grid2) {
-            sd_deposit_kernel<MAS, 1, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, halfcell, grid2,
-                                                                 scale_h, scale_d, f);
-            PYL_LAUNCH_CHECK();
-        }
-    }
+    if (w) sd_deposit_kernel<MAS, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f);
+    else sd_deposit_kernel<MAS, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f);
+    PYL_LAUNCH_CHECK();
     stage_mark(PYL_STAGE_DEPOSIT, false, st);
     return PYL_OK;
+}
+
+template <int MAS>
+int sorted_run(const float *pos, const float *w, long long n, float *grid, float *grid2, int dims, float inv,
+               float halfcell, void *workspace, float scale_h, const float *scale_d, bool fold, cudaStream_t st)
+{
+    const SortedWs ws = sorted_layout(workspace, n, dims);
+    int rc = sorted_pass<MAS, false>(pos, w, n, grid, dims, inv, halfcell, ws, scale_h, scale_d, fold, st);
+    if (rc || !grid2) return rc;
+    return sorted_pass<MAS, true>(pos, w, n, grid2, dims, inv, halfcell, ws, scale_h, scale_d, fold, st);
 }
 
 }  // namespace
