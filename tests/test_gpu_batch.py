@@ -100,3 +100,40 @@ def test_pk_bin_batch_equals_one_field_calls(mods, axis, inter):
     a, b = many.cpu().numpy(), one.cpu().numpy()
     for i in range(n):
         np.testing.assert_allclose(a[i], b[i], rtol=1e-5, atol=1e-6 * np.abs(b[i]).max(), err_msg='item %d' % i)
+
+
+@pytest.mark.parametrize('axis', [0, 2])
+def test_pk_bin_batch_coarsened_partition(mods, axis):
+    """With many items the batched launch gives each CTA more rows than a one-field call
+    (200 interlaced 128^3 fields: 512 representatives a CTA along axis 2, one row chunk
+    per plane along axis 0); the sums still agree with pyl_pk_bin item by item to
+    float32 rounding."""
+    import ctypes
+    from pylians_gb300 import _lib
+    from pylians_gb300._device import ptr
+    from pylians_gb300.batch import PK_ITEM_DT
+    L = _lib.load()
+    dims, n = 128, 200
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(31 + axis)
+    shape = (n, dims, dims, dims // 2 + 1)
+    dk = torch.complex(torch.randn(shape, generator=gen, device='cuda'), torch.randn(shape, generator=gen, device='cuda'))
+    dk2 = torch.complex(torch.randn(shape, generator=gen, device='cuda'), torch.randn(shape, generator=gen, device='cuda'))
+    slen = L.pyl_pk_sums_len(dims, 1)
+    many = torch.zeros((n, slen), dtype=torch.float64, device='cuda')
+    rec = np.zeros(n, dtype=PK_ITEM_DT)
+    for i in range(n):
+        rec[i] = (dk[i].data_ptr(), dk2[i].data_ptr(), many[i].data_ptr(), 1 + i % 4, 0)
+    table = torch.from_numpy(rec.view(np.uint8)).cuda()
+    nb = L.pyl_pk_bin_batch_workspace_size(dims, n, axis, 1)
+    wsb = torch.empty(nb, dtype=torch.uint8, device='cuda')
+    _lib.call('pyl_pk_bin_batch', ptr(table), n, dims, axis, 1, ptr(wsb), nb, None)
+    one = torch.zeros(slen, dtype=torch.float64, device='cuda')
+    ws = torch.empty(max(L.pyl_pk_workspace_size(dims, 1, axis), 1), dtype=torch.uint8, device='cuda')
+    a = many.cpu().numpy()
+    for i in range(0, n, 37):
+        mp = (ctypes.c_int * 1)(1 + i % 4)
+        _lib.call('pyl_pk_bin', ptr(dk[i]), ptr(dk2[i]), 1, dk[0].numel(), dims, axis, mp, ptr(one), ptr(ws),
+                  ws.numel(), None)
+        b = one.cpu().numpy()
+        np.testing.assert_allclose(a[i], b, rtol=1e-5, atol=1e-6 * np.abs(b).max(), err_msg='item %d' % i)
