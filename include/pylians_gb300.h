@@ -118,8 +118,8 @@ int pyl_ma_f64(const float *pos, const float *weights, int64_t n_particles, int 
  * process exits.  Limits: n_particles <= 524288 and dims <= 512; larger
  * requests return PYL_ERR_INVALID.  The first call on a device looks up the
  * array's device address, and the first call with each combination of MAS,
- * weights and interlacing raises the shared-memory limits of its kernels; make
- * those first calls before any stream capture.  All calls share the one array
+ * weights and interlacing raises the shared-memory limits of its kernels
+ * (cudaFuncSetAttribute).  All calls share the one array
  * and each keeps the previous call's contents (the call clears what must start
  * at zero), so calls that overlap on the GPU (different streams, or different
  * host threads) race and must be serialised by the caller.  Calls no
