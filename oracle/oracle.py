@@ -1,8 +1,8 @@
 """Oracle for Pylians' density-field and clustering path: MA, Pk, XPk, Bk on the CPU.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline / reference legs of ``bench.py`` use this module, as the checker
-and as the timed CPU baseline.  The product (``pylians_gb300``) never imports it.
+CPU-baseline / reference legs of ``bench.py`` use this module, as the reference
+results the GPU path is compared with and as the timed CPU baseline.  The product (``pylians_gb300``) never imports it.
 
 The hot loops are the plain-C restatement in ``pyl_oracle.c`` (mass assignment,
 P(k) mode loop); this file restates the rest in numpy, each part citing the
@@ -402,8 +402,8 @@ if __name__ == '__main__':
 
 # ----------------------------------------------------- MLP (learned correction)
 # float64 restatement of the 4 -> 64 -> 64 -> 64 -> 1 tanh network of the
-# learned aliasing correction (no counterpart in the reference): the checker of
-# the GPU forward/backward kernels' gradients.
+# learned aliasing correction (no counterpart in the reference): the values the
+# GPU forward/backward kernels' outputs and gradients are compared with.
 MLP_SHAPES = [('W1', (64, 4)), ('b1', (64,)), ('W2', (64, 64)), ('b2', (64,)),
               ('W3', (64, 64)), ('b3', (64,)), ('W4', (1, 64)), ('b4', (1,))]
 
