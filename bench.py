@@ -410,6 +410,20 @@ def kernels_per_step(dims):
     return 3 + placement + 1 + (1 if owned else 2) + 2
 
 
+def chain_bytes(n, dims, grids):
+    """Algorithmic HBM bytes of one particles -> P(k) chain: positions read once
+    (12 B a particle), each grid written by the deposit (4 B a cell), transformed
+    (4 B a cell read, 8 B a mode written) and binned (8 B a mode read)."""
+    g, h = float(dims) ** 3, float(dims) * dims * (dims // 2 + 1)
+    return 12.0 * n + grids * (4.0 * g + 4.0 * g + 8.0 * h + 8.0 * h)
+
+
+def hbm_peak():
+    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
+        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
+    return peaks.get('hbm_gbs', 6800.0), ('measured' if 'hbm_gbs' in peaks else 'fallback')
+
+
 def bench_zeldovich(reps=3):
     """512^3 lattice particles displaced by the Zel'dovich field of a 256^3 Gaussian
     field (P ~ k^-1.5 exp(-(k/0.5)^2), sigma 0.5, 1000 Mpc/h, seed 1) in redshift space
@@ -424,7 +438,10 @@ def bench_zeldovich(reps=3):
     import pylians_gb300.Pk_library as PKL
     pos = synthetic.zeldovich(N_field=256, N_lattice=512, BoxSize=BOX, sigma=0.5, f=0.5, rsd_axis=2, seed=1)
     n = pos.shape[0]
-    out = dict(workload="zeldovich 512^3 particles, 512^3 grid, RSD axis 2", particles=n)
+    hbm, src = hbm_peak()
+    out = dict(workload="zeldovich 512^3 particles, 512^3 grid, RSD axis 2", particles=n,
+               roofline=dict(peak=hbm, peak_source=src, unit='GB/s',
+                             bytes='12 N_p + G (8 N_g + 16 N_h), G grids (chain_bytes)'))
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     for mas in ('TSC', 'PCS'):
@@ -438,7 +455,10 @@ def bench_zeldovich(reps=3):
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
-            out['%s%s' % (mas, '_interlaced' if inter else '')] = dict(ms=ms, particles_per_s=n / (ms / 1e3))
+            alg = chain_bytes(n, 512, 2 if inter else 1)
+            out['%s%s' % (mas, '_interlaced' if inter else '')] = dict(
+                ms=ms, particles_per_s=n / (ms / 1e3), alg_bytes=alg, gbs=alg / (ms / 1e3) / 1e9,
+                frac=alg / (ms / 1e3) / 1e9 / hbm)
             del pp
             torch.cuda.empty_cache()
     # the deterministic sorted strategy on the same chain (TSC, interlaced)
@@ -451,7 +471,9 @@ def bench_zeldovich(reps=3):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    out['TSC_interlaced_sorted'] = dict(ms=ms, particles_per_s=n / (ms / 1e3))
+    alg = chain_bytes(n, 512, 2)
+    out['TSC_interlaced_sorted'] = dict(ms=ms, particles_per_s=n / (ms / 1e3), alg_bytes=alg,
+                                        gbs=alg / (ms / 1e3) / 1e9, frac=alg / (ms / 1e3) / 1e9 / hbm)
     del pp
     torch.cuda.empty_cache()
     a = torch.empty((512, 512, 512), device='cuda')
@@ -606,8 +628,13 @@ def bench_batch(count, steps=3):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     npart = sum(s['n'] for s in specs)
+    alg = sum(chain_bytes(s['n'], s['dims'], 2 if s['interlaced'] else 1) for s in specs)
+    hbm, src = hbm_peak()
     out = dict(metric='realizations/s', value=count / (ms / 1e3), particles_per_s=npart / (ms / 1e3),
-               ms_per_batch=ms, realizations=count, particles=npart, ctas_per_sm=B.ctas_per_sm)
+               ms_per_batch=ms, realizations=count, particles=npart, ctas_per_sm=B.ctas_per_sm,
+               roofline=dict(alg_bytes=alg, gbs=alg / (ms / 1e3) / 1e9, peak=hbm, peak_source=src,
+                             frac=alg / (ms / 1e3) / 1e9 / hbm, unit='GB/s',
+                             bytes='sum over realizations of 12 N_p + G (8 N_g + 16 N_h) (chain_bytes)'))
     del B, pos
     torch.cuda.empty_cache()
     return out
