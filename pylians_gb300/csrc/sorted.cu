@@ -27,6 +27,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "deposit.cuh"
 #include "sorted.cuh"
 
 namespace pyl {
@@ -343,48 +344,183 @@ __global__ void __launch_bounds__(256) sd_gather_kernel(const float *__restrict_
 }
 
 // ---- 5. gather deposit ----------------------------------------------------------
-// Thread (x, y, z): threadIdx.x + 32*blockIdx.x = z, threadIdx.y + 8*blockIdx.y = y,
-// blockIdx.z = x.  The cell sums, over base cells c - (l, m, q) with offsets
-// 0..S-1 per axis in that order and each run's particles in index order, the
-// weight of its corner.  The half-cell-shifted grid runs the same gather on its
-// own sort of the shifted positions (sorted_pass<MAS, true>).
+// Cell (x, y, z) sums, over base cells c - (l, m, q) with offsets 0..S-1 per axis
+// in that order and each run's particles in index order, the weight of its corner
+// ((c0 c1) c2, times the weight), in float32 adds: a fixed order, so the grid is
+// the same bits on every run.  The half-cell-shifted grid runs the same gather on
+// its own sort of the shifted positions (sorted_pass<MAS, true>).
 // scale/base: out = (fold ? out : 0) + sum in fixed order, then
 //   (fold ? sum : out_old + sum * scale).
+
+// One (l, m) of one cell straight from the runs and the sorted positions.
+template <int MAS, bool WEIGHTED>
+__device__ __forceinline__ float sd_direct_lm(const float4 *__restrict__ spos, const uint2 *__restrict__ runs,
+                                              long long row, int z, int dims, float inv, int l, int m, float acc)
+{
+    constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS;
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+        const uint2 rr = runs[row + wrap_index(z - q, dims)];
+        if (rr.x == EMPTY) continue;
+        for (unsigned j = rr.x; j < rr.y; j++) {
+            const float4 p = spos[j];
+            int f;
+            const float c0 = sd_weight<MAS>(p.x, inv, l, &f);
+            const float c1 = sd_weight<MAS>(p.y, inv, m, &f);
+            const float c2 = sd_weight<MAS>(p.z, inv, q, &f);
+            float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c0, c1), c2);
+            if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
+            acc = __fadd_rn(acc, v);
+        }
+    }
+    return acc;
+}
+
+constexpr int SDT_CAP = 1024;      // particles a CTA stages per x offset l
+
+// Of one staged particle: the products (x weight at offset l) (y weight at offset
+// m) for m = 0..S-1, the z weights at offsets 0..S-1 (and the weight).
+template <int MAS, bool WEIGHTED>
+struct SdStage {
+    static constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS;
+    static constexpr int NV = 2 * S + (WEIGHTED ? 1 : 0);
+    static constexpr int RY = 8 + S - 1, W = 32 + S - 1;   // base rows along y, base cells along z
+    static constexpr int NC = RY * W;                       // window cells of one l
+};
+
+// A CTA takes the 32 x 8 cells (z, y) of one x plane; block (32, 8), grid
+// (ceil(dims / 32), ceil(dims / 8), dims).  For each x offset l the CTA reads the
+// runs of the (8 + S - 1) x (32 + S - 1) base cells its cells reach in plane
+// x - l, places their particles in shared memory by a block scan, and computes
+// each staged particle's S (x, y) weight products and S z weights once (all S
+// weights of an axis from one axis_weights, the arithmetic of sd_weight),
+// instead of once for each of the S^2 cells of the plane that it reaches.
+// Every cell then sums its base cells' staged particles in the order above, with
+// the same products and adds as sd_direct_lm, which takes over for an l whose
+// window holds more than SDT_CAP particles.
 template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restrict__ spos,
                                                          const uint2 *__restrict__ runs, int dims, float inv,
                                                          float *__restrict__ out, float scale_h,
                                                          const float *__restrict__ scale_d, int fold)
 {
-    constexpr int S = MAS == PYL_MAS_NGP ? 1 : MAS;
-    const int z = blockIdx.x * 32 + threadIdx.x;
-    const int y = blockIdx.y * 8 + threadIdx.y;
-    const int x = blockIdx.z;
-    if (z >= dims || y >= dims) return;
+    using ST = SdStage<MAS, WEIGHTED>;
+    constexpr int S = ST::S, NV = ST::NV, W = ST::W, NC = ST::NC;
+    constexpr int CPT = (NC + 255) / 256;                   // window cells a thread reads
+    __shared__ unsigned s_off[NC + 1];                      // staged start of each window cell
+    __shared__ unsigned s_rx[NC];                           // its first particle in sorted order
+    __shared__ float s_e[SDT_CAP * NV];
+    __shared__ unsigned s_wsum[8];
+    const int tid = threadIdx.y * 32 + threadIdx.x, lane = threadIdx.x, warp = threadIdx.y;
+    const int z0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+    const int z = z0 + threadIdx.x, y = y0 + threadIdx.y, x = blockIdx.z;
+    const bool live = z < dims && y < dims;
     const long long d = dims;
     const long long cell = ((long long)x * d + y) * d + z;
-    float acc = fold ? out[cell] : 0.0f;
+    float acc = (fold && live) ? out[cell] : 0.0f;
 #pragma unroll 1
-    for (int l = 0; l < S; l++)
-#pragma unroll 1
-        for (int m = 0; m < S; m++) {
-            const long long row = ((long long)wrap_index(x - l, dims) * d + wrap_index(y - m, dims)) * d;
+    for (int l = 0; l < S; l++) {
+        const long long plane = (long long)wrap_index(x - l, dims) * d;
+        // 1. runs of this thread's window cells tid * CPT + k (row r = c / W, cell
+        //    i = c % W: base cell (y0 - (S - 1) + r, z0 - (S - 1) + i)); cells past
+        //    the grid's end serve no live cell and stay empty
+        unsigned cnt[CPT], sum = 0;
 #pragma unroll
-            for (int q = 0; q < S; q++) {
-                const uint2 rr = runs[row + wrap_index(z - q, dims)];
-                if (rr.x == EMPTY) continue;
-                for (unsigned j = rr.x; j < rr.y; j++) {
-                    const float4 p = spos[j];
-                    int f;
-                    const float c0 = sd_weight<MAS>(p.x, inv, l, &f);
-                    const float c1 = sd_weight<MAS>(p.y, inv, m, &f);
-                    const float c2 = sd_weight<MAS>(p.z, inv, q, &f);
-                    float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(__fmul_rn(c0, c1), c2);
-                    if (WEIGHTED) v = MAS == PYL_MAS_NGP ? p.w : __fmul_rn(v, p.w);
-                    acc = __fadd_rn(acc, v);
+        for (int k = 0; k < CPT; k++) {
+            const int c = tid * CPT + k;
+            cnt[k] = 0;
+            if (c < NC) {
+                const int yb = y0 - (S - 1) + c / W, zb = z0 - (S - 1) + c % W;
+                unsigned rx = 0;
+                if (yb < dims && zb < dims) {
+                    const uint2 rr = runs[(plane + wrap_index(yb, dims)) * d + wrap_index(zb, dims)];
+                    if (rr.x != EMPTY) { cnt[k] = rr.y - rr.x; rx = rr.x; }
+                }
+                s_rx[c] = rx;
+            }
+            sum += cnt[k];
+        }
+        // 2. block exclusive scan of the thread sums
+        unsigned inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) s_wsum[warp] = inc;
+        __syncthreads();
+        unsigned before = 0, total = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < 8; w2++) {
+            const unsigned v = s_wsum[w2];
+            before += w2 < warp ? v : 0u;
+            total += v;
+        }
+        unsigned run = before + inc - sum;
+#pragma unroll
+        for (int k = 0; k < CPT; k++) {
+            const int c = tid * CPT + k;
+            if (c < NC) s_off[c] = run;
+            run += cnt[k];
+        }
+        if (tid == 0) s_off[NC] = total;
+        __syncthreads();                                    // s_wsum reads done, s_off / s_rx written
+        if (total > SDT_CAP) {                              // the same for the whole CTA
+            if (live)
+#pragma unroll 1
+                for (int m = 0; m < S; m++)
+                    acc = sd_direct_lm<MAS, WEIGHTED>(spos, runs, (plane + wrap_index(y - m, dims)) * d, z, dims,
+                                                      inv, l, m, acc);
+            __syncthreads();
+            continue;
+        }
+        // 3. stage: particle t of the window is particle t - s_off[c] of window cell c
+        for (unsigned t = tid; t < total; t += 256) {
+            int lo = 0, hi = NC;                            // s_off[lo] <= t < s_off[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_off[mid] <= t) lo = mid; else hi = mid;
+            }
+            const float4 p = spos[s_rx[lo] + (t - s_off[lo])];
+            float *e = s_e + t * NV;
+            if (MAS == PYL_MAS_NGP) {
+                e[0] = e[1] = 1.0f;
+            } else {
+                float cx[S], cy[S], cz[S];
+                axis_weights<MAS>(p.x, inv, cx);
+                axis_weights<MAS>(p.y, inv, cy);
+                axis_weights<MAS>(p.z, inv, cz);
+                float c0 = cx[0];
+#pragma unroll
+                for (int j = 1; j < S; j++) c0 = l == j ? cx[j] : c0;
+#pragma unroll
+                for (int m = 0; m < S; m++) e[m] = __fmul_rn(c0, cy[m]);
+#pragma unroll
+                for (int q = 0; q < S; q++) e[S + q] = cz[q];
+            }
+            if (WEIGHTED) e[2 * S] = p.w;
+        }
+        __syncthreads();
+        // 4. each cell: base rows y - m, base cells z - q, particles in index order
+        if (live) {
+#pragma unroll 1
+            for (int m = 0; m < S; m++) {
+#pragma unroll
+                for (int q = 0; q < S; q++) {
+                    const int c = (warp + (S - 1) - m) * W + lane + (S - 1) - q;
+                    const unsigned a = s_off[c], b = s_off[c + 1];
+                    for (unsigned t = a; t < b; t++) {
+                        const float *e = s_e + t * NV;
+                        float v = MAS == PYL_MAS_NGP ? 1.0f : __fmul_rn(e[m], e[S + q]);
+                        if (WEIGHTED) v = MAS == PYL_MAS_NGP ? e[2 * S] : __fmul_rn(v, e[2 * S]);
+                        acc = __fadd_rn(acc, v);
+                    }
                 }
             }
         }
+        __syncthreads();                                    // before the next l restages
+    }
+    if (!live) return;
     if (fold) {
         out[cell] = acc;
     } else if (acc != 0.0f) {
