@@ -409,6 +409,15 @@ int pyl_ma_set_thresholds(int owned_min_dims, double tot_min_per_cell);
  * that want smaller workspaces.  Change it only between calls. */
 int pyl_ma_set_pass_limit(int64_t max_particles);
 
+/* Particles a CTA of the sorted strategy's gather stages in shared memory per x
+ * offset of its cells' support (no counterpart in the reference), process-wide,
+ * for tests: default and maximum 1024; a window holding more is summed straight
+ * from the sorted runs, in the same order and with the same products, so the
+ * grid does not depend on it.  0 sums every window straight from the runs; a
+ * negative value restores the default; above 1024 returns PYL_ERR_INVALID.
+ * Change it only between calls. */
+int pyl_sorted_set_stage_limit(int max_particles);
+
 /* Device-side error word (no counterpart in the reference): nonzero when a kernel's
  * bounded wait for its own bulk copies ran out and the kernel left early (its
  * output is then incomplete).  Synchronous; reset = 1 clears it. */

@@ -72,6 +72,7 @@ SIGNATURES = {
     'pyl_device_error': (_I, [_I, _P]),
     'pyl_ma_set_thresholds': (_I, [_I, _D]),
     'pyl_ma_set_pass_limit': (_I, [_I64]),
+    'pyl_sorted_set_stage_limit': (_I, [_I]),
     'pyl_wait_probe': (_I, [ctypes.c_uint, ctypes.c_longlong, _P, _P]),
     'pyl_cic_interp': (_I, [_P, _I, _F, _P, _I64, _P, _P]),
     'pyl_pos_redshift_space': (_I, [_P, _P, _I64, _F, _F, _F, _I, _P]),

@@ -24,6 +24,7 @@
 // Limits: dims^3 <= 2^32 (dims <= 1625) and fewer than 2^32 particles.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 
 #include "common.cuh"
@@ -376,7 +377,8 @@ __device__ __forceinline__ float sd_direct_lm(const float4 *__restrict__ spos, c
     return acc;
 }
 
-constexpr int SDT_CAP = 1024;      // particles a CTA stages per x offset l
+constexpr int SDT_CAP = 1024;      // particles a CTA stages per x offset l (shared-memory capacity)
+std::atomic<int> g_sd_stage_cap{SDT_CAP};   // pyl_sorted_set_stage_limit
 
 // Of one staged particle: the products (x weight at offset l) (y weight at offset
 // m) for m = 0..S-1, the z weights at offsets 0..S-1 (and the weight).
@@ -397,12 +399,13 @@ struct SdStage {
 // instead of once for each of the S^2 cells of the plane that it reaches.
 // Every cell then sums its base cells' staged particles in the order above, with
 // the same products and adds as sd_direct_lm, which takes over for an l whose
-// window holds more than SDT_CAP particles.
+// window holds more than cap (at most SDT_CAP) particles.
 template <int MAS, bool WEIGHTED>
 __global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restrict__ spos,
                                                          const uint2 *__restrict__ runs, int dims, float inv,
                                                          float *__restrict__ out, float scale_h,
-                                                         const float *__restrict__ scale_d, int fold)
+                                                         const float *__restrict__ scale_d, int fold,
+                                                         unsigned cap)
 {
     using ST = SdStage<MAS, WEIGHTED>;
     constexpr int S = ST::S, NV = ST::NV, W = ST::W, NC = ST::NC;
@@ -465,7 +468,7 @@ __global__ void __launch_bounds__(256) sd_deposit_kernel(const float4 *__restric
         }
         if (tid == 0) s_off[NC] = total;
         __syncthreads();                                    // s_wsum reads done, s_off / s_rx written
-        if (total > SDT_CAP) {                              // the same for the whole CTA
+        if (total > cap) {                                  // the same for the whole CTA (cap <= SDT_CAP)
             if (live)
 #pragma unroll 1
                 for (int m = 0; m < S; m++)
@@ -605,8 +608,9 @@ int sorted_pass(const float *pos, const float *w, long long n, float *out, int d
     stage_mark(PYL_STAGE_DEPOSIT, true, st);
     const dim3 blk(32, 8), grd((unsigned)((dims + 31) / 32), (unsigned)((dims + 7) / 8), (unsigned)dims);
     const int f = fold ? 1 : 0;
-    if (w) sd_deposit_kernel<MAS, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f);
-    else sd_deposit_kernel<MAS, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f);
+    const unsigned cap = (unsigned)g_sd_stage_cap.load();
+    if (w) sd_deposit_kernel<MAS, true><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f, cap);
+    else sd_deposit_kernel<MAS, false><<<grd, blk, 0, st>>>(ws.spos, ws.runs, dims, inv, out, scale_h, scale_d, f, cap);
     PYL_LAUNCH_CHECK();
     stage_mark(PYL_STAGE_DEPOSIT, false, st);
     return PYL_OK;
@@ -658,3 +662,10 @@ int launch_sorted(int mas, const float *pos, const float *w, long long n, float 
 }
 
 }  // namespace pyl
+
+extern "C" int pyl_sorted_set_stage_limit(int max_particles)
+{
+    PYL_CHECK_ARG(max_particles <= pyl::SDT_CAP, "max_particles above the stage capacity (1024)");
+    pyl::g_sd_stage_cap.store(max_particles < 0 ? pyl::SDT_CAP : max_particles);
+    return PYL_OK;
+}

@@ -212,6 +212,10 @@ def test_wait_probe_and_thresholds_reject_bad_arguments(lib):
     assert lib.pyl_ma_set_thresholds(0, 1.0) == 1
     assert lib.pyl_ma_set_thresholds(-1, float('nan')) == 1
     assert lib.pyl_ma_set_thresholds(-1, -1.0) == 0
+    assert lib.pyl_sorted_set_stage_limit(1025) == 1
+    assert 'capacity' in lib.pyl_last_error().decode()
+    assert lib.pyl_sorted_set_stage_limit(0) == 0
+    assert lib.pyl_sorted_set_stage_limit(-1) == 0
 
 
 def test_pass_limit_sizes_the_workspace(lib):
