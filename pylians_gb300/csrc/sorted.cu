@@ -231,71 +231,74 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(unsigned *__re
     }
 }
 
-// Stable scatter of one tile by one digit.  Element e = r*RS_THREADS + t of the
-// tile (round r, thread t) ranks after every element of the tile with the same
-// digit and a smaller e.  Per round, each warp's count of a digit is published
-// in wc[warp][digit] tagged with the round number (no clearing between rounds).
+// Stable scatter of one tile by one digit.  Warp w holds the tile's elements
+// w*512 .. w*512+511 (round r, lane l: element w*512 + r*32 + l), so the order
+// (warp, round, lane) is the tile's order.  Each warp ranks its elements with
+// its own digit counters (a match_any per round, no block barrier), one block
+// scan turns the tile's digit counts into each digit's first staging slot and
+// each warp's first slot within it, and the tile is staged in digit order in
+// shared memory before the coalesced write.
 __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(
     const unsigned *__restrict__ kin, const unsigned *__restrict__ vin, long long n, int shift, unsigned tiles,
     const unsigned *__restrict__ goff, unsigned *__restrict__ kout, unsigned *__restrict__ vout)
 {
+    constexpr int PER_WARP = RS_ITEMS * 32;
     __shared__ unsigned sk[RS_TILE], sv[RS_TILE];
-    __shared__ unsigned wc[RS_WARPS][256];
-    __shared__ unsigned run[256];      // elements of each digit ranked so far
-    __shared__ unsigned start[256];    // first staging slot of each digit
-    __shared__ unsigned gbase[256];    // global position of the digit's first element
-    __shared__ unsigned h[256];
+    __shared__ unsigned wc[RS_WARPS][256];   // a warp's count of each digit, then its first slot
+    __shared__ unsigned start[256];          // first staging slot of each digit
+    __shared__ unsigned gbase[256];          // global position of the digit's first element
     __shared__ unsigned ws[32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const long long base = (long long)blockIdx.x * RS_TILE;
-    for (int i = t; i < RS_WARPS * 256; i += RS_THREADS) (&wc[0][0])[i] = 0xffffffffu;
-    run[t] = 0u;
-    h[t] = 0u;
-    unsigned dg[RS_ITEMS], key[RS_ITEMS], val[RS_ITEMS];
+    const long long tile0 = (long long)blockIdx.x * RS_TILE;
+    const long long base = tile0 + (long long)warp * PER_WARP;
+    for (int i = lane; i < 256; i += 32) wc[warp][i] = 0u;
+    unsigned dg[RS_ITEMS], key[RS_ITEMS], val[RS_ITEMS], rk[RS_ITEMS];
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; r++) {
-        const long long i = base + r * RS_THREADS + t;
+        const long long i = base + r * 32 + lane;
         key[r] = i < n ? kin[i] : 0u;
         val[r] = i < n ? vin[i] : 0u;
         dg[r] = i < n ? ((key[r] >> shift) & 255u) : 256u;
     }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RS_ITEMS; r++)
-        if (dg[r] < 256u) atomicAdd(&h[dg[r]], 1u);
-    __syncthreads();
-    start[t] = block_excl_scan(h[t], ws, nullptr);
-    gbase[t] = goff[(long long)t * tiles + blockIdx.x];
-    __syncthreads();
+    __syncwarp();
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; r++) {
         const unsigned d = dg[r];
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const unsigned lrank = __popc(peers & lt);
-        if (lrank == 0u && d < 256u) wc[warp][d] = ((unsigned)r << 8) | (unsigned)__popc(peers);
-        __syncthreads();
-        if (d < 256u) {
-            unsigned before = run[d];
-            for (int w = 0; w < warp; w++) {
-                const unsigned v = wc[w][d];
-                before += (v >> 8) == (unsigned)r ? (v & 255u) : 0u;
-            }
-            const unsigned slot = start[d] + before + lrank;
+        const unsigned before = d < 256u ? wc[warp][d] : 0u;
+        __syncwarp();
+        if (lrank == 0u && d < 256u) wc[warp][d] = before + (unsigned)__popc(peers);
+        __syncwarp();
+        rk[r] = before + lrank;
+    }
+    __syncthreads();
+    // thread t = digit t: the tile's count, its first slot, each warp's first slot
+    unsigned c = 0u;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) c += wc[w][t];
+    const unsigned s0 = block_excl_scan(c, ws, nullptr);
+    start[t] = s0;
+    gbase[t] = goff[(long long)t * tiles + blockIdx.x];
+    unsigned run = s0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+        const unsigned v = wc[w][t];
+        wc[w][t] = run;
+        run += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; r++) {
+        if (dg[r] < 256u) {
+            const unsigned slot = wc[warp][dg[r]] + rk[r];
             sk[slot] = key[r];
             sv[slot] = val[r];
         }
-        __syncthreads();
-        unsigned add = 0u;
-#pragma unroll
-        for (int w = 0; w < RS_WARPS; w++) {
-            const unsigned v = wc[w][t];
-            add += (v >> 8) == (unsigned)r ? (v & 255u) : 0u;
-        }
-        run[t] += add;
-        __syncthreads();
     }
-    const unsigned cnt = (unsigned)min((long long)RS_TILE, n - base);
+    __syncthreads();
+    const unsigned cnt = (unsigned)min((long long)RS_TILE, n - tile0);
     for (unsigned p = t; p < cnt; p += RS_THREADS) {
         const unsigned k = sk[p];
         const unsigned d = (k >> shift) & 255u;
