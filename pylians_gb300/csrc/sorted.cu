@@ -14,7 +14,9 @@
 //   4. the particles' positions (and weights) gathered into sorted order.
 //   5. gather deposit: one thread per output cell walks the S^3 neighbouring
 //      base cells in a fixed order and, within each run, the particles in index
-//      order, recomputing the weight of its corner.  The interlaced grid runs
+//      order, adding the weight of its corner; the CTA stages the particles of
+//      its base cells in shared memory with their weights computed once per x
+//      offset (sd_deposit_kernel).  The interlaced grid runs
 //      steps 1-5 again on the shifted positions (its own sort), so its cells
 //      also visit S^3 base cells (a gather over the plain grid's sort visited
 //      (S+1)^3 and checked each corner: 4x the work for TSC).
