@@ -408,6 +408,108 @@ __global__ void __launch_bounds__(1024) chunk_hist_tma_kernel(const float *pos, 
     if (coh && threadIdx.x == 0 && s_same) atomicAdd(coh, (unsigned long long)s_same);
 }
 
+// chunk_scatter_kernel with its positions streamed through shared memory as in
+// chunk_hist_tma_kernel (bulk copies of HT_BATCH particles, HT_NBUF in flight, no
+// block barrier per batch: lane 0 of each warp waits, the warp copies its
+// particles to registers and counts itself out, the last warp issues the next
+// copy into the buffer).  NT threads: 1024 with one chunk per SM, 512 with two
+// chunks per SM (two CTAs per SM, 64 registers a thread).  Lanes hold
+// consecutive particles, so equal bins still take one reservation per warp.
+template <int MAS, bool WEIGHTED, int NT>
+__global__ void __launch_bounds__(NT) chunk_scatter_tma_kernel(
+    const float *pos, const float *__restrict__ w, long long n, long long chunk, float inv, TileGeom g,
+    const unsigned *__restrict__ colpre, const unsigned *__restrict__ offsets, float4 *__restrict__ rec,
+    unsigned *err, Gate gate)
+{
+    if (gate_closed(gate)) return;
+    constexpr int HB = HT_BATCH, PER = HB / NT, NW = NT / 32;
+    static_assert(PER * NT == HB && (NW & (NW - 1)) == 0, "whole batches, a power-of-two warp count");
+    extern __shared__ __align__(16) unsigned char sraw[];
+    __shared__ __align__(8) unsigned long long bar[HT_NBUF];
+    __shared__ unsigned s_rel[HT_NBUF];     // warps done reading each buffer, counted up forever
+    __shared__ long long s_last[HT_NBUF];   // batch of the last copy into each buffer (-1: none)
+    __shared__ int s_fail;
+    const int T = (int)g.ntiles;
+    const unsigned lane = threadIdx.x & 31u;
+    float *inb = (float *)sraw;                                  // [HT_NBUF][HB * 3]
+    unsigned *cur = (unsigned *)(sraw + HT_NBUF * HB * 12);
+    const unsigned *row = colpre + (long long)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += NT) cur[t] = offsets[t] + row[t];
+    const long long b = blockIdx.x * chunk, e = min(n, b + chunk);
+    const long long nbat = e > b ? (e - b + HB - 1) / HB : 0;
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        for (int k = 0; k < HT_NBUF; k++) {
+            mbar_init(&bar[k], 1);
+            s_rel[k] = 0u;
+            s_last[k] = -1;
+        }
+        mbar_fence_init();
+        for (long long j = 0; j < HT_NBUF && j < nbat; j++) {
+            const long long s0 = b + j * HB;
+            stage_copy(inb + (j % HT_NBUF) * HB * 3, pos + 3 * s0, staged_bytes(min((long long)HB, e - s0)),
+                       &bar[j % HT_NBUF]);
+            s_last[j % HT_NBUF] = j;
+        }
+    }
+    __syncthreads();
+    for (long long j = 0; j < nbat; j++) {
+        const long long s0 = b + j * HB;
+        const int c = (int)min((long long)HB, e - s0);
+        const int full = staged_full(c);
+        const int buf = (int)(j % HT_NBUF);
+        const float *in = inb + buf * HB * 3;
+        int got = 0;
+        if (lane == 0) got = mbar_wait_bounded(&bar[buf], (unsigned)((j / HT_NBUF) & 1), err);
+        got = __shfl_sync(0xffffffffu, got, 0);
+        __syncwarp();
+        const bool all_staged = full == HB;
+        float p[PER][3];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int i = threadIdx.x + u * NT;
+            const long long q = s0 + i;
+            if (all_staged || i < full) {
+                p[u][0] = in[3 * i]; p[u][1] = in[3 * i + 1]; p[u][2] = in[3 * i + 2];
+            } else if (i < c) {
+                p[u][0] = pos[3 * q]; p[u][1] = pos[3 * q + 1]; p[u][2] = pos[3 * q + 2];
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (!got) atomicOr(&s_fail, 1);
+            __threadfence_block();                          // this warp's reads before its count
+            const unsigned done = atomicAdd(&s_rel[buf], 1u);
+            if ((done & (NW - 1u)) == NW - 1u && j + HT_NBUF < nbat && !*(volatile int *)&s_fail) {
+                const long long s2 = b + (j + HT_NBUF) * HB;
+                fence_proxy_async_smem();
+                stage_copy(inb + buf * HB * 3, pos + 3 * s2, staged_bytes(min((long long)HB, e - s2)), &bar[buf]);
+                s_last[buf] = j + HT_NBUF;
+            }
+        }
+        if (!got) continue;
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int i = threadIdx.x + u * NT;
+            const unsigned act = __ballot_sync(0xffffffffu, i < c);
+            if (i < c) {
+                const unsigned key = tile_key<MAS>(p[u], inv, g);
+                const unsigned peers = __match_any_sync(act, key);
+                const unsigned leader = (unsigned)__ffs(peers) - 1u;
+                unsigned slot = 0u;
+                if (lane == leader) slot = atomicAdd(cur + key, (unsigned)__popc(peers));
+                slot = __shfl_sync(peers, slot, leader) + (unsigned)__popc(peers & ((1u << lane) - 1u));
+                const float4 r = make_float4(p[u][0], p[u][1], p[u][2], WEIGHTED ? __ldg(w + s0 + i) : 1.0f);
+                if (slot < (unsigned long long)n) rec[slot] = r;
+            }
+        }
+    }
+    __syncthreads();
+    if (s_fail && threadIdx.x == 0)
+        for (int k = 0; k < HT_NBUF; k++)
+            if (s_last[k] >= 0) mbar_drain_bounded(&bar[k], (unsigned)((s_last[k] / HT_NBUF) & 1));
+}
+
 // Two CTAs per SM (grids binned by twice as many chunks as SMs): thread 0 waits
 // and the CTA meets at two barriers per batch, with 30 registers a thread.  (The
 // barrier-free loop above needs 44 registers; held to 32 it spills, and on
@@ -1459,7 +1561,18 @@ int launch_tiled(const float *pos, const float *w, long long n, float *grid, flo
             // coherent when at least 3/4 of the particles share their predecessor's bin
             const unsigned long long thresh = (unsigned long long)n - (unsigned long long)n / 4;
             const Gate coherent{same, thresh, 1}, incoherent{same, thresh, 0};
-            if (gated) {
+            if (gated && hsm <= 227 * 1024) {      // positions staged by bulk copies
+#define PYL_SCATTER_TMA(WW, NT)                                                                               \
+    do {                                                                                                     \
+        PYL_CUDA(ensure_smem(chunk_scatter_tma_kernel<MAS, WW, NT>, hsm));                                   \
+        chunk_scatter_tma_kernel<MAS, WW, NT><<<C, NT, hsm, st>>>(pos, w, n, chunk, inv, g, ws.hist, ws.offsets, \
+                                                                 ws.rec, err, coherent);                     \
+    } while (0)
+                if (w) { if (two) PYL_SCATTER_TMA(true, 512); else PYL_SCATTER_TMA(true, 1024); }
+                else   { if (two) PYL_SCATTER_TMA(false, 512); else PYL_SCATTER_TMA(false, 1024); }
+#undef PYL_SCATTER_TMA
+                PYL_LAUNCH_CHECK();
+            } else if (gated) {
                 if (w) {
                     PYL_CUDA(ensure_smem(chunk_scatter_kernel<MAS, true>, sm));
                     chunk_scatter_kernel<MAS, true><<<C, 1024, sm, st>>>(pos, w, n, chunk, inv, g, ws.hist,
