@@ -1,26 +1,30 @@
 """Model check, on the CPU, of the barrier-free staging protocol of the deposit
-(owned-cell launches) and histogram kernels: 32 warps stream batches through two
-shared-memory buffers, each filled by one bulk copy that completes one phase of
+(owned-cell launches), histogram and one-pass placement kernels: 32 (or 16)
+warps stream batches through two shared-memory buffers, each filled by one bulk
+copy that completes one phase of
 the buffer's mbarrier.  Batch q (counted over all passes of a CTA) sits in
 buffer q % 2 and completes phase q // 2 there.  A warp waits for it with a
 parity wait (true once the barrier's current phase has the other parity), reads
 its records, and adds one to the buffer's release counter; the warp that brings
-the counter to a multiple of 32 issues the copy of batch q + 2 of the same pass
+the counter to a multiple of the warp count issues the copy of batch q + 2 of the same pass
 into that buffer.  Passes (bins, grids, float32 redos) follow one another after
 a block barrier; each starts with thread 0 issuing its first two copies.
 
 Random interleavings, with copies landing at random later times, check that no
 parity wait succeeds on any phase but its own, that no warp reads a buffer
-that is being refilled, that each copy is issued once and only after all 32
-warps have left the buffer, and that every run ends."""
+that is being refilled, that each copy is issued once and only after every
+warp has left the buffer, and that every run ends."""
 import numpy as np
 import pytest
 
 WARPS = 32
 
 
-def run(passes, seed, last=31):
+def run(passes, seed, last=None, warps=WARPS):
+    """warps: warps of the CTA (32, or 16 for the 512-thread placement kernels);
+    last: the release count, modulo warps, whose warp issues the refill."""
     rng = np.random.default_rng(seed)
+    last = warps - 1 if last is None else last
     phases = [0, 0]                 # completed phases per buffer
     content = [None, None]          # batch held by each buffer (None: copy in flight)
     in_flight = []                  # (buffer, batch) copies not yet landed
@@ -45,14 +49,14 @@ def run(passes, seed, last=31):
         for j in range(min(2, nb)):             # thread 0, then the pass-start barrier
             issue(q0 + j)
         left = [set() for _ in range(nb)]
-        pos = [0] * WARPS
-        waiting = [True] * WARPS
+        pos = [0] * warps
+        waiting = [True] * warps
         while any(p < nb for p in pos):
             steps += 1
-            assert steps < 400 * (sum(passes) + 1) * WARPS, 'no progress: deadlock'
+            assert steps < 400 * (sum(passes) + 1) * warps, 'no progress: deadlock'
             if in_flight and rng.random() < 0.3:
                 land()
-            w = int(rng.integers(WARPS))
+            w = int(rng.integers(warps))
             j = pos[w]
             if j >= nb:
                 continue
@@ -67,22 +71,23 @@ def run(passes, seed, last=31):
                 left[j].add(w)
                 done = rel[b]
                 rel[b] += 1
-                if (done & 31) == last and j + 2 < nb:
-                    assert len(left[j]) == WARPS, 'refilled before every warp left'
+                if (done & (warps - 1)) == last and j + 2 < nb:
+                    assert len(left[j]) == warps, 'refilled before every warp left'
                     issue(q + 2)
                 waiting[w] = True
                 pos[w] += 1
         assert not in_flight                    # every copy of the pass was waited for
-        assert rel[0] % WARPS == 0 and rel[1] % WARPS == 0
+        assert rel[0] % warps == 0 and rel[1] % warps == 0
         q0 += nb
     assert sorted(issued) == list(range(q0)) and set(issued.values()) <= {1}
     return steps
 
 
+@pytest.mark.parametrize('warps', [32, 16])
 @pytest.mark.parametrize('nb', [0, 1, 2, 3, 7, 16])
-def test_one_pass(nb):
+def test_one_pass(nb, warps):
     for seed in range(30):
-        run([nb], seed)
+        run([nb], seed, warps=warps)
 
 
 @pytest.mark.parametrize('passes', [[5, 2, 9], [1, 1, 1, 1], [3, 0, 4, 4], [16, 16]])
