@@ -420,7 +420,11 @@ int pyl_sorted_set_stage_limit(int max_particles);
 
 /* Device-side error word (no counterpart in the reference): nonzero when a kernel's
  * bounded wait for its own bulk copies ran out and the kernel left early (its
- * output is then incomplete).  Synchronous; reset = 1 clears it. */
+ * output is then incomplete).  While it is set, the tiled strategy's second
+ * placement level and deposit return at once (their input may be incomplete),
+ * so grids are left as they were.  Synchronous; reset = 1 clears it.  The Python
+ * package reads and clears it after every call that returns host results, and
+ * raises if it was set. */
 int pyl_device_error(int reset, unsigned *out);
 
 /* Exercises that bounded wait (no counterpart in the reference; for tests): one

@@ -103,14 +103,19 @@ def MA(pos, number, BoxSize, MAS='CIC', W=None, verbose=False, renormalize_2D=Tr
     dgrid = as_device_f32(number, 'number')
     dint = as_device_f32(interlaced, 'interlaced') if interlaced is not None else None
     ma_device(dpos, dgrid, BoxSize, MAS, dW, dint, renormalize_2D, strategy)
+    copied = False
     for host, dev in ((number, dgrid), (interlaced, dint)):
         if host is None or dev is None:
             continue
         if is_torch(host):
             if not host.is_cuda:
                 host.copy_(dev.cpu())
+                copied = True
         else:
             np.copyto(host, dev.cpu().numpy())
+            copied = True
+    if copied:                    # host results: the call has synchronised anyway
+        _lib.check_device('MA')
     if verbose:
         torch.cuda.synchronize()
         print('Time taken = %.3f seconds\n' % (time.time() - start))

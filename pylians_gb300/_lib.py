@@ -117,3 +117,14 @@ def call(name, *args):
     rc = getattr(load(), name)(*args)
     check(rc, name)
     return rc
+
+
+def check_device(what=''):
+    """Raise if a device-side bounded wait gave up since the last check (the device
+    error word, read and cleared; the read waits for the device).  The tiled
+    deposits launched while the word was set deposited nothing."""
+    out = ctypes.c_uint(0)
+    check(load().pyl_device_error(1, ctypes.byref(out)), 'pyl_device_error')
+    if out.value:
+        raise PylError('%s: a device-side wait gave up (error word %#x); the results of the calls '
+                       'since the last check are incomplete' % (what, out.value))

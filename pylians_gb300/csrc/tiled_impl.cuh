@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(LBT_THREADS) level_b_tma_kernel(
     __shared__ unsigned seg_start, seg_len;
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ int s_ok;
-    if (gate_closed(gate)) return;
+    if (gate_closed(gate) || *(volatile unsigned *)err) return;   // set: a wait upstream gave up
     extern __shared__ __align__(16) float4 braw[];
     float4 *inb = braw;                                     // [2][LBT_BATCH]
     float4 *stage = braw + 2 * LBT_BATCH;
@@ -1382,6 +1382,9 @@ __global__ void __launch_bounds__(1024) bin_deposit_fx_tma_kernel(
     float halfcell, float *__restrict__ grid, float *__restrict__ grid2, OutScale sc, unsigned n_rec,
     Owned ow, const float *inv_w, unsigned *err)
 {
+    // a bounded wait of the placement gave up (its records may be incomplete, and
+    // stale records may lie outside the bin): deposit nothing, the error stands
+    if (*(volatile unsigned *)err) return;
     using FS = FxShape<MAS, INTER>;
     constexpr int E = FS::E;
     extern __shared__ __align__(16) unsigned smw[];

@@ -100,4 +100,5 @@ class ParticlePk(object):
 
     def result(self, sums=None):
         s = (sums if sums is not None else self.sums).cpu().numpy()
+        _lib.check_device('ParticlePk')
         return PKL.finalize_pk(s, self.geom, self.BoxSize, self.dims, 1, cross=False)

@@ -50,3 +50,27 @@ def test_wait_runs_out_sets_error_word(lib):
         assert _error_word(lib, False) == 0
     finally:
         _error_word(lib, True)
+
+
+def test_error_word_stops_tiled_deposits_and_raises(lib):
+    """While the error word is set the tiled deposit leaves the grid as it was (its
+    placement's input may be incomplete), and MA with host results raises, reading
+    and clearing the word; the next call deposits normally."""
+    import numpy as np
+    import pylians_gb300.MAS_library as MASL
+    from pylians_gb300._lib import PylError
+    out = torch.full((1,), 7, dtype=torch.int32, device='cuda')
+    _error_word(lib, True)
+    try:
+        assert lib.pyl_wait_probe(16, 100000, ctypes.c_void_p(out.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        pos = (np.random.default_rng(3).random((2_000_000, 3)) * 100.0).astype(np.float32)
+        g = np.zeros((64, 64, 64), np.float32)
+        with pytest.raises(PylError, match='wait gave up'):
+            MASL.MA(pos, g, 100.0, 'NGP', strategy='tiled')
+        assert g.sum() == 0.0
+        assert _error_word(lib, False) == 0
+        MASL.MA(pos, g, 100.0, 'NGP', strategy='tiled')
+        assert g.sum() == 2_000_000
+    finally:
+        _error_word(lib, True)
