@@ -236,3 +236,36 @@ def test_pass_limit_sizes_the_workspace(lib):
         assert lib.pyl_ma_set_pass_limit(-1) == 0
     assert size(10 ** 6, 3, 64, 2, 2, 0) > size(4096, 3, 64, 2, 2, 0)
 
+
+
+def test_check_device_reads_clears_and_raises(monkeypatch):
+    """pylians_gb300._lib.check_device reads the device error word with reset = 1
+    and raises PylError when it was set; a failing read raises too (no GPU: a fake
+    library stands in for pyl_device_error)."""
+    from pylians_gb300 import _lib
+
+    class Fake:
+        def __init__(self, word, rc=0):
+            self.word, self.rc, self.calls = word, rc, []
+
+        def pyl_device_error(self, reset, out):
+            self.calls.append(reset)
+            ctypes.cast(out, ctypes.POINTER(ctypes.c_uint))[0] = self.word
+            return self.rc
+
+        def pyl_strerror(self, rc):
+            return b'CUDA error'
+
+        def pyl_last_error(self):
+            return b'no device'
+
+    fake = Fake(0)
+    monkeypatch.setattr(_lib, 'load', lambda: fake)
+    _lib.check_device('MA')
+    assert fake.calls == [1]
+    fake.word = 1
+    with pytest.raises(_lib.PylError, match='MA: a device-side wait gave up'):
+        _lib.check_device('MA')
+    fake.word, fake.rc = 0, _lib.PYL_ERR_CUDA
+    with pytest.raises(_lib.PylError, match='pyl_device_error'):
+        _lib.check_device('MA')
