@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(256) pk_bin_seq_kernel(BinArgs a, int chunk, u
 // sight along x for axis 0, y for axis 1), its warps the row representatives q
 // of the CTA's chunk; each (p, q) is the four sign rows of sign_rows.
 template <bool INTER, int AXIS, bool BATCH>
-__global__ void __launch_bounds__(256) pk_bin_sym_kernel(BinArgs a, int chunk, unsigned chunk_magic)
+__global__ void __launch_bounds__(256, INTER ? 3 : 4) pk_bin_sym_kernel(BinArgs a, int chunk, unsigned chunk_magic)
 {
     static_assert(AXIS == 0 || AXIS == 1, "axes 0 and 1");
     extern __shared__ float sm[];
